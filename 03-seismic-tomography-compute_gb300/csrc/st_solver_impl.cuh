@@ -1,0 +1,56 @@
+// Internal state of a solver handle, shared by the C-ABI translation units.
+#pragma once
+
+#include "st_kernels.cuh"
+
+#include <vector>
+
+struct st_solver {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    stg::Layout L{};
+    st_grid_params grid{};
+    st_solver_config cfg{};
+    double amp_limit = 1e10;
+    double cfl_safety = 0.49;
+    int max_repair_attempts = 3;
+    std::vector<double> vel_host;  // reference layout, authoritative velocity
+    float* f[3] = {nullptr, nullptr, nullptr};
+    int ic = 0, ip = 1, in = 2;
+    float* c = nullptr;
+    float* dtab = nullptr;
+    int sw = 0;
+    double* staging = nullptr;  // FP64 reference-layout buffer on the device
+    unsigned* flags = nullptr;
+    unsigned long long* counter = nullptr;
+    double* dsum = nullptr;
+    CUtensorMap map_cur[3];
+    CUtensorMap map_ctr[3];
+    CUtensorMap map_c;
+    bool coeff_dirty = true;
+    std::vector<float*> snapshots;  // save_snapshot: interior FP32 copies
+    st_fault_stats stats{};
+    bool cfl_warned = false;
+    // device scratch of the fused shot / RTM / gradient entry points
+    void* snap_buf = nullptr;       // forward snapshots (library-owned when the caller passes none)
+    size_t snap_cap = 0;
+    void* aux_buf = nullptr;        // seismograms / image accumulators / checkpoint states
+    size_t aux_cap = 0;
+    void* data_buf = nullptr;       // host-API staging of receiver data
+    size_t data_cap = 0;
+};
+
+
+namespace stg {
+int64_t ref_elems(const st_solver* s);
+int ensure_staging(st_solver* s);
+int refresh_coeff(st_solver* s);
+int read_flags(st_solver* s, unsigned* out);
+StepArgs base_args(st_solver* s, float* out);
+int fused_step(st_solver* s, StepArgs a, int snap_out, int snap_in, bool image);
+int zero_fields(st_solver* s);
+long long dev_index(const st_solver* s, int64_t ix, int64_t iy, int64_t iz);
+bool finite_sample(const double* w, int64_t len, int64_t t, float* out);
+// Device scratch owned by the handle, grown on demand.
+int ensure_buffer(st_solver* s, void** buf, size_t* cap, size_t bytes);
+}  // namespace stg

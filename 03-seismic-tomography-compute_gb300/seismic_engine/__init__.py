@@ -1,0 +1,16 @@
+"""seismic_engine — the GB300 (sm_103a) implementation of the hot path of
+13262233692/03-seismic-tomography-compute behind the reference's own Python
+module name and API (src/cpp/pybind/bindings.cpp:13-301), extended with the
+fused GPU shot, RTM, gradient and tomography-solve entry points.
+
+All compute runs in libseismic_gb300.so (CUDA, sm_103a) through its C ABI
+(include/seismic_gb300.h); there is no CPU fallback.
+"""
+from ._lib import SeismicError, load as load_library, lib_path  # noqa: F401
+from .wave import (  # noqa: F401
+    FaultStats, GridParams, HealthStatus, PropagationResult, SolverConfig, StepResult, WaveEquationSolver,
+    WaveField, field_layout, shot_forward, shot_forward_host,
+)
+from . import workloads  # noqa: F401
+
+__version__ = "1.2.0+gb300"

@@ -1,0 +1,155 @@
+"""Loader and ctypes signatures of the C ABI in include/seismic_gb300.h.
+
+The library is the in-tree build lib/libseismic_gb300.so (build.py). There is
+no fallback: when it is missing or fails to load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_ROOT, "lib", "libseismic_gb300.so")
+
+ST_OK = 0
+ST_NAN_DETECTED_AND_REPAIRED = 1
+ST_CFL_VIOLATION = 2
+ST_FATAL_DIVERGENCE = 3
+ST_ERR_ARG = -1
+ST_ERR_CUDA = -2
+ST_ERR_ALLOC = -3
+ST_ERR_STATE = -4
+ST_ERR_TIMEOUT = -5
+ST_ERR_UNSUPPORTED = -6
+
+ST_FIELD_CURRENT, ST_FIELD_PREVIOUS, ST_FIELD_NEXT, ST_FIELD_VELOCITY = 0, 1, 2, 3
+ST_SNAP_NONE, ST_SNAP_BF16, ST_SNAP_FP16, ST_SNAP_FP32, ST_SNAP_CHECKPOINT = 0, 1, 2, 3, 4
+
+
+class SeismicError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"seismic_gb300 error {code}: {msg}")
+        self.code = code
+
+
+class GridParams(C.Structure):
+    _fields_ = [("nx_global", C.c_int64), ("ny_global", C.c_int64), ("nz_global", C.c_int64),
+                ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+                ("origin_x", C.c_double), ("origin_y", C.c_double), ("origin_z", C.c_double),
+                ("halo_width", C.c_int)]
+
+
+class SolverConfigC(C.Structure):
+    _fields_ = [("frequency", C.c_double), ("dt", C.c_double), ("nt", C.c_int), ("water_depth", C.c_double),
+                ("seafloor_gradient", C.c_double), ("sponge_width", C.c_int), ("sponge_damping", C.c_double),
+                ("snapshot_interval", C.c_int)]
+
+
+class PropagationResultC(C.Structure):
+    _fields_ = [("status", C.c_int), ("total_nan_encountered", C.c_int64), ("total_cells_repaired", C.c_int64),
+                ("timesteps_completed", C.c_int), ("completed_successfully", C.c_int)]
+
+
+class FaultStatsC(C.Structure):
+    _fields_ = [("total_nan_count", C.c_int64), ("total_inf_count", C.c_int64), ("cells_repaired", C.c_int64),
+                ("timesteps_recovered", C.c_int64), ("global_abort_count", C.c_int)]
+
+
+class ReceiverGridC(C.Structure):
+    _fields_ = [("x0", C.c_int64), ("sx", C.c_int64), ("nx", C.c_int64),
+                ("y0", C.c_int64), ("sy", C.c_int64), ("ny", C.c_int64), ("z", C.c_int64)]
+
+
+class ShotC(C.Structure):
+    _fields_ = [("src_ix", C.c_int64), ("src_iy", C.c_int64), ("src_iz", C.c_int64),
+                ("wavelet", C.POINTER(C.c_double)), ("wavelet_len", C.c_int64), ("nt", C.c_int),
+                ("rec", ReceiverGridC)]
+
+
+_d = C.POINTER(C.c_double)
+_f = C.POINTER(C.c_float)
+_i64 = C.POINTER(C.c_int64)
+_vp = C.c_void_p
+
+# name -> argtypes (restype int unless listed in _RESTYPES)
+SIGNATURES = {
+    "st_last_error": [],
+    "st_version": [],
+    "st_device_count": [C.POINTER(C.c_int)],
+    "st_field_layout": [C.c_int64, C.c_int64, C.c_int64, _i64],
+    "st_solver_create": [C.POINTER(GridParams), C.POINTER(SolverConfigC), C.c_int, C.POINTER(_vp)],
+    "st_solver_destroy": [_vp],
+    "st_solver_initialize_velocity": [_vp, C.c_double],
+    "st_solver_set_velocity_field": [_vp, _d, C.c_int64],
+    "st_solver_inject_source": [_vp, C.c_int64, C.c_int64, C.c_int64, _d, C.c_int64],
+    "st_solver_step_forward": [_vp, C.c_int],
+    "st_solver_step_adjoint": [_vp, C.c_int],
+    "st_solver_forward_propagate": [_vp, _d, C.c_int64, C.POINTER(PropagationResultC)],
+    "st_solver_adjoint_propagate": [_vp, _d, C.c_int64, C.POINTER(PropagationResultC)],
+    "st_solver_reset_field": [_vp],
+    "st_solver_get_field": [_vp, C.c_int, _d, C.c_int64],
+    "st_solver_set_field": [_vp, C.c_int, _d, C.c_int64],
+    "st_solver_compute_energy": [_vp, _d],
+    "st_solver_verify_cfl": [_vp, C.POINTER(C.c_int)],
+    "st_solver_set_amplitude_limit": [_vp, C.c_double],
+    "st_solver_amplitude_limit": [_vp, _d],
+    "st_solver_nan_count_current": [_vp, _i64],
+    "st_solver_save_snapshot": [_vp, C.c_int],
+    "st_solver_clear_snapshots": [_vp],
+    "st_solver_snapshot_values": [_vp, _i64],
+    "st_solver_get_snapshots": [_vp, _d, C.c_int64],
+    "st_solver_fault_stats": [_vp, C.POINTER(FaultStatsC)],
+    "st_solver_device_field": [_vp, C.c_int, C.POINTER(_vp)],
+    "st_solver_stream": [_vp, C.POINTER(_vp)],
+    "st_shot_forward": [_vp, C.POINTER(ShotC), _vp, C.c_int, _vp, _vp],
+    "st_shot_forward_host": [_vp, _d, C.c_int64, C.POINTER(ShotC), _d],
+    "st_rtm_shot": [_vp, C.POINTER(ShotC), _vp, C.c_int, _vp, _vp, _vp, _vp, _vp],
+    "st_rtm_shot_host": [_vp, _d, C.c_int64, C.POINTER(ShotC), _f, C.c_int, _d, _d, _d],
+}
+_RESTYPES = {"st_last_error": C.c_char_p}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def lib_path() -> str:
+    return LIB_PATH
+
+
+def load(build_if_missing: bool = False):
+    """Returns the loaded CDLL. Raises when the library is missing."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            if build_if_missing:
+                import importlib.util
+                spec = importlib.util.spec_from_file_location("_st_build", os.path.join(PKG_ROOT, "build.py"))
+                mod = importlib.util.module_from_spec(spec)
+                spec.loader.exec_module(mod)
+                mod.build()
+            else:
+                raise ImportError(f"{LIB_PATH} is missing: build it with build.py (there is no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        for name, args in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = _RESTYPES.get(name, C.c_int)
+        _lib = L
+        return L
+
+
+def check(rc: int, allow_status: bool = False) -> int:
+    """Raises SeismicError for negative codes; returns StepResult codes."""
+    if rc < 0:
+        msg = load().st_last_error()
+        raise SeismicError(rc, msg.decode() if msg else "")
+    if rc > 0 and not allow_status:
+        return rc
+    return rc
+
+
+def call(name: str, *args, allow_status: bool = True) -> int:
+    return check(getattr(load(), name)(*args), allow_status=allow_status)

@@ -1,0 +1,293 @@
+"""Propagator face of seismic_engine: the reference's types and the
+WaveEquationSolver class (solver/wave_equation.h:16-144), plus the fused shot
+entry points that take torch device tensors without copies.
+
+Every call goes through libseismic_gb300.so; fields returned by `field()` are
+FP64 numpy arrays in the reference's halo-padded layout.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+from dataclasses import dataclass, field as dc_field
+
+import numpy as np
+
+from . import _lib
+from ._lib import call
+
+
+class StepResult(enum.IntEnum):
+    """seismic::StepResult (solver/wave_equation.h:24-29)."""
+    OK = 0
+    NAN_DETECTED_AND_REPAIRED = 1
+    CFL_VIOLATION = 2
+    FATAL_DIVERGENCE = 3
+
+
+class HealthStatus(enum.IntEnum):
+    """seismic::HealthStatus (core/fault_tolerance.h:13-20)."""
+    HEALTHY = 0
+    NAN_DETECTED = 1
+    INF_DETECTED = 2
+    CFL_VIOLATION = 3
+    DIVERGENCE = 4
+    COMM_FAILURE = 5
+
+
+@dataclass
+class GridParams:
+    """seismic::GridParams (core/grid.h:9-20)."""
+    nx_global: int
+    ny_global: int
+    nz_global: int
+    dx: float
+    dy: float
+    dz: float
+    origin_x: float = 0.0
+    origin_y: float = 0.0
+    origin_z: float = 0.0
+    halo_width: int = 1
+
+    def c(self) -> _lib.GridParams:
+        return _lib.GridParams(self.nx_global, self.ny_global, self.nz_global, self.dx, self.dy, self.dz,
+                               self.origin_x, self.origin_y, self.origin_z, self.halo_width)
+
+
+@dataclass
+class SolverConfig:
+    """seismic::SolverConfig (core/config.h:9-19), defaults of load_config
+    (core/config.cpp:12-20)."""
+    frequency: float = 2.0
+    dt: float = 0.001
+    nt: int = 5000
+    water_depth: float = 4000.0
+    seafloor_gradient: float = 0.05
+    sponge_width: int = 20
+    sponge_damping: float = 0.015
+    snapshot_interval: int = 100
+    output_dir: str = "./output"
+
+    def c(self) -> _lib.SolverConfigC:
+        return _lib.SolverConfigC(self.frequency, self.dt, self.nt, self.water_depth, self.seafloor_gradient,
+                                  self.sponge_width, self.sponge_damping, self.snapshot_interval)
+
+
+@dataclass
+class PropagationResult:
+    """seismic::PropagationResult (solver/wave_equation.h:31-37)."""
+    status: StepResult
+    total_nan_encountered: int
+    total_cells_repaired: int
+    timesteps_completed: int
+    completed_successfully: bool
+
+
+@dataclass
+class FaultStats:
+    """seismic::FaultTolerance::FaultStats (core/fault_tolerance.h:61-67)."""
+    total_nan_count: int = 0
+    total_inf_count: int = 0
+    cells_repaired: int = 0
+    timesteps_recovered: int = 0
+    global_abort_count: int = 0
+
+
+@dataclass
+class WaveField:
+    """seismic::WaveField (solver/wave_equation.h:16-22), FP64 host copies."""
+    current: np.ndarray
+    previous: np.ndarray
+    next: np.ndarray
+    velocity: np.ndarray
+    snapshots: np.ndarray = dc_field(default_factory=lambda: np.zeros(0))
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def field_layout(nx: int, ny: int, nz: int) -> dict:
+    out = (C.c_int64 * 6)()
+    call("st_field_layout", nx, ny, nz, out)
+    return dict(NXh=out[0], NYh=out[1], NZP=out[2], ZOFF=out[3], plane=out[4], elems=out[5])
+
+
+class WaveEquationSolver:
+    """seismic::WaveEquationSolver over the GPU library. The constructor takes
+    (grid, config) like the reference's (mpi, grid, config) minus the MPI
+    context: one device-resident domain, no halo exchange."""
+
+    def __init__(self, grid: GridParams, config: SolverConfig, device: int = 0):
+        self._grid = grid
+        self._cfg = config
+        h = C.c_void_p()
+        call("st_solver_create", C.byref(grid.c()), C.byref(config.c()), device, C.byref(h), allow_status=False)
+        self._h = h
+        self.nx, self.ny, self.nz = grid.nx_global, grid.ny_global, grid.nz_global
+        self.padded_size = (self.nx + 2) * (self.ny + 2) * (self.nz + 2)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.load().st_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def grid(self) -> GridParams:
+        return self._grid
+
+    def config(self) -> SolverConfig:
+        return self._cfg
+
+    # ---- reference API (wave_equation.h:57-110)
+    def initialize_velocity(self, vp0: float):
+        call("st_solver_initialize_velocity", self._h, float(vp0))
+
+    def set_velocity_field(self, vp, count: int | None = None):
+        a = np.ascontiguousarray(vp, dtype=np.float64).reshape(-1)
+        n = a.size if count is None else int(count)
+        call("st_solver_set_velocity_field", self._h, _dptr(a), min(n, a.size))
+
+    def inject_source(self, ix: int, iy: int, iz: int, wavelet):
+        w = np.ascontiguousarray(wavelet, dtype=np.float64).reshape(-1)
+        if w.size == 0:
+            return
+        call("st_solver_inject_source", self._h, ix, iy, iz, _dptr(w), w.size)
+
+    def step_forward(self, timestep: int) -> StepResult:
+        return StepResult(call("st_solver_step_forward", self._h, timestep))
+
+    def step_adjoint(self, timestep: int) -> StepResult:
+        return StepResult(call("st_solver_step_adjoint", self._h, timestep))
+
+    def _prop(self, name, w):
+        w = np.ascontiguousarray(w, dtype=np.float64).reshape(-1)
+        if w.size == 0:
+            w = np.zeros(1)
+            n = 0
+        else:
+            n = w.size
+        r = _lib.PropagationResultC()
+        call(name, self._h, _dptr(w), n, C.byref(r))
+        return PropagationResult(StepResult(r.status), r.total_nan_encountered, r.total_cells_repaired,
+                                 r.timesteps_completed, bool(r.completed_successfully))
+
+    def forward_propagate(self, wavelet) -> PropagationResult:
+        return self._prop("st_solver_forward_propagate", wavelet)
+
+    def adjoint_propagate(self, residual_wavelet) -> PropagationResult:
+        return self._prop("st_solver_adjoint_propagate", residual_wavelet)
+
+    def reset_field(self):
+        call("st_solver_reset_field", self._h)
+
+    def get_field(self, which: int) -> np.ndarray:
+        out = np.empty(self.padded_size)
+        call("st_solver_get_field", self._h, which, _dptr(out), out.size)
+        return out
+
+    def set_field(self, which: int, values):
+        a = np.ascontiguousarray(values, dtype=np.float64).reshape(-1)
+        call("st_solver_set_field", self._h, which, _dptr(a), a.size)
+
+    def field(self) -> WaveField:
+        return WaveField(self.get_field(_lib.ST_FIELD_CURRENT), self.get_field(_lib.ST_FIELD_PREVIOUS),
+                         self.get_field(_lib.ST_FIELD_NEXT), self.get_field(_lib.ST_FIELD_VELOCITY),
+                         self.snapshots())
+
+    def snapshots(self) -> np.ndarray:
+        n = C.c_int64()
+        call("st_solver_snapshot_values", self._h, C.byref(n))
+        out = np.empty(n.value)
+        if n.value:
+            call("st_solver_get_snapshots", self._h, _dptr(out), out.size)
+        return out
+
+    def save_snapshot(self, timestep: int):
+        call("st_solver_save_snapshot", self._h, timestep)
+
+    def clear_snapshots(self):
+        call("st_solver_clear_snapshots", self._h)
+
+    def compute_energy(self) -> float:
+        e = C.c_double()
+        call("st_solver_compute_energy", self._h, C.byref(e))
+        return e.value
+
+    def verify_cfl(self) -> bool:
+        ok = C.c_int()
+        call("st_solver_verify_cfl", self._h, C.byref(ok))
+        return bool(ok.value)
+
+    def set_amplitude_limit(self, limit: float):
+        call("st_solver_set_amplitude_limit", self._h, float(limit))
+
+    def amplitude_limit(self) -> float:
+        v = C.c_double()
+        call("st_solver_amplitude_limit", self._h, C.byref(v))
+        return v.value
+
+    def nan_count_current(self) -> int:
+        v = C.c_int64()
+        call("st_solver_nan_count_current", self._h, C.byref(v))
+        return v.value
+
+    def fault_stats(self) -> FaultStats:
+        s = _lib.FaultStatsC()
+        call("st_solver_fault_stats", self._h, C.byref(s))
+        return FaultStats(s.total_nan_count, s.total_inf_count, s.cells_repaired, s.timesteps_recovered,
+                          s.global_abort_count)
+
+    # ---- GB300 additions
+    def device_field_ptr(self, which: int) -> int:
+        p = C.c_void_p()
+        call("st_solver_device_field", self._h, which, C.byref(p))
+        return p.value
+
+    def stream_ptr(self) -> int:
+        p = C.c_void_p()
+        call("st_solver_stream", self._h, C.byref(p))
+        return p.value or 0
+
+
+def _shot_c(src, wavelet: np.ndarray, nt: int, rec):
+    w = np.ascontiguousarray(wavelet, dtype=np.float64).reshape(-1)
+    rc = _lib.ReceiverGridC(rec.x0, rec.sx, rec.nx, rec.y0, rec.sy, rec.ny, rec.z) if rec is not None \
+        else _lib.ReceiverGridC(0, 1, 0, 0, 1, 0, 0)
+    shot = _lib.ShotC(int(src[0]), int(src[1]), int(src[2]), _dptr(w), w.size, int(nt), rc)
+    return shot, w
+
+
+def shot_forward(solver: WaveEquationSolver, src, wavelet, nt: int, rec, seis=None, snap_kind: int = 0,
+                 snaps=None, snap_amax=None) -> int:
+    """Fused forward shot on the solver's stream. seis / snaps / snap_amax are
+    torch CUDA tensors (or None); returns the StepResult code."""
+    shot, _keep = _shot_c(src, wavelet, nt, rec)
+    sp = seis.data_ptr() if seis is not None else None
+    snp = snaps.data_ptr() if snaps is not None else None
+    amp = snap_amax.data_ptr() if snap_amax is not None else None
+    return call("st_shot_forward", solver.handle, C.byref(shot), sp, snap_kind, snp, amp)
+
+
+def shot_forward_host(solver: WaveEquationSolver, vel_ref, src, wavelet, nt: int, rec) -> np.ndarray:
+    """Host-buffer forward shot (all copies included): velocity in the
+    reference layout (or None), returns FP64 seismograms [nt, nrec]."""
+    shot, _keep = _shot_c(src, wavelet, nt, rec)
+    nrec = rec.nx * rec.ny if rec is not None else 0
+    out = np.zeros((nt, max(nrec, 1)))
+    if vel_ref is None:
+        vp, n = C.cast(None, C.POINTER(C.c_double)), 0
+    else:
+        v = np.ascontiguousarray(vel_ref, dtype=np.float64).reshape(-1)
+        vp, n = _dptr(v), v.size
+    call("st_shot_forward_host", solver.handle, vp, n, C.byref(shot), _dptr(out))
+    return out[:, :nrec]

@@ -1,0 +1,189 @@
+"""Seeded synthetic inputs of the benchmark workloads: layered velocity models
+with Gaussian anomalies, the CFL time-step rule, the Ricker wavelet and the
+surface receiver grids. There is no public dataset for this path; these
+generators stand in for field data with the stated shapes and value ranges.
+
+Velocity arrays are (nx, ny, nz) with z as depth (z fastest, the reference's
+index order, core/grid.cpp:45-49); `to_reference_layout` pads them to the
+reference's halo-padded layout with edge values.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+
+def ricker(f0: float, dt: float, nt: int, t0: float | None = None) -> np.ndarray:
+    """w(t) = (1 - 2 pi^2 f0^2 tau^2) exp(-pi^2 f0^2 tau^2), tau = n dt - t0,
+    t0 = 1.2 / f0 by default."""
+    t0 = 1.2 / f0 if t0 is None else t0
+    tau = np.arange(nt) * dt - t0
+    a = (math.pi * f0 * tau) ** 2
+    return (1.0 - 2.0 * a) * np.exp(-a)
+
+
+def cfl_dt(d: float, vmax: float, courant: float = 0.45) -> float:
+    """dt = floor_1e-6(courant * d / vmax); the reference accepts
+    vmax dt / d <= 0.49 per axis (core/fault_tolerance.cpp:49-70)."""
+    return math.floor(courant * d / vmax * 1e6) / 1e6
+
+
+def layered(nx: int, ny: int, nz: int, velocities) -> np.ndarray:
+    """Equal-thickness horizontal layers along z (depth)."""
+    v = np.empty((nx, ny, nz), np.float64)
+    L = len(velocities)
+    bounds = [int(math.ceil(k * nz / L)) for k in range(L + 1)]
+    for k, vel in enumerate(velocities):
+        v[:, :, bounds[k]:bounds[k + 1]] = vel
+    return v
+
+
+def add_gaussian(v: np.ndarray, centre, amp: float, sigma: float) -> np.ndarray:
+    """v *= 1 + amp exp(-r^2 / (2 sigma^2)) around centre (cell units)."""
+    nx, ny, nz = v.shape
+    x = np.arange(nx)[:, None, None] - centre[0]
+    y = np.arange(ny)[None, :, None] - centre[1]
+    z = np.arange(nz)[None, None, :] - centre[2]
+    v *= 1.0 + amp * np.exp(-(x * x + y * y + z * z) / (2.0 * sigma * sigma))
+    return v
+
+
+def random_anomalies(v: np.ndarray, count: int, seed: int, amp: float = 0.10, sigma: float = 8.0):
+    """`count` anomalies with centres uniform in the central 50% of each axis
+    and amplitude +-amp (random sign)."""
+    rng = np.random.default_rng(seed)
+    n = np.array(v.shape)
+    for _ in range(count):
+        c = rng.uniform(0.25 * n, 0.75 * n)
+        s = 1.0 if rng.random() < 0.5 else -1.0
+        add_gaussian(v, c, s * amp, sigma)
+    return v
+
+
+def smooth(v: np.ndarray, sigma: float) -> np.ndarray:
+    from scipy.ndimage import gaussian_filter
+    return gaussian_filter(v, sigma=sigma, mode="nearest")
+
+
+def to_reference_layout(v: np.ndarray) -> np.ndarray:
+    """(nx,ny,nz) interior -> flat (nx+2)*(ny+2)*(nz+2) padded array (edge halo)."""
+    return np.ascontiguousarray(np.pad(v, 1, mode="edge")).reshape(-1)
+
+
+@dataclass
+class ReceiverGrid:
+    """Receiver q = irx*ny + iry at (x0 + irx*sx, y0 + iry*sy, z)."""
+    x0: int
+    sx: int
+    nx: int
+    y0: int
+    sy: int
+    ny: int
+    z: int
+
+    @property
+    def count(self) -> int:
+        return self.nx * self.ny
+
+    def coords(self) -> np.ndarray:
+        ix = self.x0 + self.sx * np.arange(self.nx)
+        iy = self.y0 + self.sy * np.arange(self.ny)
+        X, Y = np.meshgrid(ix, iy, indexing="ij")
+        return np.stack([X.ravel(), Y.ravel(), np.full(X.size, self.z)], axis=1).astype(np.int64)
+
+
+@dataclass
+class ShotSpec:
+    src: tuple
+    wavelet: np.ndarray
+    rec: ReceiverGrid
+
+
+@dataclass
+class Workload:
+    name: str
+    nx: int
+    ny: int
+    nz: int
+    d: float
+    dt: float
+    nt: int
+    vel: np.ndarray          # (nx,ny,nz) true model
+    shots: list
+    sponge_width: int = 20
+    sponge_damping: float = 0.015
+    vel_migration: np.ndarray | None = None
+
+    @property
+    def points(self) -> int:
+        return self.nx * self.ny * self.nz
+
+
+def forward_128(nt: int = 1000) -> Workload:
+    """128^3 forward modelling: 3 layers 1500/2500/3500 m/s, +10% Gaussian
+    anomaly (sigma 8 cells) at the centre, 15 Hz Ricker at (64,64,5), 64x64
+    receivers every 2nd cell on z = 5."""
+    n = 128
+    v = layered(n, n, n, [1500.0, 2500.0, 3500.0])
+    add_gaussian(v, (64, 64, 64), 0.10, 8.0)
+    dt = cfl_dt(10.0, 3500.0)
+    rec = ReceiverGrid(0, 2, 64, 0, 2, 64, 5)
+    return Workload("forward-128^3", n, n, n, 10.0, dt, nt, v, [ShotSpec((64, 64, 5), ricker(15.0, dt, nt), rec)])
+
+
+def rtm_256(nt: int = 2000) -> Workload:
+    """256^3 single-shot RTM: 4 layers 1500..4500 m/s, two seeded (seed 2)
+    +-10% anomalies, source (128,128,5), 128x128 receivers every 2nd cell on
+    z = 5, migration velocity = true model smoothed with sigma 6 cells."""
+    n = 256
+    v = layered(n, n, n, [1500.0, 2500.0, 3500.0, 4500.0])
+    random_anomalies(v, 2, seed=2)
+    vmax = float(v.max())
+    dt = cfl_dt(10.0, vmax)
+    rec = ReceiverGrid(0, 2, 128, 0, 2, 128, 5)
+    w = Workload("rtm-256^3", n, n, n, 10.0, dt, nt, v, [ShotSpec((128, 128, 5), ricker(15.0, dt, nt), rec)])
+    return w
+
+
+def fwi_192(nt: int = 1500) -> Workload:
+    """192^3 FWI: 4 layers + 2 seeded (seed 3) anomalies; 4 shots on a 2x2
+    surface grid; start model = true model smoothed with sigma 6 cells."""
+    n = 192
+    v = layered(n, n, n, [1500.0, 2500.0, 3500.0, 4500.0])
+    random_anomalies(v, 2, seed=3)
+    dt = cfl_dt(10.0, float(v.max()))
+    rec = ReceiverGrid(0, 2, 96, 0, 2, 96, 5)
+    w = ricker(15.0, dt, nt)
+    shots = [ShotSpec((sx, sy, 5), w, rec) for sx in (64, 128) for sy in (64, 128)]
+    return Workload("fwi-192^3", n, n, n, 10.0, dt, nt, v, shots)
+
+
+def large_512(nt: int = 4000) -> Workload:
+    """512^3: 6 layers 1500..5000 m/s + 6 seeded (seed 5) anomalies, 20 Hz
+    Ricker, 8 shots on a 2x4 surface grid at z = 5, 256x256 receivers."""
+    n = 512
+    v = layered(n, n, n, list(np.linspace(1500.0, 5000.0, 6)))
+    random_anomalies(v, 6, seed=5)
+    dt = cfl_dt(10.0, float(v.max()))
+    rec = ReceiverGrid(0, 2, 256, 0, 2, 256, 5)
+    w = ricker(20.0, dt, nt)
+    shots = [ShotSpec((int(sx), int(sy), 5), w, rec) for sx in (170, 341) for sy in (102, 204, 307, 409)]
+    return Workload("large-512^3", n, n, n, 10.0, dt, nt, v, shots)
+
+
+def small_case(n=(24, 20, 28), nt: int = 80, seed: int = 7, sponge_width: int = 6) -> Workload:
+    """Small seeded case for parity tests (the oracle finishes it in
+    milliseconds): 2 layers + one anomaly, Ricker at the upper centre,
+    receivers every 3rd cell on z = 3."""
+    nx, ny, nz = n
+    v = layered(nx, ny, nz, [1500.0, 2400.0])
+    rng = np.random.default_rng(seed)
+    add_gaussian(v, (nx / 2, ny / 2, nz / 2), 0.1, 3.0)
+    v *= 1.0 + 0.02 * rng.standard_normal(v.shape)
+    dt = cfl_dt(10.0, float(v.max()))
+    rec = ReceiverGrid(1, 3, (nx - 2) // 3, 1, 3, (ny - 2) // 3, 3)
+    w = ricker(25.0, dt, nt)
+    return Workload("small", nx, ny, nz, 10.0, dt, nt, v,
+                    [ShotSpec((nx // 2, ny // 2, 4), w, rec)], sponge_width=sponge_width)

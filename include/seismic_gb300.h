@@ -1,0 +1,206 @@
+/*
+ * seismic_gb300 — C ABI of the GB300 (sm_103a) implementation of the seismic
+ * hot path of 13262233692/03-seismic-tomography-compute: the 3-D acoustic
+ * finite-difference propagator, its exact adjoint and RTM imaging, and the
+ * CSR SpMV / CG tomography solve.
+ *
+ * Conventions
+ *  - Every function returns int: 0 = ST_OK; 1..3 mirror seismic::StepResult
+ *    (solver/wave_equation.h:24-29); negative values are errors, and
+ *    st_last_error() gives the message for the calling thread.
+ *  - "Reference layout": the reference's halo-padded FP64 field of
+ *    (nx+2)*(ny+2)*(nz+2) doubles, idx = ix*NYh*NZh + iy*NZh + iz
+ *    (core/grid.cpp:45-49). Host entry points take and return that layout.
+ *  - "Device layout": FP32, x/y halo 1, z interior starting at column 4 of a
+ *    row of NZP floats (st_field_layout). Device entry points take device
+ *    pointers in that layout and a cudaStream_t passed as void*.
+ *  - Handles own their device memory; caller buffers are borrowed for the
+ *    duration of a call. One handle per host thread (the reference runs
+ *    MPI_THREAD_FUNNELED, core/mpi_context.cpp:10); work is ordered on the
+ *    handle's stream and host-visible results synchronise.
+ */
+#ifndef SEISMIC_GB300_H
+#define SEISMIC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum st_status {
+    ST_OK = 0,
+    ST_NAN_DETECTED_AND_REPAIRED = 1, /* StepResult::NAN_DETECTED_AND_REPAIRED */
+    ST_CFL_VIOLATION = 2,             /* StepResult::CFL_VIOLATION */
+    ST_FATAL_DIVERGENCE = 3,          /* StepResult::FATAL_DIVERGENCE */
+    ST_ERR_ARG = -1,
+    ST_ERR_CUDA = -2,
+    ST_ERR_ALLOC = -3,
+    ST_ERR_STATE = -4,
+    ST_ERR_TIMEOUT = -5,
+    ST_ERR_UNSUPPORTED = -6
+};
+
+/* Which field of WaveEquationSolver::field() (wave_equation.h:16-22). */
+enum st_field_id { ST_FIELD_CURRENT = 0, ST_FIELD_PREVIOUS = 1, ST_FIELD_NEXT = 2, ST_FIELD_VELOCITY = 3 };
+
+/* Storage of forward snapshots for RTM / gradients. */
+enum st_snap_kind { ST_SNAP_NONE = 0, ST_SNAP_BF16 = 1, ST_SNAP_FP16 = 2, ST_SNAP_FP32 = 3, ST_SNAP_CHECKPOINT = 4 };
+
+/* seismic::GridParams (core/grid.h:9-20). halo_width must be 1 (7-point stencil). */
+typedef struct st_grid_params {
+    int64_t nx_global, ny_global, nz_global;
+    double dx, dy, dz;
+    double origin_x, origin_y, origin_z;
+    int halo_width;
+} st_grid_params;
+
+/* seismic::SolverConfig (core/config.h:9-19) without output_dir. */
+typedef struct st_solver_config {
+    double frequency;
+    double dt;
+    int nt;
+    double water_depth;
+    double seafloor_gradient;
+    int sponge_width;
+    double sponge_damping;
+    int snapshot_interval;
+} st_solver_config;
+
+/* seismic::PropagationResult (wave_equation.h:31-37). */
+typedef struct st_propagation_result {
+    int status;
+    int64_t total_nan_encountered;
+    int64_t total_cells_repaired;
+    int timesteps_completed;
+    int completed_successfully;
+} st_propagation_result;
+
+/* seismic::FaultTolerance::FaultStats (core/fault_tolerance.h:61-67). */
+typedef struct st_fault_stats {
+    int64_t total_nan_count;
+    int64_t total_inf_count;
+    int64_t cells_repaired;
+    int64_t timesteps_recovered;
+    int global_abort_count;
+} st_fault_stats;
+
+/* Receivers on a regular grid of one z-plane (interior coordinates):
+ * receiver q = irx*ny + iry sits at (x0 + irx*sx, y0 + iry*sy, z). */
+typedef struct st_receiver_grid {
+    int64_t x0, sx, nx;
+    int64_t y0, sy, ny;
+    int64_t z;
+} st_receiver_grid;
+
+/* One shot: a point source (interior coordinates) with an nt-sample wavelet
+ * on the host, injected raw into the current field before each step as
+ * inject_source does (wave_equation.cpp:39-54), and a receiver grid. */
+typedef struct st_shot {
+    int64_t src_ix, src_iy, src_iz;
+    const double* wavelet; /* host, nt values (fewer: missing samples are 0) */
+    int64_t wavelet_len;
+    int nt;
+    st_receiver_grid rec;
+} st_shot;
+
+typedef struct st_solver st_solver;
+
+/* ---------------------------------------------------------------- library */
+const char* st_last_error(void);
+int st_version(void);
+int st_device_count(int* count);
+
+/* Device layout of an nx*ny*nz interior: out = {NXh, NYh, NZP, ZOFF, plane, elems}. */
+int st_field_layout(int64_t nx, int64_t ny, int64_t nz, int64_t out[6]);
+
+/* ------------------------------------------ seismic::WaveEquationSolver face */
+/* Replaces WaveEquationSolver::WaveEquationSolver (wave_equation.cpp:10-23). */
+int st_solver_create(const st_grid_params* grid, const st_solver_config* cfg, int device, st_solver** out);
+/* Replaces ~WaveEquationSolver (wave_equation.cpp:25-27). */
+int st_solver_destroy(st_solver* s);
+/* Replaces initialize_velocity (wave_equation.cpp:29-31). */
+int st_solver_initialize_velocity(st_solver* s, double vp0);
+/* Replaces set_velocity_field (wave_equation.cpp:33-37): linear copy of
+ * min(count, padded size) values into the reference-layout velocity. */
+int st_solver_set_velocity_field(st_solver* s, const double* vp, int64_t count);
+/* Replaces inject_source (wave_equation.cpp:39-54): current[pad(ix,iy,iz)] += wavelet[0]
+ * unless non-finite or out of the padded array. */
+int st_solver_inject_source(st_solver* s, int64_t ix, int64_t iy, int64_t iz, const double* wavelet, int64_t len);
+/* Replace step_forward / step_adjoint (wave_equation.cpp:56-98); return StepResult. */
+int st_solver_step_forward(st_solver* s, int timestep);
+int st_solver_step_adjoint(st_solver* s, int timestep);
+/* Replace forward_propagate / adjoint_propagate (wave_equation.cpp:100-194). */
+int st_solver_forward_propagate(st_solver* s, const double* wavelet, int64_t len, st_propagation_result* out);
+int st_solver_adjoint_propagate(st_solver* s, const double* residual, int64_t len, st_propagation_result* out);
+/* Replaces reset_field (wave_equation.cpp:501-506). */
+int st_solver_reset_field(st_solver* s);
+/* field() / mutable_field() (wave_equation.h:72-73) in the reference layout. */
+int st_solver_get_field(st_solver* s, int which, double* out, int64_t count);
+int st_solver_set_field(st_solver* s, int which, const double* in, int64_t count);
+/* Replaces compute_energy (wave_equation.cpp:482-490): FP64 sum of squares of finite current values. */
+int st_solver_compute_energy(st_solver* s, double* out);
+/* Replaces verify_cfl (wave_equation.cpp:445-451). */
+int st_solver_verify_cfl(st_solver* s, int* ok);
+/* Replace set_amplitude_limit / amplitude_limit (wave_equation.cpp:453-456, .h:90). */
+int st_solver_set_amplitude_limit(st_solver* s, double limit);
+int st_solver_amplitude_limit(st_solver* s, double* out);
+/* Replaces nan_count_current (wave_equation.cpp:458-461). */
+int st_solver_nan_count_current(st_solver* s, int64_t* out);
+/* Replace save_snapshot / clear_snapshots / field().snapshots (wave_equation.cpp:463-480, .h:78). */
+int st_solver_save_snapshot(st_solver* s, int timestep);
+int st_solver_clear_snapshots(st_solver* s);
+int st_solver_snapshot_values(st_solver* s, int64_t* count);
+int st_solver_get_snapshots(st_solver* s, double* out, int64_t count);
+/* Replaces fault_stats (wave_equation.h:94). */
+int st_solver_fault_stats(st_solver* s, st_fault_stats* out);
+
+/* ----------------------------------------------------- GB300 shot entry points */
+/* Device pointers to the solver's fields in the device layout (for zero-copy
+ * torch views): which = ST_FIELD_*. */
+int st_solver_device_field(st_solver* s, int which, float** out);
+/* The CUDA stream the handle orders its work on (a cudaStream_t). */
+int st_solver_stream(st_solver* s, void** out);
+
+/* Forward modelling of one shot, one fused kernel launch per step: leapfrog
+ * update, sponge, source injection, receiver sampling and (snap_kind != NONE)
+ * snapshot store of the post-injection field V_t of every step t.
+ *   seis:  device FP32 [nt][nrec], nrec = rec.nx*rec.ny
+ *   snaps: device buffer of nt * nx*ny*nz values of snap_kind (NULL if NONE)
+ *   snap_amax: device uint32 [nt+1] (float bits of per-snapshot |max|), NULL if NONE
+ * The solver's fields are reset first and hold the final state on return. */
+int st_shot_forward(st_solver* s, const st_shot* shot, float* seis, int snap_kind, void* snaps,
+                    unsigned* snap_amax);
+
+/* Host-buffer convenience around st_shot_forward: velocity in the reference
+ * layout (FP64, may be NULL to keep the current model), seismograms returned
+ * as FP64 [nt][nrec] on the host. Includes all host<->device copies. */
+int st_shot_forward_host(st_solver* s, const double* vp, int64_t vp_count, const st_shot* shot, double* seis_host);
+
+/* Reverse-time migration of one shot with the exact discrete adjoint: forward
+ * pass storing every post-injection field V_t (snap_kind BF16/FP16/FP32 with
+ * a per-snapshot scale), backward pass of lambda (the transpose of the
+ * forward step) forced by the receiver data, with the zero-lag
+ * cross-correlation of RTMEngine::apply_image_condition fused in
+ * (image += V_t*lambda_t, illum += V_t^2; rtm/rtm_engine.cpp:24-57) and
+ * finalize_image (:170-182) into refl when refl != NULL.
+ *   data: device FP32 [nt][nrec] receiver data
+ *   snaps/snap_amax: device buffers as in st_shot_forward, or NULL to use
+ *     library-owned ones (kept by the handle between calls)
+ *   image/illum/refl: device FP32, nx*ny*nz interior values (x slowest).
+ * Replaces the imaging of run_rtm (solver/wave_equation.cpp:621-688). */
+int st_rtm_shot(st_solver* s, const st_shot* shot, const float* data, int snap_kind, void* snaps,
+                unsigned* snap_amax, float* image, float* illum, float* refl);
+
+/* Host-buffer RTM with every copy included: velocity in the reference layout
+ * (FP64, NULL keeps the model), receiver data FP32 [nt][nrec] on the host,
+ * image / illumination / reflectivity returned as FP64 interior arrays (any
+ * may be NULL). The RTMImageCondition of rtm/rtm_engine.h:25-29. */
+int st_rtm_shot_host(st_solver* s, const double* vp, int64_t vp_count, const st_shot* shot, const float* data_host,
+                     int snap_kind, double* image_host, double* illum_host, double* refl_host);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SEISMIC_GB300_H */

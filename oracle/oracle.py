@@ -1,0 +1,369 @@
+"""ctypes front end of the CPU oracle (oracle/seismic_oracle.c) and of the
+reference build (oracle/_ref/libseismic_ref.so, present only where the
+reference sources were available at build time).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU legs of bench.py, as the checker or the timed CPU baseline. The product
+package never imports this module.
+
+Field layout everywhere: the reference's halo-padded array of
+(nx+2)*(ny+2)*(nz+2) values, x slowest, z fastest (core/grid.cpp:45-49).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libseismic_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libseismic_ref.so")
+
+_d = C.POINTER(C.c_double)
+_f = C.POINTER(C.c_float)
+_i64 = C.POINTER(C.c_int64)
+_i32 = C.POINTER(C.c_int)
+
+
+class OrcGrid(C.Structure):
+    _fields_ = [("nx", C.c_int64), ("ny", C.c_int64), ("nz", C.c_int64),
+                ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double), ("dt", C.c_double),
+                ("sponge_width", C.c_int), ("sponge_damping", C.c_double),
+                ("amp_limit", C.c_double), ("cfl_safety", C.c_double)]
+
+
+def build_oracle(force: bool = False) -> str:
+    """Compile the C oracle (plain gcc, OpenMP, no fast-math, no FMA
+    contraction so x86 and Arm give the same FP64 bits)."""
+    src = os.path.join(HERE, "seismic_oracle.c")
+    hdr = os.path.join(HERE, "oracle_prop.h")
+    if (not force and os.path.exists(ORACLE_SO)
+            and os.path.getmtime(ORACLE_SO) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
+        return ORACLE_SO
+    os.makedirs(os.path.dirname(ORACLE_SO), exist_ok=True)
+    tmp = ORACLE_SO + f".tmp{os.getpid()}"
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
+                           src, "-o", tmp, "-lm"])
+    os.replace(tmp, ORACLE_SO)
+    return ORACLE_SO
+
+
+def build_ref() -> str | None:
+    """Build oracle/_ref from the reference sources when they are present."""
+    subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh")])
+    return REF_SO if os.path.exists(REF_SO) else None
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+class Oracle:
+    def __init__(self):
+        self.lib = C.CDLL(build_oracle())
+        L = self.lib
+        for pre, ptr in (("orc64", _d), ("orc32", _f)):
+            fn = getattr(L, pre + "_run")
+            fn.argtypes = [C.POINTER(OrcGrid), ptr, C.c_int, C.c_int, _i64, ptr, C.c_int, _i64, ptr,
+                           _i32, ptr, ptr, ptr, ptr, ptr]
+            fn.restype = C.c_int
+        L.orc64_adjoint.argtypes = [C.POINTER(OrcGrid), _d, C.c_int, C.c_int, _i64, _d, C.c_int, _i64, _d,
+                                    _d, _d, _d, _d]
+        L.orc64_adjoint.restype = C.c_int
+        L.orc64_rtm_image.argtypes = [C.c_int64, C.c_int64, C.c_int64, C.c_int, _d, _d, _d, _d, _d]
+        L.orc_csr_build.argtypes = [C.c_int64, C.c_int64, C.c_int64, _i64, _i64, _d, C.c_int]
+        L.orc_csr_build.restype = C.c_void_p
+        L.orc_csr_free.argtypes = [C.c_void_p]
+        L.orc_csr_nnz.argtypes = [C.c_void_p]
+        L.orc_csr_nnz.restype = C.c_int64
+        L.orc_csr_copy.argtypes = [C.c_void_p, _i64, _i64, _d]
+        L.orc_csr_wrap.argtypes = [C.c_int64, C.c_int64, _i64, _i64, _d]
+        L.orc_csr_wrap.restype = C.c_void_p
+        L.orc_csr_unwrap.argtypes = [C.c_void_p]
+        L.orc_spmv.argtypes = [C.c_void_p, _d, _d]
+        L.orc_spmv_t.argtypes = [C.c_void_p, _d, _d]
+        L.orc_dot.argtypes = [_d, _d, C.c_int64]
+        L.orc_dot.restype = C.c_double
+        L.orc_cg.argtypes = [C.c_void_p, _d, C.c_int, C.c_double, C.c_int, _d, _d]
+        L.orc_cg.restype = C.c_int
+        L.orc_normal_cg.argtypes = [C.c_void_p, _d, C.c_double, C.c_int, C.c_double, C.c_int, _d, _d, _d]
+        L.orc_normal_cg.restype = C.c_int
+        L.orc_normal_apply.argtypes = [C.c_void_p, C.c_double, _d, _d]
+        L.orc_smooth_gradient.argtypes = [_d, C.c_int64, C.c_int64, C.c_int64, C.c_double, _d]
+        L.orc_num_threads.restype = C.c_int
+        L.orc64_repair_field_nan.argtypes = [_d, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int, C.c_double]
+        L.orc64_repair_field_nan.restype = C.c_int64
+        L.orc64_clamp_field.argtypes = [_d, C.c_int64, C.c_double, C.c_double]
+        L.orc64_count_nan_inf.argtypes = [_d, C.c_int64]
+        L.orc64_count_nan_inf.restype = C.c_int64
+
+    # ------------------------------------------------------------ propagator
+    @staticmethod
+    def grid(nx, ny, nz, dx, dy, dz, dt, sponge_width=20, sponge_damping=0.015, amp_limit=1e10):
+        return OrcGrid(nx, ny, nz, dx, dy, dz, dt, sponge_width, sponge_damping, amp_limit, 0.49)
+
+    def run(self, g: OrcGrid, vel, nsteps, src_xyz, src_w, rec_xyz, fp32=False, keep_states=False,
+            init_cur=None, init_prev=None):
+        """Reference stepping (inject, step, sample) in FP64 or FP32, from zero
+        fields or from init_cur / init_prev (reference layout).
+        Returns dict(seis [nsteps,nrec], status [nsteps], cur, prev, states)."""
+        dt = np.float32 if fp32 else np.float64
+        ptr = _f if fp32 else _d
+        npad = (g.nx + 2) * (g.ny + 2) * (g.nz + 2)
+        vel = np.ascontiguousarray(vel, dtype=dt).reshape(-1)
+        assert vel.size == npad
+        src_xyz = np.ascontiguousarray(src_xyz, dtype=np.int64).reshape(-1, 3)
+        rec_xyz = np.ascontiguousarray(rec_xyz, dtype=np.int64).reshape(-1, 3)
+        ns, nr = src_xyz.shape[0], rec_xyz.shape[0]
+        src_w = np.ascontiguousarray(src_w, dtype=dt).reshape(nsteps, ns)
+        seis = np.zeros((nsteps, max(nr, 1)), dt)
+        st = np.zeros(nsteps, np.int32)
+        cur = np.zeros(npad, dt)
+        prev = np.zeros(npad, dt)
+        states = np.zeros((nsteps, npad), dt) if keep_states else None
+        fn = self.lib.orc32_run if fp32 else self.lib.orc64_run
+        nul = C.cast(None, ptr)
+        ic = None if init_cur is None else np.ascontiguousarray(init_cur, dtype=dt).reshape(-1)
+        ip = None if init_prev is None else np.ascontiguousarray(init_prev, dtype=dt).reshape(-1)
+        rc = fn(C.byref(g), _p(vel, ptr), nsteps, ns, _p(src_xyz, _i64), _p(src_w, ptr), nr, _p(rec_xyz, _i64),
+                _p(seis, ptr), _p(st, _i32), _p(cur, ptr), _p(prev, ptr),
+                _p(states, ptr) if states is not None else nul,
+                _p(ic, ptr) if ic is not None else nul, _p(ip, ptr) if ip is not None else nul)
+        assert rc == 0, rc
+        return dict(seis=seis[:, :nr], status=st, cur=cur, prev=prev, states=states)
+
+    def adjoint(self, g: OrcGrid, vel, nt, rec_xyz, resid, src_xyz=None, states=None,
+                want_image=False, want_grad=False):
+        npad = (g.nx + 2) * (g.ny + 2) * (g.nz + 2)
+        n = g.nx * g.ny * g.nz
+        vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1)
+        rec_xyz = np.ascontiguousarray(rec_xyz, dtype=np.int64).reshape(-1, 3)
+        resid = np.ascontiguousarray(resid, dtype=np.float64).reshape(nt, rec_xyz.shape[0])
+        src_xyz = np.zeros((0, 3), np.int64) if src_xyz is None else np.ascontiguousarray(src_xyz, np.int64).reshape(-1, 3)
+        ns = src_xyz.shape[0]
+        src_adj = np.zeros((nt, max(ns, 1)))
+        image = np.zeros(n) if want_image else None
+        illum = np.zeros(n) if want_image else None
+        grad = np.zeros(n) if want_grad else None
+        if states is not None:
+            states = np.ascontiguousarray(states, dtype=np.float64).reshape(nt, npad)
+        nul = C.cast(None, _d)
+        rc = self.lib.orc64_adjoint(C.byref(g), _p(vel, _d), nt, rec_xyz.shape[0], _p(rec_xyz, _i64),
+                                    _p(resid, _d), ns, _p(src_xyz, _i64), _p(src_adj, _d),
+                                    _p(states, _d) if states is not None else nul,
+                                    _p(image, _d) if image is not None else nul,
+                                    _p(illum, _d) if illum is not None else nul,
+                                    _p(grad, _d) if grad is not None else nul)
+        assert rc == 0, rc
+        return dict(src_adj=src_adj[:, :ns], image=image, illum=illum, grad_c=grad)
+
+    def rtm_image(self, nx, ny, nz, fwd, adj):
+        nsteps = fwd.shape[0]
+        n = nx * ny * nz
+        fwd = np.ascontiguousarray(fwd, np.float64)
+        adj = np.ascontiguousarray(adj, np.float64)
+        image, illum, refl = np.zeros(n), np.zeros(n), np.zeros(n)
+        self.lib.orc64_rtm_image(nx, ny, nz, nsteps, _p(fwd, _d), _p(adj, _d), _p(image, _d), _p(illum, _d),
+                                 _p(refl, _d))
+        return image, illum, refl
+
+    # ---------------------------------------------------------------- sparse
+    def csr_build(self, rows, cols, r, c, v, pad=False):
+        r = np.ascontiguousarray(r, np.int64)
+        c = np.ascontiguousarray(c, np.int64)
+        v = np.ascontiguousarray(v, np.float64)
+        h = self.lib.orc_csr_build(rows, cols, r.size, _p(r, _i64), _p(c, _i64), _p(v, _d), int(pad))
+        assert h
+        nnz = self.lib.orc_csr_nnz(h)
+        rp = np.zeros(rows + 1, np.int64)
+        col = np.zeros(max(nnz, 1), np.int64)
+        val = np.zeros(max(nnz, 1), np.float64)
+        self.lib.orc_csr_copy(h, _p(rp, _i64), _p(col, _i64), _p(val, _d))
+        self.lib.orc_csr_free(h)
+        return rp, col[:nnz], val[:nnz]
+
+    class _Wrapped:
+        def __init__(self, lib, rows, cols, rp, col, val):
+            self.lib = lib
+            self.rows, self.cols = rows, cols
+            self.rp = np.ascontiguousarray(rp, np.int64)
+            self.col = np.ascontiguousarray(col, np.int64)
+            self.val = np.ascontiguousarray(val, np.float64)
+            if self.col.size == 0:
+                self.col = np.zeros(1, np.int64)
+                self.val = np.zeros(1, np.float64)
+            self.h = lib.orc_csr_wrap(rows, cols, _p(self.rp, _i64), _p(self.col, _i64), _p(self.val, _d))
+
+        def __del__(self):
+            if getattr(self, "h", None):
+                self.lib.orc_csr_unwrap(self.h)
+                self.h = None
+
+    def csr(self, rows, cols, rp, col, val):
+        return Oracle._Wrapped(self.lib, rows, cols, rp, col, val)
+
+    def spmv(self, m, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(m.rows)
+        self.lib.orc_spmv(m.h, _p(x, _d), _p(y, _d))
+        return y
+
+    def spmv_t(self, m, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(m.cols)
+        self.lib.orc_spmv_t(m.h, _p(x, _d), _p(y, _d))
+        return y
+
+    def dot(self, a, b):
+        a = np.ascontiguousarray(a, np.float64)
+        b = np.ascontiguousarray(b, np.float64)
+        return self.lib.orc_dot(_p(a, _d), _p(b, _d), min(a.size, b.size))
+
+    def cg(self, m, b, max_iter=1000, tol=1e-8, jacobi=False):
+        b = np.ascontiguousarray(b, np.float64)
+        x = np.zeros(m.rows)
+        rel = C.c_double(0)
+        it = self.lib.orc_cg(m.h, _p(b, _d), max_iter, tol, int(jacobi), _p(x, _d), C.byref(rel))
+        return x, it, rel.value
+
+    def normal_cg(self, m, d, lam, max_iter=1000, tol=1e-6, jacobi=True):
+        d = np.ascontiguousarray(d, np.float64)
+        x = np.zeros(m.cols)
+        rhs = np.zeros(m.cols)
+        rel = C.c_double(0)
+        it = self.lib.orc_normal_cg(m.h, _p(d, _d), lam, max_iter, tol, int(jacobi), _p(x, _d), _p(rhs, _d),
+                                    C.byref(rel))
+        return x, it, rel.value, rhs
+
+    def normal_apply(self, m, lam, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(m.cols)
+        self.lib.orc_normal_apply(m.h, lam, _p(x, _d), _p(y, _d))
+        return y
+
+    def smooth_gradient(self, g, nx, ny, nz, sigma):
+        g = np.ascontiguousarray(g, np.float64).reshape(-1)
+        out = np.zeros(nx * ny * nz)
+        if g.size < nx * ny * nz:
+            return out
+        self.lib.orc_smooth_gradient(_p(g, _d), nx, ny, nz, sigma, _p(out, _d))
+        return out
+
+    def repair_field_nan(self, data, nx, ny, nz, hw=1, repl=0.0):
+        d = np.array(data, np.float64, copy=True)
+        self.lib.orc64_repair_field_nan(_p(d, _d), d.size, nx, ny, nz, hw, repl)
+        return d
+
+    def clamp_field(self, data, lo, hi):
+        d = np.array(data, np.float64, copy=True)
+        self.lib.orc64_clamp_field(_p(d, _d), d.size, lo, hi)
+        return d
+
+    def count_nan_inf(self, data):
+        d = np.ascontiguousarray(data, np.float64)
+        return self.lib.orc64_count_nan_inf(_p(d, _d), d.size)
+
+    def num_threads(self):
+        return self.lib.orc_num_threads()
+
+
+class Reference:
+    """The reference's own C++ through oracle/ref_harness.cpp (x86 only)."""
+
+    def __init__(self):
+        if not os.path.exists(REF_SO):
+            raise FileNotFoundError(REF_SO)
+        L = self.lib = C.CDLL(REF_SO)
+        L.ref_run_steps.argtypes = [C.c_int64] * 3 + [C.c_double] * 4 + [C.c_int, C.c_double, _d, C.c_int, _i64,
+                                                                          _d, C.c_int, _i64, _d, C.c_int, C.c_int,
+                                                                          _i32, _d, _d]
+        L.ref_forward_propagate.argtypes = [C.c_int64] * 3 + [C.c_double] * 4 + [C.c_int, C.c_int, C.c_double,
+                                                                                  C.c_int, _d, _d, C.c_int64, _d,
+                                                                                  _d, _d, C.c_int64, _i64]
+        L.ref_rtm_image.argtypes = [C.c_int64] * 3 + [C.c_int, _d, _d, _d, _d, _d]
+        L.ref_csr_build.argtypes = [C.c_int64, C.c_int64, C.c_int64, _i64, _i64, _d]
+        L.ref_csr_build.restype = C.c_int64
+        L.ref_csr_get.argtypes = [_i64, _i64, _d]
+        L.ref_csr_spmv.argtypes = [_d, C.c_int64, _d]
+        L.ref_repair_field_nan.argtypes = [_d, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int, C.c_double]
+        L.ref_count_nan_inf.argtypes = [_d, C.c_int64]
+        L.ref_count_nan_inf.restype = C.c_int64
+        L.ref_clamp_field.argtypes = [_d, C.c_int64, C.c_double, C.c_double]
+        L.ref_load_config.argtypes = [C.c_char_p, _d]
+
+    def run_steps(self, nx, ny, nz, dx, dy, dz, dt, sw, damp, vel, nsteps, src_xyz, src_w, rec_xyz, adjoint=False):
+        npad = (nx + 2) * (ny + 2) * (nz + 2)
+        vel = np.ascontiguousarray(vel, np.float64).reshape(-1)
+        src_xyz = np.ascontiguousarray(src_xyz, np.int64).reshape(-1, 3)
+        rec_xyz = np.ascontiguousarray(rec_xyz, np.int64).reshape(-1, 3)
+        ns, nr = src_xyz.shape[0], rec_xyz.shape[0]
+        src_w = np.ascontiguousarray(src_w, np.float64).reshape(nsteps, ns)
+        seis = np.zeros((nsteps, max(nr, 1)))
+        st = np.zeros(nsteps, np.int32)
+        cur = np.zeros(npad)
+        prev = np.zeros(npad)
+        self.lib.ref_run_steps(nx, ny, nz, dx, dy, dz, dt, sw, damp, _p(vel, _d), ns, _p(src_xyz, _i64),
+                               _p(src_w, _d), nr, _p(rec_xyz, _i64), _p(seis, _d), nsteps, int(adjoint),
+                               _p(st, _i32), _p(cur, _d), _p(prev, _d))
+        return dict(seis=seis[:, :nr], status=st, cur=cur, prev=prev)
+
+    def forward_propagate(self, nx, ny, nz, dx, dy, dz, dt, nt, sw, damp, snap_int, vel, wavelet):
+        npad = (nx + 2) * (ny + 2) * (nz + 2)
+        vel = np.ascontiguousarray(vel, np.float64).reshape(-1)
+        wavelet = np.ascontiguousarray(wavelet, np.float64)
+        cur, prev = np.zeros(npad), np.zeros(npad)
+        cap = (nt // max(snap_int, 1) + 2) * nx * ny * nz
+        snaps = np.zeros(cap)
+        res = np.zeros(6, np.int64)
+        self.lib.ref_forward_propagate(nx, ny, nz, dx, dy, dz, dt, nt, sw, damp, snap_int, _p(vel, _d),
+                                       _p(wavelet, _d), wavelet.size, _p(cur, _d), _p(prev, _d), _p(snaps, _d),
+                                       cap, _p(res, _i64))
+        return dict(status=int(res[0]), total_nan=int(res[1]), repaired=int(res[2]), steps=int(res[3]),
+                    ok=bool(res[4]), cur=cur, prev=prev, snapshots=snaps[:res[5]])
+
+    def rtm_image(self, nx, ny, nz, fwd, adj):
+        n = nx * ny * nz
+        fwd = np.ascontiguousarray(fwd, np.float64)
+        adj = np.ascontiguousarray(adj, np.float64)
+        image, illum, refl = np.zeros(n), np.zeros(n), np.zeros(n)
+        self.lib.ref_rtm_image(nx, ny, nz, fwd.shape[0], _p(fwd, _d), _p(adj, _d), _p(image, _d),
+                               _p(illum, _d), _p(refl, _d))
+        return image, illum, refl
+
+    def csr_build(self, rows, cols, r, c, v):
+        r = np.ascontiguousarray(r, np.int64)
+        c = np.ascontiguousarray(c, np.int64)
+        v = np.ascontiguousarray(v, np.float64)
+        nnz = self.lib.ref_csr_build(rows, cols, r.size, _p(r, _i64), _p(c, _i64), _p(v, _d))
+        rp = np.zeros(rows + 1, np.int64)
+        col = np.zeros(max(nnz, 1), np.int64)
+        val = np.zeros(max(nnz, 1))
+        self.lib.ref_csr_get(_p(rp, _i64), _p(col, _i64), _p(val, _d))
+        return rp, col[:nnz], val[:nnz]
+
+    def csr_spmv(self, x, rows):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(rows)
+        self.lib.ref_csr_spmv(_p(x, _d), x.size, _p(y, _d))
+        return y
+
+    def repair_field_nan(self, data, nx, ny, nz, hw=1, repl=0.0):
+        d = np.array(data, np.float64, copy=True)
+        self.lib.ref_repair_field_nan(_p(d, _d), d.size, nx, ny, nz, hw, repl)
+        return d
+
+    def count_nan_inf(self, data):
+        d = np.ascontiguousarray(data, np.float64)
+        return self.lib.ref_count_nan_inf(_p(d, _d), d.size)
+
+    def clamp_field(self, data, lo, hi):
+        d = np.array(data, np.float64, copy=True)
+        self.lib.ref_clamp_field(_p(d, _d), d.size, lo, hi)
+        return d
+
+    def load_config(self, path):
+        out = np.zeros(17)
+        self.lib.ref_load_config(path.encode(), _p(out, _d))
+        return out

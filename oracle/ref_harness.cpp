@@ -1,0 +1,211 @@
+// C entry points over the reference's own public C++ API, compiled together
+// with the reference sources (solver/wave_equation.cpp, rtm/rtm_engine.cpp,
+// sparse/csr_matrix.cpp, core/*.cpp) into oracle/_ref/libseismic_ref.so by
+// oracle/build_ref.sh. Test infrastructure only: it pins the C restatement in
+// oracle/seismic_oracle.c and generates the golden fixtures under tests/golden/.
+// Nothing in the product links or loads it.
+#include "solver/wave_equation.h"
+#include "rtm/rtm_engine.h"
+#include "sparse/csr_matrix.h"
+#include "core/config.h"
+#include "core/fault_tolerance.h"
+
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+namespace {
+
+struct RefWorld {
+    int argc = 1;
+    char arg0[8] = "oracle";
+    char* argv_store[2] = {arg0, nullptr};
+    char** argv = argv_store;
+    std::unique_ptr<seismic::MpiContext> mpi;
+    RefWorld() { mpi = std::make_unique<seismic::MpiContext>(argc, argv); }
+};
+
+RefWorld& world() {
+    static RefWorld w;
+    return w;
+}
+
+seismic::GridParams make_params(int64_t nx, int64_t ny, int64_t nz, double dx, double dy, double dz) {
+    seismic::GridParams p{};
+    p.nx_global = nx;
+    p.ny_global = ny;
+    p.nz_global = nz;
+    p.dx = dx;
+    p.dy = dy;
+    p.dz = dz;
+    p.halo_width = 1;
+    return p;
+}
+
+seismic::SolverConfig make_config(double dt, int nt, int sponge_width, double sponge_damping, int snapshot_interval) {
+    seismic::SolverConfig c{};
+    c.frequency = 2.0;
+    c.dt = dt;
+    c.nt = nt;
+    c.water_depth = 4000.0;
+    c.seafloor_gradient = 0.05;
+    c.sponge_width = sponge_width;
+    c.sponge_damping = sponge_damping;
+    c.snapshot_interval = snapshot_interval;
+    c.output_dir = "./output";
+    return c;
+}
+
+std::unique_ptr<seismic::CSRMatrix> g_csr;
+
+}  // namespace
+
+extern "C" {
+
+// Steps the reference solver `nsteps` times. Before step t every source s
+// gets inject_source(src_xyz[s], {src_w[t*n_src+s]}) (wave_equation.cpp:39-54);
+// then step_forward(t) (or step_adjoint(t) when use_adjoint), whose status is
+// stored in statuses[t]; then every receiver r samples field().current into
+// seis[t*nrec+r]. The final current/previous padded fields are copied out.
+int ref_run_steps(int64_t nx, int64_t ny, int64_t nz, double dx, double dy, double dz,
+                  double dt, int sponge_width, double sponge_damping,
+                  const double* vel_padded, int n_src, const int64_t* src_xyz, const double* src_w,
+                  int nrec, const int64_t* rec_xyz, double* seis, int nsteps, int use_adjoint,
+                  int* statuses, double* out_current, double* out_previous) {
+    auto& w = world();
+    int coords[3] = {0, 0, 0};
+    int dims[3] = {1, 1, 1};
+    seismic::CartesianGrid grid(make_params(nx, ny, nz, dx, dy, dz), coords, dims);
+    seismic::WaveEquationSolver solver(*w.mpi, grid, make_config(dt, nsteps, sponge_width, sponge_damping, 100));
+    const int64_t n = grid.local().total_cells_with_halo;
+    solver.set_velocity_field(vel_padded, n);
+    const int64_t nyh = grid.local().ny_with_halo, nzh = grid.local().nz_with_halo;
+    for (int t = 0; t < nsteps; ++t) {
+        for (int s = 0; s < n_src; ++s) {
+            std::vector<double> wv = {src_w[(int64_t)t * n_src + s]};
+            solver.inject_source(src_xyz[3 * s], src_xyz[3 * s + 1], src_xyz[3 * s + 2], wv);
+        }
+        seismic::StepResult r = use_adjoint ? solver.step_adjoint(t) : solver.step_forward(t);
+        statuses[t] = static_cast<int>(r);
+        const auto& cur = solver.field().current;
+        for (int q = 0; q < nrec; ++q) {
+            int64_t idx = (rec_xyz[3 * q] + 1) * nyh * nzh + (rec_xyz[3 * q + 1] + 1) * nzh + (rec_xyz[3 * q + 2] + 1);
+            seis[(int64_t)t * nrec + q] = cur[idx];
+        }
+    }
+    std::memcpy(out_current, solver.field().current.data(), n * sizeof(double));
+    std::memcpy(out_previous, solver.field().previous.data(), n * sizeof(double));
+    return 0;
+}
+
+// The reference's forward_propagate (wave_equation.cpp:100-152): centre source,
+// CFL check, snapshots every snapshot_interval steps. result[0..3] = status,
+// total_nan_encountered, total_cells_repaired, timesteps_completed;
+// result[4] = completed_successfully; result[5] = snapshot doubles stored.
+int ref_forward_propagate(int64_t nx, int64_t ny, int64_t nz, double dx, double dy, double dz,
+                          double dt, int nt, int sponge_width, double sponge_damping, int snapshot_interval,
+                          const double* vel_padded, const double* wavelet, int64_t nw,
+                          double* out_current, double* out_previous, double* out_snapshots,
+                          int64_t snap_cap, int64_t* result) {
+    auto& w = world();
+    int coords[3] = {0, 0, 0};
+    int dims[3] = {1, 1, 1};
+    seismic::CartesianGrid grid(make_params(nx, ny, nz, dx, dy, dz), coords, dims);
+    seismic::WaveEquationSolver solver(*w.mpi, grid,
+                                       make_config(dt, nt, sponge_width, sponge_damping, snapshot_interval));
+    const int64_t n = grid.local().total_cells_with_halo;
+    solver.set_velocity_field(vel_padded, n);
+    std::vector<double> wav(wavelet, wavelet + nw);
+    seismic::PropagationResult pr = solver.forward_propagate(wav);
+    result[0] = static_cast<int64_t>(pr.status);
+    result[1] = pr.total_nan_encountered;
+    result[2] = pr.total_cells_repaired;
+    result[3] = pr.timesteps_completed;
+    result[4] = pr.completed_successfully ? 1 : 0;
+    const auto& snaps = solver.field().snapshots;
+    result[5] = static_cast<int64_t>(snaps.size());
+    std::memcpy(out_current, solver.field().current.data(), n * sizeof(double));
+    std::memcpy(out_previous, solver.field().previous.data(), n * sizeof(double));
+    int64_t m = std::min<int64_t>(snap_cap, static_cast<int64_t>(snaps.size()));
+    if (m > 0) std::memcpy(out_snapshots, snaps.data(), m * sizeof(double));
+    return 0;
+}
+
+// RTMEngine::apply_image_condition over nsteps pairs of halo-padded fields,
+// then finalize_image (rtm/rtm_engine.cpp:24-57,170-182).
+int ref_rtm_image(int64_t nx, int64_t ny, int64_t nz, int nsteps, const double* fwd, const double* adj,
+                  double* image, double* illum, double* refl) {
+    seismic::RTMEngine eng(nx, ny, nz, 10.0, 10.0, 10.0, 1);
+    const int64_t nyh = ny + 2, nzh = nz + 2, np = (nx + 2) * nyh * nzh;
+    for (int t = 0; t < nsteps; ++t)
+        eng.apply_image_condition(fwd + (int64_t)t * np, adj + (int64_t)t * np, nyh, nzh, t);
+    eng.finalize_image();
+    const auto& r = eng.result();
+    std::memcpy(image, r.image.data(), r.image.size() * sizeof(double));
+    std::memcpy(illum, r.illumination.data(), r.illumination.size() * sizeof(double));
+    std::memcpy(refl, r.reflectivity.data(), r.reflectivity.size() * sizeof(double));
+    return 0;
+}
+
+// CSRMatrix::build_from_triplets (sparse/csr_matrix.cpp:25-72). The shipped
+// pad_to_alignment under-allocates whenever it fires, so callers pass only
+// inputs where every merged row has >= 8 entries (padding then never fires).
+int64_t ref_csr_build(int64_t rows, int64_t cols, int64_t n, const int64_t* r, const int64_t* c, const double* v) {
+    std::vector<seismic::SparseEntry> e(n);
+    for (int64_t i = 0; i < n; ++i) e[i] = {r[i], c[i], v[i]};
+    g_csr = std::make_unique<seismic::CSRMatrix>();
+    g_csr->build_from_triplets(rows, cols, e);
+    return g_csr->nnz();
+}
+
+int ref_csr_get(int64_t* row_ptr, int64_t* col, double* val) {
+    if (!g_csr) return -1;
+    std::memcpy(row_ptr, g_csr->row_ptr().data(), (g_csr->rows() + 1) * sizeof(int64_t));
+    std::memcpy(col, g_csr->col_ind().data(), g_csr->nnz() * sizeof(int64_t));
+    std::memcpy(val, g_csr->values().data(), g_csr->nnz() * sizeof(double));
+    return 0;
+}
+
+// CSRMatrix::spmv (sparse/csr_matrix.cpp:118-149) on the last built matrix.
+int ref_csr_spmv(const double* x, int64_t nxv, double* y) {
+    if (!g_csr) return -1;
+    seismic::AlignedVector<double> xv(nxv);
+    for (int64_t i = 0; i < nxv; ++i) xv[i] = x[i];
+    auto yv = g_csr->spmv(xv);
+    for (int64_t i = 0; i < g_csr->rows(); ++i) y[i] = yv[i];
+    return 0;
+}
+
+// FaultTolerance::repair_field_nan / clamp_field / count_nan_inf
+// (core/fault_tolerance.cpp:72-157).
+int ref_repair_field_nan(double* data, int64_t count, int64_t nx, int64_t ny, int64_t nz, int hw, double repl) {
+    seismic::FaultTolerance ft(MPI_COMM_SELF, 0, 1);
+    ft.repair_field_nan(data, count, nx, ny, nz, hw, repl);
+    return 0;
+}
+int64_t ref_count_nan_inf(const double* data, int64_t count) {
+    return seismic::FaultTolerance::count_nan_inf(data, count);
+}
+int ref_clamp_field(double* data, int64_t count, double lo, double hi) {
+    seismic::FaultTolerance::clamp_field(data, count, lo, hi);
+    return 0;
+}
+
+// load_config (core/config.cpp:9-94). out[0..] = frequency, dt, nt, water_depth,
+// seafloor_gradient, sponge_width, sponge_damping, snapshot_interval,
+// vp_min, vp_max, initial_vp, initial_vs, initial_rho, max_iterations,
+// step_length, gradient_smoothing_sigma, regularization_lambda.
+int ref_load_config(const char* path, double* out) {
+    seismic::TomographyConfig c = seismic::load_config(path);
+    double v[] = {c.solver.frequency, c.solver.dt, (double)c.solver.nt, c.solver.water_depth,
+                  c.solver.seafloor_gradient, (double)c.solver.sponge_width, c.solver.sponge_damping,
+                  (double)c.solver.snapshot_interval, c.model.vp_min, c.model.vp_max, c.model.initial_vp,
+                  c.model.initial_vs, c.model.initial_rho, (double)c.inversion.max_iterations,
+                  c.inversion.step_length, c.inversion.gradient_smoothing_sigma,
+                  c.inversion.regularization_lambda};
+    std::memcpy(out, v, sizeof(v));
+    return 0;
+}
+
+}  // extern "C"
