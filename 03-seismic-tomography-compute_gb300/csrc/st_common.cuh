@@ -50,6 +50,11 @@ enum : unsigned {
     FLAG_TIMEOUT = 2u,  // a bounded mbarrier wait gave up (pipeline fault)
 };
 
+// Number of kernels this library has launched in the process (every launch
+// site calls count_launch right after its <<<>>>).
+void count_launch(long long n = 1);
+long long launch_count();
+
 // ---------------------------------------------------------------- layout
 // Device layout of one FP32 field. x and y carry the reference's one-cell
 // halo (x slowest, z fastest, as core/grid.cpp:45-49); along z the interior

@@ -34,6 +34,15 @@ __global__ void rec_force_kernel(float* f, const float* c, Layout L, st_receiver
     f[i] += c[i] * row[q];
 }
 
+// trace[t] = lambda at the source before the forcing of step t-1:
+// (mu - c * d_{t-1}[q_src]) / c, where q_src < 0 when the source is not a receiver.
+__global__ void probe_kernel(const float* f, const float* c, long long idx, const float* force_row, long long q,
+                             float* out) {
+    float v = f[idx];
+    if (force_row && q >= 0) v -= c[idx] * force_row[q];
+    *out = v / c[idx];
+}
+
 __global__ void f32_to_f64_kernel(const float* a, double* b, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         b[i] = (double)a[i];
@@ -102,35 +111,58 @@ int shot_forward_impl(st_solver* s, const st_shot* shot, float* seis, int snap_k
     return ST_OK;
 }
 
-// Backward pass with imaging, given the forward snapshots of every step.
+// Receiver number of grid point (ix, iy, iz), or -1.
+long long receiver_at(const st_receiver_grid& R, int64_t ix, int64_t iy, int64_t iz) {
+    if (R.nx * R.ny == 0 || iz != R.z) return -1;
+    const int64_t xx = ix - R.x0, yy = iy - R.y0;
+    if (xx < 0 || yy < 0 || xx % R.sx || yy % R.sy || xx / R.sx >= R.nx || yy / R.sy >= R.ny) return -1;
+    return (xx / R.sx) * R.ny + yy / R.sy;
+}
+
+// Backward pass of the exact adjoint. With snaps != null the imaging
+// epilogue runs (image/illum); with src_trace != null lambda at the source
+// is sampled after every step (the transpose of the wavelet -> data map).
 int rtm_backward_impl(st_solver* s, const st_shot* shot, const float* data, int snap_kind, const void* snaps,
-                      const unsigned* amax, float* image, float* illum) {
+                      const unsigned* amax, float* image, float* illum, float* src_trace = nullptr) {
     const Layout& L = s->L;
     const st_receiver_grid& R = shot->rec;
     const int64_t nrec = R.nx * R.ny;
     const int nt = shot->nt;
     const size_t npts = (size_t)(L.nx * L.ny * L.nz);
     const size_t per = npts * (size_t)snap_bytes(snap_kind);
+    const bool imaging = snaps != nullptr;
     ST_TRY(zero_fields(s));
-    ST_CUDA(cudaMemsetAsync(image, 0, npts * sizeof(float), s->stream));
-    ST_CUDA(cudaMemsetAsync(illum, 0, npts * sizeof(float), s->stream));
+    if (imaging) {
+        ST_CUDA(cudaMemsetAsync(image, 0, npts * sizeof(float), s->stream));
+        ST_CUDA(cudaMemsetAsync(illum, 0, npts * sizeof(float), s->stream));
+    }
     if (nt <= 0) return ST_OK;
     if (nrec > 0) {
         rec_force_kernel<<<(unsigned)((nrec + 255) / 256), 256, 0, s->stream>>>(s->f[s->ic], s->c, L, R,
                                                                                data + (size_t)(nt - 1) * nrec);
+    ::stg::count_launch();
         ST_CUDA(cudaGetLastError());
     }
+    const long long src = dev_index(s, shot->src_ix, shot->src_iy, shot->src_iz);
+    const long long q_src = receiver_at(R, shot->src_ix, shot->src_iy, shot->src_iz);
     for (int t = nt - 1; t >= 0; --t) {
         StepArgs a = base_args(s, nullptr);
         if (nrec > 0 && t >= 1) {
             set_receivers(a, R);
             a.force_row = data + (size_t)(t - 1) * nrec;
         }
-        a.snap_in = static_cast<const char*>(snaps) + (size_t)t * per;
-        a.amax_in = amax + t;
-        a.image = image;
-        a.illum = illum;
-        ST_TRY(fused_step(s, a, SNAP_NONE, snap_kind, true));
+        if (imaging) {
+            a.snap_in = static_cast<const char*>(snaps) + (size_t)t * per;
+            a.amax_in = amax + t;
+            a.image = image;
+            a.illum = illum;
+        }
+        ST_TRY(fused_step(s, a, SNAP_NONE, imaging ? snap_kind : SNAP_NONE, imaging));
+        if (src_trace) {
+            probe_kernel<<<1, 1, 0, s->stream>>>(s->f[s->ic], s->c, src, a.force_row, q_src, src_trace + t);
+    ::stg::count_launch();
+            ST_CUDA(cudaGetLastError());
+        }
     }
     return ST_OK;
 }
@@ -148,6 +180,22 @@ int st_shot_forward(st_solver* s, const st_shot* shot, float* seis, int snap_kin
     ST_CHECK(shot->rec.nx * shot->rec.ny == 0 || seis, ST_ERR_ARG, "receivers given but no seismogram buffer");
     ST_CUDA(cudaSetDevice(s->device));
     ST_TRY(shot_forward_impl(s, shot, seis, snap_kind, snaps, snap_amax));
+    unsigned fl = 0;
+    ST_TRY(read_flags(s, &fl));
+    return (fl & FLAG_GUARD) ? ST_NAN_DETECTED_AND_REPAIRED : ST_OK;
+}
+
+int st_shot_adjoint(st_solver* s, const st_shot* shot, const float* data, float* src_trace) {
+    ST_CHECK(s && shot && src_trace, ST_ERR_ARG, "null argument");
+    const int64_t nrec = shot->rec.nx * shot->rec.ny;
+    ST_CHECK(nrec == 0 || data, ST_ERR_ARG, "receiver data missing");
+    ST_CHECK(shot->src_ix >= 0 && shot->src_ix < s->L.nx && shot->src_iy >= 0 && shot->src_iy < s->L.ny &&
+                 shot->src_iz >= 0 && shot->src_iz < s->L.nz,
+             ST_ERR_ARG, "source outside the interior");
+    ST_TRY(check_receivers(s, shot->rec));
+    ST_CUDA(cudaSetDevice(s->device));
+    ST_TRY(refresh_coeff(s));
+    ST_TRY(rtm_backward_impl(s, shot, data, SNAP_NONE, nullptr, nullptr, nullptr, nullptr, src_trace));
     unsigned fl = 0;
     ST_TRY(read_flags(s, &fl));
     return (fl & FLAG_GUARD) ? ST_NAN_DETECTED_AND_REPAIRED : ST_OK;
@@ -172,8 +220,12 @@ int st_rtm_shot(st_solver* s, const st_shot* shot, const float* data, int snap_k
         ST_TRY(ensure_buffer(s, &s->aux_buf, &s->aux_cap, sizeof(unsigned) * (size_t)(shot->nt + 1)));
         amax = static_cast<unsigned*>(s->aux_buf);
     }
+    ST_CUDA(cudaEventRecord(s->ev[0], s->stream));
     ST_TRY(shot_forward_impl(s, shot, nullptr, snap_kind, snaps, amax));
+    ST_CUDA(cudaEventRecord(s->ev[1], s->stream));
     ST_TRY(rtm_backward_impl(s, shot, data, snap_kind, snaps, amax, image, illum));
+    ST_CUDA(cudaEventRecord(s->ev[2], s->stream));
+    s->phases_recorded = 1;
     if (refl) ST_TRY(launch_finalize_image(image, illum, refl, (long long)npts, s->stream));
     unsigned fl = 0;
     ST_TRY(read_flags(s, &fl));
@@ -214,6 +266,7 @@ int st_rtm_shot_host(st_solver* s, const double* vp, int64_t vp_count, const st_
     for (int k = 0; k < 3; ++k) {
         if (!dsts[k]) continue;
         f32_to_f64_kernel<<<1024, 256, 0, s->stream>>>(srcs[k], out64, (long long)npts);
+    ::stg::count_launch();
         ST_CUDA(cudaGetLastError());
         ST_CUDA(cudaMemcpyAsync(dsts[k], out64, npts * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     }

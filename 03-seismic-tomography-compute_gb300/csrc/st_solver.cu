@@ -247,11 +247,15 @@ int health_check(st_solver* s, int timestep, int* result) {
     for (int attempt = 0; attempt < s->max_repair_attempts; ++attempt) {
         ST_CUDA(cudaMemsetAsync(s->counter, 0, sizeof(unsigned long long), s->stream));
         repair_nan_kernel<<<1, 1024, 0, s->stream>>>(s->f[s->ic], s->L, s->dtab, s->sw, 0, 0.0f, s->counter);
+    ::stg::count_launch();
         repair_nan_kernel<<<1, 1024, 0, s->stream>>>(s->f[s->ip], s->L, s->dtab, s->sw, 1, 0.0f, s->counter);
+    ::stg::count_launch();
         clamp_view_kernel<<<256, 256, 0, s->stream>>>(s->f[s->ic], s->L, s->dtab, s->sw, 0, (float)-s->amp_limit,
                                                       (float)s->amp_limit);
+    ::stg::count_launch();
         clamp_view_kernel<<<256, 256, 0, s->stream>>>(s->f[s->ip], s->L, s->dtab, s->sw, 1, (float)-s->amp_limit,
                                                       (float)s->amp_limit);
+    ::stg::count_launch();
         ST_CUDA(cudaGetLastError());
         unsigned long long post = 0;
         ST_TRY(launch_count_nonfinite(s->f[s->ic], s->L.elems, s->counter, s->stream));
@@ -375,6 +379,7 @@ int st_solver_create(const st_grid_params* grid, const st_solver_config* cfg, in
     s->L = make_layout(grid->nx_global, grid->ny_global, grid->nz_global);
     s->vel_host.assign((size_t)ref_elems(s.get()), 0.0);
     ST_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 3; ++k) ST_CUDA(cudaEventCreate(&s->ev[k]));
     const size_t fb = (size_t)s->L.elems * sizeof(float);
     for (int k = 0; k < 3; ++k) ST_CUDA(cudaMalloc(&s->f[k], fb));
     ST_CUDA(cudaMalloc(&s->c, fb));
@@ -419,6 +424,8 @@ int st_solver_destroy(st_solver* s) {
     cudaFree(s->snap_buf);
     cudaFree(s->aux_buf);
     cudaFree(s->data_buf);
+    for (int k = 0; k < 3; ++k)
+        if (s->ev[k]) cudaEventDestroy(s->ev[k]);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return ST_OK;
@@ -675,6 +682,22 @@ int st_solver_device_field(st_solver* s, int which, float** out) {
         }
         default: ST_CHECK(false, ST_ERR_ARG, "bad field id %d", which);
     }
+    return ST_OK;
+}
+
+int st_launch_count(long long* out) {
+    ST_CHECK(out, ST_ERR_ARG, "null argument");
+    *out = launch_count();
+    return ST_OK;
+}
+
+int st_solver_last_phase_ms(st_solver* s, float out[2]) {
+    ST_CHECK(s && out, ST_ERR_ARG, "null argument");
+    ST_CHECK(s->phases_recorded, ST_ERR_STATE, "no RTM call has recorded its phases yet");
+    ST_CUDA(cudaSetDevice(s->device));
+    ST_CUDA(cudaEventSynchronize(s->ev[2]));
+    ST_CUDA(cudaEventElapsedTime(&out[0], s->ev[0], s->ev[1]));
+    ST_CUDA(cudaEventElapsedTime(&out[1], s->ev[1], s->ev[2]));
     return ST_OK;
 }
 

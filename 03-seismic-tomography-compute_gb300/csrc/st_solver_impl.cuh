@@ -3,7 +3,53 @@
 
 #include "st_kernels.cuh"
 
+#include <algorithm>
+#include <cstdlib>
 #include <vector>
+
+namespace stg {
+// Host array in page-locked memory (plain heap memory if pinning fails), so
+// host->device copies from it run at full link speed.
+class PinnedVec {
+   public:
+    PinnedVec() = default;
+    PinnedVec(const PinnedVec&) = delete;
+    PinnedVec& operator=(const PinnedVec&) = delete;
+    ~PinnedVec() { release(); }
+    void assign(size_t n, double v) {
+        release();
+        if (cudaMallocHost(reinterpret_cast<void**>(&p_), n * sizeof(double)) == cudaSuccess) {
+            pinned_ = true;
+        } else {
+            cudaGetLastError();
+            p_ = static_cast<double*>(std::malloc(n * sizeof(double)));
+            pinned_ = false;
+        }
+        n_ = p_ ? n : 0;
+        std::fill(p_, p_ + n_, v);
+    }
+    double* data() { return p_; }
+    const double* data() const { return p_; }
+    size_t size() const { return n_; }
+    double* begin() { return p_; }
+    double* end() { return p_ + n_; }
+    const double* begin() const { return p_; }
+    const double* end() const { return p_ + n_; }
+
+   private:
+    void release() {
+        if (p_) {
+            if (pinned_) cudaFreeHost(p_);
+            else std::free(p_);
+        }
+        p_ = nullptr;
+        n_ = 0;
+    }
+    double* p_ = nullptr;
+    size_t n_ = 0;
+    bool pinned_ = false;
+};
+}  // namespace stg
 
 struct st_solver {
     int device = 0;
@@ -14,7 +60,7 @@ struct st_solver {
     double amp_limit = 1e10;
     double cfl_safety = 0.49;
     int max_repair_attempts = 3;
-    std::vector<double> vel_host;  // reference layout, authoritative velocity
+    stg::PinnedVec vel_host;  // reference layout, authoritative velocity
     float* f[3] = {nullptr, nullptr, nullptr};
     int ic = 0, ip = 1, in = 2;
     float* c = nullptr;
@@ -38,6 +84,10 @@ struct st_solver {
     size_t aux_cap = 0;
     void* data_buf = nullptr;       // host-API staging of receiver data
     size_t data_cap = 0;
+    // phase boundaries of the last shot-level call, recorded on `stream`:
+    // [0] start, [1] forward done, [2] backward done
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    int phases_recorded = 0;
 };
 
 

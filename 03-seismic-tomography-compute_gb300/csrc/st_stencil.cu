@@ -29,6 +29,7 @@
 #include "st_kernels.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <mutex>
 
@@ -361,6 +362,7 @@ int launch_variant(dim3 grid, const CUtensorMap& mcur, const CUtensorMap& mprev,
         }
     }
     fd_step_kernel<SO, SI, IM><<<grid, NTHREADS, SMEM_BYTES, st>>>(mcur, mprev, mc, a);
+    ::stg::count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
 }
@@ -585,6 +587,7 @@ int launch_fd_step(const Layout& L, const CUtensorMap& mcur, const CUtensorMap& 
 
 int launch_add_point(float* f, long long idx, float val, unsigned* amax_slot, cudaStream_t st) {
     add_point_kernel<<<1, 1, 0, st>>>(f, idx, val, amax_slot);
+    ::stg::count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
 }
@@ -592,6 +595,7 @@ int launch_add_point(float* f, long long idx, float val, unsigned* amax_slot, cu
 int launch_gather(const float* f, const long long* idx, int n, float* out, cudaStream_t st) {
     if (n <= 0) return ST_OK;
     gather_kernel<<<(n + 255) / 256, 256, 0, st>>>(f, idx, n, out);
+    ::stg::count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
 }
@@ -599,12 +603,14 @@ int launch_gather(const float* f, const long long* idx, int n, float* out, cudaS
 int launch_scatter_scaled(float* f, const long long* idx, int n, const float* val, const float* c, cudaStream_t st) {
     if (n <= 0) return ST_OK;
     scatter_scaled_kernel<<<(n + 255) / 256, 256, 0, st>>>(f, idx, n, val, c);
+    ::stg::count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
 }
 
 int launch_ref_to_dev(const double* src, float* dst, const Layout& L, cudaStream_t st) {
     ref_to_dev_kernel<<<grid_for(L.elems), 256, 0, st>>>(src, dst, L, nullptr, 0, 0);
+    ::stg::count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
 }
@@ -612,6 +618,7 @@ int launch_ref_to_dev(const double* src, float* dst, const Layout& L, cudaStream
 int launch_ref_to_dev_undamp(const double* src, float* dst, const Layout& L, const float* dtab, int sw, int pow,
                              cudaStream_t st) {
     ref_to_dev_kernel<<<grid_for(L.elems), 256, 0, st>>>(src, dst, L, dtab, sw, pow);
+    ::stg::count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
 }
@@ -620,12 +627,14 @@ int launch_dev_to_ref(const float* src, double* dst, const Layout& L, const floa
                       cudaStream_t st) {
     const long long n = L.NXh * L.NYh * (L.nz + 2);
     dev_to_ref_kernel<<<grid_for(n), 256, 0, st>>>(src, dst, L, dtab, sw, damp_pow);
+    ::stg::count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
 }
 
 int launch_vel_to_coeff(const double* vel_ref, float* c, const Layout& L, double dt2damp, cudaStream_t st) {
     vel_to_coeff_kernel<<<grid_for(L.elems), 256, 0, st>>>(vel_ref, c, L, dt2damp);
+    ::stg::count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
 }
@@ -633,6 +642,7 @@ int launch_vel_to_coeff(const double* vel_ref, float* c, const Layout& L, double
 int launch_count_nonfinite(const float* f, long long n, unsigned long long* out, cudaStream_t st) {
     ST_CUDA(cudaMemsetAsync(out, 0, sizeof(unsigned long long), st));
     count_nonfinite_kernel<<<grid_for(n), 256, 0, st>>>(f, n, out);
+    ::stg::count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
 }
@@ -640,21 +650,32 @@ int launch_count_nonfinite(const float* f, long long n, unsigned long long* out,
 int launch_sumsq_finite(const float* f, long long n, double* out, cudaStream_t st) {
     ST_CUDA(cudaMemsetAsync(out, 0, sizeof(double), st));
     sumsq_finite_kernel<<<grid_for(n), 256, 0, st>>>(f, n, out);
+    ::stg::count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
 }
 
 int launch_interior_copy(const float* f, const Layout& L, float* out, cudaStream_t st) {
     interior_copy_kernel<<<grid_for(L.nx * L.ny * L.nz), 256, 0, st>>>(f, L, out);
+    ::stg::count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
 }
 
 int launch_finalize_image(const float* image, const float* illum, float* refl, long long n, cudaStream_t st) {
     finalize_image_kernel<<<grid_for(n), 256, 0, st>>>(image, illum, refl, n);
+    ::stg::count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
 }
+
+// ---------------------------------------------------------------- launch counter
+
+namespace {
+std::atomic<long long> g_launches{0};
+}
+void count_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 // ---------------------------------------------------------------- tensor maps
 

@@ -102,8 +102,11 @@ SIGNATURES = {
     "st_solver_fault_stats": [_vp, C.POINTER(FaultStatsC)],
     "st_solver_device_field": [_vp, C.c_int, C.POINTER(_vp)],
     "st_solver_stream": [_vp, C.POINTER(_vp)],
+    "st_solver_last_phase_ms": [_vp, C.POINTER(C.c_float)],
+    "st_launch_count": [C.POINTER(C.c_longlong)],
     "st_shot_forward": [_vp, C.POINTER(ShotC), _vp, C.c_int, _vp, _vp],
     "st_shot_forward_host": [_vp, _d, C.c_int64, C.POINTER(ShotC), _d],
+    "st_shot_adjoint": [_vp, C.POINTER(ShotC), _vp, _vp],
     "st_rtm_shot": [_vp, C.POINTER(ShotC), _vp, C.c_int, _vp, _vp, _vp, _vp, _vp],
     "st_rtm_shot_host": [_vp, _d, C.c_int64, C.POINTER(ShotC), _f, C.c_int, _d, _d, _d],
 }

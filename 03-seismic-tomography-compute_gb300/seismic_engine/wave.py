@@ -278,6 +278,45 @@ def shot_forward(solver: WaveEquationSolver, src, wavelet, nt: int, rec, seis=No
     return call("st_shot_forward", solver.handle, C.byref(shot), sp, snap_kind, snp, amp)
 
 
+def shot_adjoint(solver: WaveEquationSolver, src, nt: int, rec, data, src_trace) -> int:
+    """Exact adjoint of shot_forward: data (torch CUDA FP32 [nt, nrec]) ->
+    src_trace (torch CUDA FP32 [nt]) = d<seismograms, data>/d wavelet."""
+    shot, _keep = _shot_c(src, np.zeros(1), nt, rec)
+    return call("st_shot_adjoint", solver.handle, C.byref(shot), data.data_ptr(), src_trace.data_ptr())
+
+
+def rtm_shot(solver: WaveEquationSolver, src, wavelet, nt: int, rec, data, image, illum, refl=None,
+             snap_kind: int = _lib.ST_SNAP_BF16, snaps=None, snap_amax=None) -> int:
+    """Reverse-time migration of one shot on device tensors: data FP32
+    [nt, nrec]; image / illum / refl FP32 interior (nx*ny*nz) outputs. With
+    snaps=None the library keeps its own snapshot store."""
+    shot, _keep = _shot_c(src, wavelet, nt, rec)
+    ptr = lambda t: t.data_ptr() if t is not None else None  # noqa: E731
+    return call("st_rtm_shot", solver.handle, C.byref(shot), data.data_ptr(), snap_kind, ptr(snaps),
+                ptr(snap_amax), image.data_ptr(), illum.data_ptr(), ptr(refl))
+
+
+def rtm_shot_host(solver: WaveEquationSolver, vel_ref, src, wavelet, nt: int, rec, data_host,
+                  snap_kind: int = _lib.ST_SNAP_BF16, want=("image", "illumination", "reflectivity")):
+    """Host-buffer RTM (every copy included). data_host: FP32 numpy [nt, nrec]
+    (pinned memory gives full copy speed). Returns a dict of FP64 interior
+    arrays named like RTMImageCondition (rtm/rtm_engine.h:25-29)."""
+    shot, _keep = _shot_c(src, wavelet, nt, rec)
+    n = solver.nx * solver.ny * solver.nz
+    outs = {k: np.empty(n) for k in want}
+    nul = C.cast(None, C.POINTER(C.c_double))
+    if vel_ref is None:
+        vp, nv = nul, 0
+    else:
+        v = np.ascontiguousarray(vel_ref, dtype=np.float64).reshape(-1)
+        vp, nv = _dptr(v), v.size
+    d = data_host if isinstance(data_host, np.ndarray) else data_host.numpy()
+    assert d.dtype == np.float32 and d.flags.c_contiguous
+    call("st_rtm_shot_host", solver.handle, vp, nv, C.byref(shot), d.ctypes.data_as(C.POINTER(C.c_float)),
+         snap_kind, *(_dptr(outs[k]) if k in outs else nul for k in ("image", "illumination", "reflectivity")))
+    return outs
+
+
 def shot_forward_host(solver: WaveEquationSolver, vel_ref, src, wavelet, nt: int, rec) -> np.ndarray:
     """Host-buffer forward shot (all copies included): velocity in the
     reference layout (or None), returns FP64 seismograms [nt, nrec]."""

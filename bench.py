@@ -1,0 +1,383 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 seismic hot path on its headline workload.
+
+Workload (one bench step = one shot): reverse-time migration on a 256^3 grid,
+2000 time steps -- the forward pass with a fused BF16 (+per-snapshot scale)
+snapshot store of every step, then the exact-adjoint backward pass with the
+zero-lag cross-correlation imaging fused in, then the reflectivity. The
+metric is stencil throughput in Gpts/s (interior points x time steps of both
+passes per second); HBM GB/s and the roofline fraction of the dominant kernel
+are reported beside it. Inputs are seeded synthetic models (4 layers
+1500-4500 m/s, two +-10% Gaussian anomalies, 15 Hz Ricker at (128,128,5),
+128x128 receivers on z = 5; observed data modelled on the true model,
+migration on the model smoothed with sigma 6 cells).
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Multi-GPU (torchrun): every rank migrates its own shot (shot-parallel, no
+collective on the data path); value = all ranks' points / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "03-seismic-tomography-compute_gb300")
+for _p in (PKG, os.path.join(REPO, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+ALG_BYTES_FWD = 18   # read u, prev, c + write out (16) + BF16 snapshot store (2)
+ALG_BYTES_BWD = 34   # 16 + BF16 snapshot read (2) + image and illumination read-modify-write (16)
+METRIC = "stencil Gpts/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--nt", type=int, default=2000, help="time steps per shot (2000 = the workload)")
+    ap.add_argument("--n", type=int, default=256, help="grid edge (256 = the workload)")
+    ap.add_argument("--snap", choices=["bf16", "fp16", "fp32"], default="bf16")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU sample time")
+    return ap.parse_args()
+
+
+def workload(n, nt):
+    from seismic_engine import workloads as wl
+    if n == 256:
+        w = wl.rtm_256(nt)
+    else:
+        w = wl.rtm_256(nt)
+        v = wl.layered(n, n, n, [1500.0, 2500.0, 3500.0, 4500.0])
+        wl.random_anomalies(v, 2, seed=2)
+        w.nx = w.ny = w.nz = n
+        w.vel = v
+        w.dt = wl.cfl_dt(10.0, float(v.max()))
+        rec = wl.ReceiverGrid(0, 2, n // 2, 0, 2, n // 2, 5)
+        w.shots = [wl.ShotSpec((n // 2, n // 2, 5), wl.ricker(15.0, w.dt, nt), rec)]
+        w.name = f"rtm-{n}^3"
+    w.vel_migration = wl.smooth(w.vel, 6.0)
+    return w
+
+
+def config_dict(w, snap, n_gpus):
+    return {
+        "workload": f"{w.name} x {w.nt} steps (forward + exact adjoint with fused imaging)",
+        "grid": [w.nx, w.ny, w.nz], "nt": w.nt, "dx_m": w.d, "dt_s": w.dt,
+        "snapshots": f"{snap}+per-snapshot scale, store-all",
+        "receivers": f"{w.shots[0].rec.nx}x{w.shots[0].rec.ny} on z={w.shots[0].rec.z}",
+        "sponge": [w.sponge_width, w.sponge_damping],
+        "l2": "inputs larger than L2: 4 FP32 fields of %.0f MB each + %.0f GB of snapshots" % (
+            (w.nx + 2) * (w.ny + 2) * (w.nz + 8) * 4 / 1e6,
+            w.nx * w.ny * w.nz * w.nt * (4 if snap == "fp32" else 2) / 1e9),
+        "parallelism": "shot-parallel replicas" if n_gpus > 1 else "single GPU, one device-resident domain",
+    }
+
+
+def dist_setup(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-i", str(self.dev),
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in getattr(self, "lines", []):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(kernel_key):
+    """DRAM bytes per launch of a kernel from the committed ncu summary, or None."""
+    p = os.path.join(REPO, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    e = d.get(kernel_key)
+    return None if e is None else e.get("bytes_per_launch_full")
+
+
+# ---------------------------------------------------------------- CPU legs
+def cpu_rtm_sample(w, nt_sample):
+    """Oracle port (the reference's step restated in C, OpenMP over the host
+    cores): forward stepping with states kept + exact adjoint with imaging,
+    nt_sample steps of each on the workload's grid. Returns seconds."""
+    from oracle import Oracle
+    from seismic_engine import workloads as wl
+    o = Oracle()
+    g = o.grid(w.nx, w.ny, w.nz, w.d, w.d, w.d, w.dt, w.sponge_width, w.sponge_damping)
+    shot = w.shots[0]
+    vel = wl.to_reference_layout(w.vel_migration)
+    rec = shot.rec.coords()
+    data = np.random.default_rng(0).standard_normal((nt_sample, rec.shape[0])) * 1e-3
+    t0 = time.perf_counter()
+    f = o.run(g, vel, nt_sample, np.array([shot.src]), shot.wavelet[:nt_sample, None], rec, keep_states=True)
+    o.adjoint(g, vel, nt_sample, rec, data, states=f["states"], want_image=True)
+    return time.perf_counter() - t0, o.num_threads()
+
+
+def cpu_baseline(w, target_s):
+    probe_steps = 2
+    t, cores = cpu_rtm_sample(w, probe_steps)
+    per_step = t / probe_steps
+    nt_s = int(max(2, min(60, target_s / per_step)))
+    t, cores = cpu_rtm_sample(w, nt_s)
+    pts = 2.0 * nt_s * w.nx * w.ny * w.nz
+    return {"value": pts / t / 1e9, "unit": "Gpts/s", "cores": cores, "kind": "port",
+            "sample": f"{nt_s} forward + {nt_s} adjoint/imaging steps of the {w.nx}^3 workload in FP64 "
+                      f"({t:.1f} s; the reference's CPU step restated in C, OpenMP over {cores} threads)"}
+
+
+def run_reference(args):
+    world, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    if rank != 0:
+        return 0
+    w = workload(args.n, args.nt)
+    # each step: a bounded RTM sample sized so the whole run ends in minutes
+    probe, cores = cpu_rtm_sample(w, 2)
+    nt_s = int(max(2, min(40, 20.0 / (probe / 2))))
+    times = []
+    for i in range(args.warmup + args.steps):
+        t, cores = cpu_rtm_sample(w, nt_s)
+        if i >= args.warmup:
+            times.append(t)
+    el = sum(times)
+    pts = 2.0 * nt_s * w.nx * w.ny * w.nz * args.steps
+    value = pts / el / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Gpts/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded layered model + Gaussian anomalies)",
+        "config": config_dict(w, args.snap, world),
+        "cpu_baseline": {"value": value, "unit": "Gpts/s", "cores": cores, "kind": "port",
+                         "sample": f"each step: {nt_s} forward + {nt_s} adjoint/imaging steps of the "
+                                   f"{w.nx}^3 workload in FP64 (the reference's CPU step restated in C; "
+                                   f"the reference sources are not available on this machine)"},
+        "e2e": {"value": value, "unit": "Gpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- GPU leg
+def run_gpu(args):
+    import torch
+    import seismic_engine as se
+    from seismic_engine import _lib
+
+    world, rank, local = dist_setup(args)
+    w = workload(args.n, args.nt)
+    shot = w.shots[0]
+    rec = shot.rec
+    snap_kind = {"bf16": _lib.ST_SNAP_BF16, "fp16": _lib.ST_SNAP_FP16, "fp32": _lib.ST_SNAP_FP32}[args.snap]
+    grid = se.GridParams(w.nx, w.ny, w.nz, w.d, w.d, w.d)
+    cfg = se.SolverConfig(dt=w.dt, nt=w.nt, sponge_width=w.sponge_width, sponge_damping=w.sponge_damping)
+    s = se.WaveEquationSolver(grid, cfg, device=torch.cuda.current_device())
+    vel_true = se.workloads.to_reference_layout(w.vel)
+    vel_mig = se.workloads.to_reference_layout(w.vel_migration)
+    # observed data (input preparation, untimed)
+    s.set_velocity_field(vel_true)
+    data = torch.zeros((w.nt, rec.count), device="cuda")
+    se.shot_forward(s, shot.src, shot.wavelet, w.nt, rec, seis=data)
+    s.set_velocity_field(vel_mig)
+    npts = w.nx * w.ny * w.nz
+    image = torch.zeros(npts, device="cuda")
+    illum = torch.zeros(npts, device="cuda")
+    refl = torch.zeros(npts, device="cuda")
+    stream = torch.cuda.ExternalStream(s.stream_ptr())
+    L = _lib.load()
+
+    def step():
+        se.rtm_shot(s, shot.src, shot.wavelet, w.nt, rec, data, image, illum, refl, snap_kind=snap_kind)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    import ctypes as C
+    lc0 = C.c_longlong()
+    L.st_launch_count(C.byref(lc0))
+    ph = (C.c_float * 2)()
+    fwd_ms, bwd_ms = [], []
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+            L.st_solver_last_phase_ms(s.handle, ph)
+            fwd_ms.append(ph[0])
+            bwd_ms.append(ph[1])
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    el_ms = max_over_ranks(ev0.elapsed_time(ev1), world)
+    lc1 = C.c_longlong()
+    L.st_launch_count(C.byref(lc1))
+    launches = lc1.value - lc0.value
+    pts_step = 2.0 * w.nt * npts
+    value = world * pts_step * args.steps / (el_ms / 1e3) / 1e9
+    hbm_peak, peak_kind = measured_peaks()
+    bwd_launch_ms = statistics.mean(bwd_ms) / w.nt
+    fwd_launch_ms = statistics.mean(fwd_ms) / w.nt
+    bw_bwd = ALG_BYTES_BWD * npts / (bwd_launch_ms / 1e3) / 1e9
+    bw_fwd = ALG_BYTES_FWD * npts / (fwd_launch_ms / 1e3) / 1e9
+    alg_total = (ALG_BYTES_FWD + ALG_BYTES_BWD) * npts * w.nt * args.steps
+    traffic = profile_traffic("fd_step_adjoint_image_bf16_256")
+    line = {
+        "metric": METRIC, "value": value, "unit": "Gpts/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": el_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded layered model + Gaussian anomalies, Ricker source)",
+        "config": config_dict(w, args.snap, world),
+        "hbm_gbs_algorithmic": alg_total / (el_ms / 1e3) / 1e9,
+        "roofline": {"bound": "hbm", "kernel": "fd_step_kernel<SNAP_NONE, BF16, imaging> (adjoint step + imaging)",
+                     "achieved": bw_bwd, "peak": hbm_peak, "unit": "GB/s", "frac": bw_bwd / hbm_peak,
+                     "peak_kind": f"{peak_kind} copy bandwidth", "traffic": traffic,
+                     "alg_bytes_per_launch": ALG_BYTES_BWD * npts, "launch_ms": bwd_launch_ms},
+        "roofline_forward": {"bound": "hbm", "kernel": "fd_step_kernel<BF16, NONE> (forward step + snapshot store)",
+                             "achieved": bw_fwd, "peak": hbm_peak, "unit": "GB/s", "frac": bw_fwd / hbm_peak,
+                             "alg_bytes_per_launch": ALG_BYTES_FWD * npts, "launch_ms": fwd_launch_ms},
+        "phases_ms_per_step": {"forward": statistics.mean(fwd_ms), "backward": statistics.mean(bwd_ms)},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if not args.no_e2e:
+        # the same metric through the host C-ABI entry: velocity and receiver data copied in from pinned
+        # host memory, the image copied out, every step
+        vel_pin = torch.from_numpy(vel_mig).pin_memory()
+        data_pin = data.cpu().pin_memory()
+        times = []
+        out = None
+        for i in range(1 + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = se.rtm_shot_host(s, vel_pin.numpy(), shot.src, shot.wavelet, w.nt, rec, data_pin.numpy(),
+                                   snap_kind=snap_kind, want=("image",))
+            torch.cuda.synchronize()
+            if i > 0:
+                times.append(time.perf_counter() - t0)
+        e2e_s = max_over_ranks(sum(times), world)
+        line["e2e"] = {"value": world * pts_step * args.steps / e2e_s / 1e9, "unit": "Gpts/s",
+                       "h2d_bytes_per_step": int(vel_mig.nbytes + data_pin.numel() * 4),
+                       "d2h_bytes_per_step": int(npts * 8),
+                       "api": "st_rtm_shot_host (include/seismic_gb300.h)"}
+        img_dev = image.cpu().numpy().astype(np.float64)
+        line["e2e"]["matches_device_path"] = bool(
+            np.allclose(out["image"], img_dev, rtol=1e-5, atol=1e-6 * np.abs(img_dev).max()))
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    s.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -161,6 +161,12 @@ int st_solver_fault_stats(st_solver* s, st_fault_stats* out);
 int st_solver_device_field(st_solver* s, int which, float** out);
 /* The CUDA stream the handle orders its work on (a cudaStream_t). */
 int st_solver_stream(st_solver* s, void** out);
+/* Device time of the two phases of the last st_rtm_shot on this handle, from
+ * CUDA events recorded on its stream: out[0] = forward pass (fused steps with
+ * snapshot store), out[1] = backward pass (fused adjoint steps with imaging). */
+int st_solver_last_phase_ms(st_solver* s, float out[2]);
+/* Kernels this library has launched in the process so far. */
+int st_launch_count(long long* out);
 
 /* Forward modelling of one shot, one fused kernel launch per step: leapfrog
  * update, sponge, source injection, receiver sampling and (snap_kind != NONE)
@@ -176,6 +182,13 @@ int st_shot_forward(st_solver* s, const st_shot* shot, float* seis, int snap_kin
  * layout (FP64, may be NULL to keep the current model), seismograms returned
  * as FP64 [nt][nrec] on the host. Includes all host<->device copies. */
 int st_shot_forward_host(st_solver* s, const double* vp, int64_t vp_count, const st_shot* shot, double* seis_host);
+
+/* Exact transpose of the wavelet -> seismogram map of st_shot_forward: runs
+ * the discrete adjoint backward from receiver data (device FP32 [nt][nrec])
+ * and returns src_trace[t] = dJ/dw_t for J = <seismograms, data> (device
+ * FP32 [nt]). The reference's step_adjoint (wave_equation.cpp:78-98) is the
+ * forward operator; this entry point is its true adjoint. */
+int st_shot_adjoint(st_solver* s, const st_shot* shot, const float* data, float* src_trace);
 
 /* Reverse-time migration of one shot with the exact discrete adjoint: forward
  * pass storing every post-injection field V_t (snap_kind BF16/FP16/FP32 with

@@ -114,10 +114,11 @@ int orc64_adjoint(const orc_grid* g, const double* vel, int nt, int nrec, const 
         }
         if (states && (image || illum || grad_c)) {
             const double* V = states + (int64_t)t * n;
-            int64_t k = 0;
+#pragma omp parallel for collapse(2) schedule(static)
             for (int64_t ix = 1; ix <= g->nx; ++ix)
                 for (int64_t iy = 1; iy <= g->ny; ++iy)
-                    for (int64_t iz = 1; iz <= g->nz; ++iz, ++k) {
+                    for (int64_t iz = 1; iz <= g->nz; ++iz) {
+                        const int64_t k = ((ix - 1) * g->ny + (iy - 1)) * g->nz + (iz - 1);
                         const int64_t i = ix * P + iy * NZh + iz;
                         double f = isfinite(V[i]) ? V[i] : 0.0;
                         double a = isfinite(aC[i]) ? aC[i] : 0.0;
@@ -131,8 +132,12 @@ int orc64_adjoint(const orc_grid* g, const double* vel, int nt, int nrec, const 
                         }
                     }
         }
-        for (int64_t i = 0; i < n; ++i) cl[i] = c[i] * aC[i];
-        for (int64_t i = 0; i < n; ++i) nC[i] = 0.0;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; ++i) {
+            cl[i] = c[i] * aC[i];
+            nC[i] = 0.0;
+        }
+#pragma omp parallel for collapse(2) schedule(static)
         for (int64_t ix = 1; ix <= g->nx; ++ix)
             for (int64_t iy = 1; iy <= g->ny; ++iy)
                 for (int64_t iz = 1; iz <= g->nz; ++iz) {
@@ -143,6 +148,7 @@ int orc64_adjoint(const orc_grid* g, const double* vel, int nt, int nrec, const 
                                  (cl[i + 1] - 2.0 * cl[i] + cl[i - 1]) * idz2;
                     nC[i] = aP[i] + 2.0 * aC[i] + lap;
                 }
+#pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n; ++i) aP[i] = -D[i] * aC[i];
         double* tmp = aC;
         aC = nC;
