@@ -1,0 +1,111 @@
+// Internal declarations of the sparse path (CSR build, SpMV, Krylov solves).
+#pragma once
+
+#include "st_common.cuh"
+
+#include <vector>
+
+namespace stg {
+
+// Device CSR: int64 row pointers, int32 columns, FP32 values.
+struct DevCsr {
+    long long rows = 0, cols = 0, nnz = 0;
+    long long* row_ptr = nullptr;
+    int* col = nullptr;
+    float* val = nullptr;
+    void release() {
+        cudaFree(row_ptr);
+        cudaFree(col);
+        cudaFree(val);
+        row_ptr = nullptr;
+        col = nullptr;
+        val = nullptr;
+    }
+};
+
+// Scratch allocations freed together (kernels using them must have finished).
+class DeviceBuffers {
+   public:
+    ~DeviceBuffers() {
+        for (void* p : ptrs_) cudaFree(p);
+    }
+    void* get(size_t bytes) {
+        void* p = nullptr;
+        if (cudaMalloc(&p, bytes ? bytes : 1) != cudaSuccess) {
+            cudaGetLastError();
+            failed_bytes_ = bytes;
+            return nullptr;
+        }
+        ptrs_.push_back(p);
+        return p;
+    }
+    int fail() {
+        set_error("device allocation of %zu bytes failed", failed_bytes_);
+        return ST_ERR_ALLOC;
+    }
+
+   private:
+    std::vector<void*> ptrs_;
+    size_t failed_bytes_ = 0;
+};
+
+// FP64 accumulators of one CG iteration (three rotating slots).
+struct CgAcc {
+    double pq;   // <p, A p>
+    double rr;   // <r, r> after the update
+    double rzn;  // <r, z> after the update
+};
+
+struct CgScalars {
+    CgAcc acc[3];
+    double bb;   // <b, b>
+    double rel;  // sqrt(rr)/||b|| of the last iteration
+    int iters;
+    int done;
+    int breakdown;
+    int pad_;
+};
+
+// Operator and preconditioner of one solve: A (square) or A^T A + lam I
+// (A rectangular, AT its explicit transpose); dinv = Jacobi diagonal or null.
+struct CgProblem {
+    const DevCsr* A = nullptr;
+    const DevCsr* AT = nullptr;
+    double lam = 0.0;
+    long long n = 0;
+    const float* b = nullptr;
+    float* x = nullptr;
+    const float* dinv = nullptr;
+};
+
+struct CgWork {
+    float *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *t = nullptr;
+    CgScalars* sc = nullptr;
+};
+
+struct CgResult {
+    int iters = 0;
+    double rel = 0.0;
+    int breakdown = 0;
+};
+
+template <class TI, class TV>
+int build_csr(long long rows, long long cols, long long n, const TI* r, const TI* c, const TV* v, bool pad,
+              DevCsr* out, cudaStream_t st);
+int build_transpose(const DevCsr& A, DevCsr* T, cudaStream_t st);
+int launch_spmv(const DevCsr& A, const float* x, float* y, const float* add, float add_scale, const float* pdot,
+                double* dot_acc, const int* done, cudaStream_t st);
+int launch_f64_to_f32(const double* a, float* b, long long n, cudaStream_t st);
+int launch_f32_to_f64(const float* a, double* b, long long n, cudaStream_t st);
+int launch_jacobi(const DevCsr& A, float* dinv, cudaStream_t st);
+int launch_normal_jacobi(const DevCsr& AT, double lam, float* dinv, cudaStream_t st);
+int launch_scale(float* v, long long n, float a, cudaStream_t st);
+int launch_add_diag(DevCsr& A, float a, cudaStream_t st);
+int launch_sumsq(const float* v, long long n, double* acc, cudaStream_t st);
+int launch_residual(float* out, const float* b, const float* Ax, long long n, cudaStream_t st);
+int launch_dot64(const double* a, const double* b, long long n, double* acc, cudaStream_t st);
+int launch_fd_triplets(const double* vel, long long nx, long long ny, long long nz, double idx2, double idy2,
+                       double idz2, double dt2, long long* tr, long long* tc, double* tv, cudaStream_t st);
+int run_cg(const CgProblem& P, CgWork& W, int max_iter, double tol, int check_every, CgResult* res, cudaStream_t st);
+
+}  // namespace stg

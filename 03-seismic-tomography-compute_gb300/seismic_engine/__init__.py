@@ -11,6 +11,11 @@ from .wave import (  # noqa: F401
     FaultStats, GridParams, HealthStatus, PropagationResult, SolverConfig, StepResult, WaveEquationSolver,
     WaveField, field_layout, rtm_shot, rtm_shot_host, shot_adjoint, shot_forward, shot_forward_host,
 )
+from .sparse import CSRMatrix, SparseOps, compute_fd_stencil, normal_cg_device  # noqa: F401
+from .fields import check_field_health, clamp_field_safe, repair_field_nan  # noqa: F401
+from .config import (  # noqa: F401
+    InversionConfig, ModelConfig, TomographyConfig, load_config,
+)
 from . import workloads  # noqa: F401
 
 __version__ = "1.2.0+gb300"

@@ -109,6 +109,34 @@ SIGNATURES = {
     "st_shot_adjoint": [_vp, C.POINTER(ShotC), _vp, _vp],
     "st_rtm_shot": [_vp, C.POINTER(ShotC), _vp, C.c_int, _vp, _vp, _vp, _vp, _vp],
     "st_rtm_shot_host": [_vp, _d, C.c_int64, C.POINTER(ShotC), _f, C.c_int, _d, _d, _d],
+    # sparse
+    "st_csr_create": [C.c_int64, C.c_int64, C.c_int64, C.c_int, C.POINTER(_vp)],
+    "st_csr_destroy": [_vp],
+    "st_csr_build_from_triplets": [_vp, C.c_int64, C.c_int64, C.c_int64, _i64, _i64, _d, C.c_int],
+    "st_csr_build_from_triplets_device": [_vp, C.c_int64, C.c_int64, C.c_int64, _vp, _vp, _vp, C.c_int],
+    "st_csr_build_fd_stencil_7point": [_vp, C.c_int64, C.c_int64, C.c_int64, _d, C.c_double, C.c_double,
+                                       C.c_double, C.c_double, C.c_int],
+    "st_csr_shape": [_vp, _i64],
+    "st_csr_get": [_vp, _i64, _i64, _d],
+    "st_csr_device_arrays": [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)],
+    "st_csr_stream": [_vp, C.POINTER(_vp)],
+    "st_csr_spmv": [_vp, _d, C.c_int64, _d],
+    "st_csr_spmv_transpose": [_vp, _d, C.c_int64, _d],
+    "st_csr_spmv_device": [_vp, C.c_int, _vp, _vp],
+    "st_csr_frobenius_norm": [_vp, _d],
+    "st_csr_scale": [_vp, C.c_double],
+    "st_csr_add_diagonal": [_vp, C.c_double],
+    "st_csr_clone": [_vp, C.POINTER(_vp)],
+    "st_cg": [_vp, _d, C.c_int64, C.c_int, C.c_double, C.c_int, _d, C.POINTER(C.c_int), _d],
+    "st_cg_device": [_vp, _vp, _vp, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int), _d],
+    "st_normal_cg_device": [_vp, _vp, C.c_double, C.c_int, C.c_double, C.c_int, _vp, _vp, C.POINTER(C.c_int), _d,
+                            _d],
+    "st_dot": [_d, _d, C.c_int64, C.c_int, _d],
+    "st_smooth_gradient": [_d, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_int, _d],
+    "st_smooth_gradient_device": [_vp, C.c_int64, C.c_int64, C.c_int64, C.c_double, _vp, _vp, _vp],
+    "st_field_count_nonfinite": [_d, C.c_int64, C.c_int, _i64],
+    "st_field_clamp": [_d, C.c_int64, C.c_double, C.c_double, C.c_int],
+    "st_field_repair_nan": [_d, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int, C.c_double, C.c_int],
 }
 _RESTYPES = {"st_last_error": C.c_char_p}
 

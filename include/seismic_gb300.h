@@ -212,6 +212,92 @@ int st_rtm_shot(st_solver* s, const st_shot* shot, const float* data, int snap_k
 int st_rtm_shot_host(st_solver* s, const double* vp, int64_t vp_count, const st_shot* shot, const float* data_host,
                      int snap_kind, double* image_host, double* illum_host, double* refl_host);
 
+/* ------------------------------------------------ seismic::CSRMatrix face */
+/* Device CSR: int64 row pointers, int32 column indices, FP32 values. Host
+ * entry points take the reference's int64 indices and FP64 values. */
+typedef struct st_csr st_csr;
+
+/* Replaces CSRMatrix(rows, cols, nnz) (sparse/csr_matrix.cpp:19-23); the
+ * default CSRMatrix() is st_csr_create(0, 0, 0, ...). Entries are zeroed. */
+int st_csr_create(int64_t rows, int64_t cols, int64_t nnz, int device, st_csr** out);
+int st_csr_destroy(st_csr* m);
+/* Replaces build_from_triplets (csr_matrix.cpp:25-72): entries outside
+ * [0,rows)x[0,cols) dropped, rows sorted by column, duplicates summed in
+ * input order; row_ptr / col_ind bit-exact with the reference. pad != 0
+ * applies pad_to_alignment (:223-264: when it fires, every row is padded to a
+ * multiple of 8 with col = row, value 0); it is refused with ST_ERR_ARG when
+ * it would fire on a matrix with more rows than columns. */
+int st_csr_build_from_triplets(st_csr* m, int64_t rows, int64_t cols, int64_t n, const int64_t* row_idx,
+                               const int64_t* col_idx, const double* values, int pad);
+/* The same from device triplets (int32 indices, FP32 values), e.g. the ray
+ * matrix generator's output. */
+int st_csr_build_from_triplets_device(st_csr* m, int64_t rows, int64_t cols, int64_t n, const int32_t* row_idx,
+                                      const int32_t* col_idx, const float* values, int pad);
+/* Replaces build_fd_stencil_7point (csr_matrix.cpp:74-116); velocity is the
+ * nx*ny*nz interior on the host. */
+int st_csr_build_fd_stencil_7point(st_csr* m, int64_t nx, int64_t ny, int64_t nz, const double* velocity, double dx,
+                                   double dy, double dz, double dt, int pad);
+/* rows(), cols(), nnz() (csr_matrix.h:32-34): out = {rows, cols, nnz}. */
+int st_csr_shape(st_csr* m, int64_t out[3]);
+/* row_ptr(), col_ind(), values() (csr_matrix.h:36-38) copied to the host (any may be NULL). */
+int st_csr_get(st_csr* m, int64_t* row_ptr, int64_t* col_ind, double* values);
+/* Device arrays of the matrix (borrowed; valid until the next build). */
+int st_csr_device_arrays(st_csr* m, long long** row_ptr, int** col_ind, float** values);
+int st_csr_stream(st_csr* m, void** out);
+/* Replace spmv / spmv_transpose (csr_matrix.cpp:118-166; the transpose with
+ * its accumulator zeroed). Host FP64 vectors in and out. */
+int st_csr_spmv(st_csr* m, const double* x, int64_t nx, double* y);
+int st_csr_spmv_transpose(st_csr* m, const double* x, int64_t nx, double* y);
+/* y = A x (transpose = 0) or A^T x on device FP32 vectors, on the matrix's stream. */
+int st_csr_spmv_device(st_csr* m, int transpose, const float* x, float* y);
+/* Replace frobenius_norm / scale / add_diagonal (csr_matrix.cpp:168-193). */
+int st_csr_frobenius_norm(st_csr* m, double* out);
+int st_csr_scale(st_csr* m, double alpha);
+int st_csr_add_diagonal(st_csr* m, double alpha);
+/* Copy of a matrix (SparseOps::build_hessian_approx copies then adds the
+ * diagonal, sparse_ops.cpp:204-210). */
+int st_csr_clone(st_csr* m, st_csr** out);
+
+/* ------------------------------------------------ seismic::SparseOps face */
+/* Replace conjugate_gradient (jacobi = 0) and jacobi_preconditioned_cg
+ * (jacobi = 1) (sparse/sparse_ops.cpp:8-113): x0 = 0, stop when
+ * sqrt(<r,r>)/||b|| < tol after an update or when |<p,Ap>| < 1e-30; returns
+ * x0 = 0 when ||b|| < 1e-30. FP32 vectors, FP64 inner products and norms. */
+int st_cg(st_csr* A, const double* b, int64_t nb, int max_iter, double tol, int jacobi, double* x, int* iters,
+          double* final_rel);
+int st_cg_device(st_csr* A, const float* b, float* x, int max_iter, double tol, int jacobi, int* iters,
+                 double* final_rel);
+/* Tomography solve: (A^T A + lam I) x = A^T d for a rectangular A (no
+ * reference counterpart), Jacobi diagonal = column sums of A^2 + lam when
+ * jacobi != 0. rhs (may be NULL) receives A^T d; true_rel (may be NULL) the
+ * FP64 relative true residual ||A^T d - (A^T A + lam I) x|| / ||A^T d||. */
+int st_normal_cg_device(st_csr* A, const float* d, double lam, int max_iter, double tol, int jacobi, float* x,
+                        float* rhs, int* iters, double* final_rel, double* true_rel);
+/* Replaces dot_product (sparse_ops.cpp:172-187): FP64 inner product. */
+int st_dot(const double* a, const double* b, int64_t n, int device, double* out);
+/* Replaces smooth_gradient (sparse_ops.cpp:115-158): truncated Gaussian of
+ * radius floor(3 sigma), normalised per point by the in-bounds weight sum,
+ * computed as three normalised 1-D passes (the weights and the support
+ * factor per axis). FP64. n < nx*ny*nz gives zeros, as the reference. */
+int st_smooth_gradient(const double* g, int64_t n, int64_t nx, int64_t ny, int64_t nz, double sigma, int device,
+                       double* out);
+/* Device version on FP64 arrays (tmp: scratch of nx*ny*nz doubles). */
+int st_smooth_gradient_device(const double* g, int64_t nx, int64_t ny, int64_t nz, double sigma, double* out,
+                              double* tmp, void* stream);
+
+/* ------------------------------------- FaultTolerance helpers (FP64, host arrays) */
+/* check_field_health -> FaultTolerance::count_nan_inf (bindings.cpp:275-280,
+ * core/fault_tolerance.cpp:72-80). */
+int st_field_count_nonfinite(const double* data, int64_t n, int device, int64_t* out);
+/* clamp_field_safe -> FaultTolerance::clamp_field (bindings.cpp:282-289,
+ * fault_tolerance.cpp:86-96): non-finite -> 0, else clamped to [lo, hi]. In place. */
+int st_field_clamp(double* data, int64_t n, double lo, double hi, int device);
+/* repair_field_nan -> FaultTolerance::repair_field_nan (bindings.cpp:290-301,
+ * fault_tolerance.cpp:98-157), in the reference's sequential cell order. In
+ * place; nx*ny*nz must not exceed n. */
+int st_field_repair_nan(double* data, int64_t n, int64_t nx, int64_t ny, int64_t nz, int halo_width,
+                        double replace_value, int device);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,201 @@
+"""GPU parity of the sparse path (CSR build, SpMV, CG / PCG / normal-equation
+CG), the field-health helpers and the gradient smoothing, against the
+reference fixtures and the FP64 oracle, through the C ABI.
+
+Bars: CSR row_ptr / col_ind bit-exact; values equal to the FP32 rounding of
+the reference's FP64 sums (1 FP32 ulp where the FD stencil's FP64
+expressions may contract differently); SpMV relative error <= 1e-6 (FP32
+values and accumulation); CG solutions within 1e-5 relative of the FP64
+oracle's; fault helpers bit-exact; smoothing within 1e-12."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def se():
+    import importlib.util
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location(
+        "st_build", os.path.join(repo, "03-seismic-tomography-compute_gb300", "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.build()
+    import seismic_engine
+    return seismic_engine
+
+
+def f32(a):
+    return np.asarray(a, np.float64).astype(np.float32).astype(np.float64)
+
+
+def test_build_matches_reference_fixture(se, golden_dir):
+    g = np.load(os.path.join(golden_dir, "csr_small.npz"))
+    m = se.CSRMatrix().build_from_triplets(int(g["rows"]), int(g["cols"]), g["r"], g["c"], g["v"])
+    assert m.rows() == int(g["rows"]) and m.cols() == int(g["cols"]) and m.nnz() == g["col"].size
+    np.testing.assert_array_equal(m.row_ptr(), g["row_ptr"])
+    np.testing.assert_array_equal(m.col_ind(), g["col"])
+    np.testing.assert_array_equal(m.values(), f32(g["val"]))
+    y = m.spmv(g["x"])
+    assert np.linalg.norm(y - g["y"]) <= 1e-6 * np.linalg.norm(g["y"])
+
+
+@pytest.mark.parametrize("rows,cols,n,seed", [(3000, 2500, 200000, 0), (1, 70000, 150000, 1),
+                                              (50000, 7, 90000, 2), (5, 5, 0, 3), (0, 4, 10, 4)])
+def test_build_random_vs_oracle(se, oracle, rows, cols, n, seed):
+    rng = np.random.default_rng(seed)
+    r = rng.integers(-2, rows + 2, n)
+    c = rng.integers(-2, cols + 2, n)
+    dup = rng.integers(0, max(n, 1), n // 5) if n else np.zeros(0, np.int64)
+    r = np.concatenate([r, r[dup]]) if n else r
+    c = np.concatenate([c, c[dup]]) if n else c
+    v = rng.standard_normal(r.size)
+    m = se.CSRMatrix().build_from_triplets(rows, cols, r, c, v)
+    rp, col, val = oracle.csr_build(rows, cols, r, c, v)
+    np.testing.assert_array_equal(m.row_ptr(), rp)
+    np.testing.assert_array_equal(m.col_ind(), col)
+    np.testing.assert_array_equal(m.values(), f32(val))
+
+
+def test_pad_mode_vs_oracle(se, oracle):
+    rng = np.random.default_rng(5)
+    n = 300
+    r = rng.integers(0, n, 1500)
+    c = rng.integers(0, n, 1500)
+    v = rng.standard_normal(1500)
+    m = se.CSRMatrix().build_from_triplets(n, n, r, c, v, pad=True)
+    rp, col, val = oracle.csr_build(n, n, r, c, v, pad=True)
+    assert rp[-1] % 8 == 0 and m.nnz() == rp[-1]
+    np.testing.assert_array_equal(m.row_ptr(), rp)
+    np.testing.assert_array_equal(m.col_ind(), col)
+    np.testing.assert_array_equal(m.values(), f32(val))
+    with pytest.raises(se.SeismicError):
+        se.CSRMatrix().build_from_triplets(2 * n, n, r, c, v, pad=True)
+
+
+def fd_triplets(nx, ny, nz, vel, dx, dy, dz, dt):
+    """Triplets of build_fd_stencil_7point (csr_matrix.cpp:74-116) in its order."""
+    idx2, idy2, idz2, dt2 = 1 / dx ** 2, 1 / dy ** 2, 1 / dz ** 2, dt * dt
+    R, C, V = [], [], []
+    for ix in range(nx):
+        for iy in range(ny):
+            for iz in range(nz):
+                r = (ix * ny + iy) * nz + iz
+                v2 = vel[r] * vel[r] * dt2
+                R.append(r); C.append(r); V.append(-2.0 * v2 * (idx2 + idy2 + idz2) + 2.0)
+                for ok, cc, w in ((ix > 0, r - ny * nz, idx2), (ix < nx - 1, r + ny * nz, idx2),
+                                  (iy > 0, r - nz, idy2), (iy < ny - 1, r + nz, idy2),
+                                  (iz > 0, r - 1, idz2), (iz < nz - 1, r + 1, idz2)):
+                    if ok:
+                        R.append(r); C.append(cc); V.append(v2 * w)
+    return np.array(R), np.array(C), np.array(V)
+
+
+def test_fd_stencil_vs_oracle(se, oracle):
+    nx, ny, nz = 7, 6, 9
+    rng = np.random.default_rng(6)
+    vel = 1500 + 1000 * rng.random(nx * ny * nz)
+    m = se.compute_fd_stencil(nx, ny, nz, vel, 10.0, 12.0, 9.0, 1e-3)
+    R, Cc, V = fd_triplets(nx, ny, nz, vel, 10.0, 12.0, 9.0, 1e-3)
+    rp, col, val = oracle.csr_build(nx * ny * nz, nx * ny * nz, R, Cc, V)
+    np.testing.assert_array_equal(m.row_ptr(), rp)
+    np.testing.assert_array_equal(m.col_ind(), col)
+    np.testing.assert_allclose(m.values(), f32(val), rtol=2.0 ** -23, atol=0)
+
+
+def test_spmv_and_transpose_vs_oracle(se, oracle):
+    rng = np.random.default_rng(7)
+    rows, cols, n = 20000, 9000, 600000
+    r = rng.integers(0, rows, n)
+    c = rng.integers(0, cols, n)
+    v = rng.standard_normal(n).astype(np.float32).astype(np.float64)
+    m = se.CSRMatrix().build_from_triplets(rows, cols, r, c, v)
+    rp, col, val = oracle.csr_build(rows, cols, r, c, v)
+    om = oracle.csr(rows, cols, rp, col, f32(val))
+    x = rng.standard_normal(cols).astype(np.float32).astype(np.float64)
+    xt = rng.standard_normal(rows).astype(np.float32).astype(np.float64)
+    y, yr = m.spmv(x), oracle.spmv(om, x)
+    assert np.linalg.norm(y - yr) <= 1e-6 * np.linalg.norm(yr)
+    yt, ytr = m.spmv_transpose(xt), oracle.spmv_t(om, xt)
+    assert np.linalg.norm(yt - ytr) <= 1e-6 * np.linalg.norm(ytr)
+    assert abs(m.frobenius_norm() - np.linalg.norm(f32(val))) <= 1e-12 * np.linalg.norm(val)
+    m.scale(0.5)
+    np.testing.assert_array_equal(m.values(), f32(val) * 0.5)
+
+
+def spd_fd(se, oracle, n=(14, 12, 16), seed=8):
+    nx, ny, nz = n
+    vel = np.full(nx * ny * nz, 2000.0)
+    dt = 0.25 * 10.0 / 2000.0  # c = (v dt / d)^2 = 1/16: diagonally dominant, symmetric
+    R, Cc, V = fd_triplets(nx, ny, nz, vel, 10.0, 10.0, 10.0, dt)
+    rp, col, val = oracle.csr_build(nx * ny * nz, nx * ny * nz, R, Cc, V)
+    m = se.compute_fd_stencil(nx, ny, nz, vel, 10.0, 10.0, 10.0, dt)
+    return m, oracle.csr(nx * ny * nz, nx * ny * nz, rp, col, f32(val)), nx * ny * nz
+
+
+def test_cg_and_pcg_vs_oracle(se, oracle):
+    m, om, n = spd_fd(se, oracle)
+    b = np.random.default_rng(9).standard_normal(n)
+    for jac, fn in ((False, se.SparseOps.conjugate_gradient), (True, se.SparseOps.jacobi_preconditioned_cg)):
+        x = fn(m, b, 500, 1e-6)
+        it = se.SparseOps.last_iterations
+        xr, itr, relr = oracle.cg(om, b, 500, 1e-6, jacobi=jac)
+        assert abs(it - itr) <= 2, (it, itr)
+        assert np.linalg.norm(x - xr) <= 1e-5 * np.linalg.norm(xr)
+    # ||b|| < 1e-30 returns x0 = 0 with no iteration
+    assert not se.SparseOps.conjugate_gradient(m, np.zeros(n)).any() and se.SparseOps.last_iterations == 0
+    H = se.SparseOps.build_hessian_approx(m, 0.25)
+    d0 = m.values()[m.col_ind() == np.repeat(np.arange(n), np.diff(m.row_ptr()))]
+    d1 = H.values()[H.col_ind() == np.repeat(np.arange(n), np.diff(H.row_ptr()))]
+    np.testing.assert_allclose(d1, f32(d0 + 0.25), rtol=2.0 ** -23)
+
+
+def test_normal_equation_cg_vs_oracle(se, oracle):
+    import torch
+    rng = np.random.default_rng(10)
+    rows, cols = 6000, 2000
+    r = np.repeat(np.arange(rows), 12)
+    c = rng.integers(0, cols, r.size)
+    v = rng.random(r.size).astype(np.float32).astype(np.float64)
+    m = se.CSRMatrix().build_from_triplets(rows, cols, r, c, v)
+    rp, col, val = oracle.csr_build(rows, cols, r, c, v)
+    om = oracle.csr(rows, cols, rp, col, f32(val))
+    d = rng.standard_normal(rows).astype(np.float32)
+    lam = 1e-2
+    x = torch.zeros(cols, device="cuda")
+    rhs = torch.zeros(cols, device="cuda")
+    it, rel, true_rel = se.normal_cg_device(m, torch.from_numpy(d).cuda(), lam, x, 1000, 1e-6, True, rhs)
+    xr, itr, relr, rhsr = oracle.normal_cg(om, d.astype(np.float64), lam, 1000, 1e-6, jacobi=True)
+    assert rel < 1e-6 and true_rel < 1e-5
+    assert abs(it - itr) <= 3, (it, itr)
+    assert np.linalg.norm(rhs.cpu().numpy() - rhsr) <= 1e-6 * np.linalg.norm(rhsr)
+    assert np.linalg.norm(x.cpu().numpy() - xr) <= 1e-5 * np.linalg.norm(xr)
+
+
+def test_dot_product(se):
+    rng = np.random.default_rng(11)
+    a, b = rng.standard_normal(100003), rng.standard_normal(100003)
+    assert abs(se.SparseOps.dot_product(a, b) - float(np.dot(a, b))) <= 1e-12 * np.abs(a * b).sum()
+
+
+def test_fault_helpers_match_reference_fixture(se, golden_dir):
+    g = np.load(os.path.join(golden_dir, "fault_small.npz"))
+    nx, ny, nz = (int(v) for v in g["n"])
+    assert se.check_field_health(g["field"]) == int(g["nan_count"])
+    np.testing.assert_array_equal(se.clamp_field_safe(g["field"].copy(), -500.0, 500.0), g["clamped"])
+    rep = se.repair_field_nan(g["field"].copy(), nx + 2, ny + 2, nz + 2, 1, 0.0)
+    np.testing.assert_allclose(rep, g["repaired"], rtol=1e-15, atol=0)
+
+
+def test_smooth_gradient_vs_oracle(se, oracle):
+    rng = np.random.default_rng(12)
+    nx, ny, nz = 11, 9, 13
+    g = rng.standard_normal(nx * ny * nz)
+    for sigma in (0.7, 1.0, 2.0):
+        out = se.SparseOps.smooth_gradient(g, nx, ny, nz, sigma)
+        ref = oracle.smooth_gradient(g, nx, ny, nz, sigma)
+        np.testing.assert_allclose(out, ref, rtol=1e-12, atol=1e-13)
+    assert not se.SparseOps.smooth_gradient(np.ones(10), nx, ny, nz, 1.0).any()
