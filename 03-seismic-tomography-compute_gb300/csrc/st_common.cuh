@@ -143,6 +143,16 @@ __device__ __forceinline__ void tma_load_3d(void* smem_dst, const CUtensorMap* m
         : "memory");
 }
 
+// 4-D tiled TMA load (snapshot store: z, y, x, t). Same alignment rule on c0.
+__device__ __forceinline__ void tma_load_4d(void* smem_dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1,
+                                            int c2, int c3) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(smem_dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
+
 __device__ __forceinline__ void st_global_cs_f4(float* p, float4 v) {
     asm volatile("st.global.cs.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
                  : "memory");
@@ -176,6 +186,11 @@ using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t
                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 int get_encode_tiled(EncodeTiledFn* out);
+
+// 4-D tensor map over a snapshot store of nt compact interior fields
+// [t][x][y][z] of `kind` with box {bz, by, 1, 1}; needs nz * element size to
+// be a multiple of 16 bytes (TMA stride rule).
+int make_snap_map(CUtensorMap* map, const void* base, int kind, const Layout& L, long long nt, int bz, int by);
 
 // Builds a 3-D FP32 tensor map over a device field of layout L with box
 // {bz, by, 1} (innermost first).

@@ -16,7 +16,7 @@ struct StepArgs {
     float amp;               // amplitude clamp (WaveEquationSolver::amplitude_limit_)
     int sw;                  // sponge width
     const float* dtab;       // sponge factor by distance, dtab[d] for 0 <= d < sw
-    long long inj_idx;       // fused point injection into the written field, -1 = none
+    int inj_x, inj_y, inj_z; // fused point injection into the written field (interior), inj_x = -1: none
     float inj_val;
     int rz, rx0, rsx, rnx, ry0, rsy, rny;  // receiver grid on plane z = rz
     float* seis_row;         // receiver samples of the update (before injection/forcing), or null
@@ -28,28 +28,33 @@ struct StepArgs {
     const unsigned* amax_in;
     float* image;            // image += f * (centre / c)   (compact interior)
     float* illum;            // illum += f * f
+    float* grad;             // gradient: grad += (centre / c) * L(snapshot)   (compact interior)
+    int snap_t;              // gradient: time index of the snapshot in the store
     unsigned* flags;         // FLAG_GUARD / FLAG_TIMEOUT
     unsigned long long timeout_ns;
 };
 
-struct StencilMaps {
-    CUtensorMap cur;   // box {TZ+8, TY+2, 1} at (z0, y0, x)
-    CUtensorMap prev;  // box {TZ, TY, 1}
-    CUtensorMap c;     // box {TZ, TY, 1}
+// Tensor maps of one device field for the two tile heights of the stencil
+// kernels ([0]: 16-row tiles, [1]: 32-row tiles): cur boxes {TZ+8, rows+2, 1}
+// starting at (z0, y0, x), centre boxes {TZ, rows, 1}.
+struct FieldMaps {
+    CUtensorMap cur[2];
+    CUtensorMap ctr[2];
 };
 
-// Tile geometry of the stencil kernels (shared with the map builders).
+// Tile width of the stencil kernels along z.
 constexpr int FD_TZ = 64;
-constexpr int FD_TY = 16;
 
-int build_stencil_map_cur(CUtensorMap* m, const float* base, const Layout& L);
-int build_stencil_map_ctr(CUtensorMap* m, const float* base, const Layout& L);
+int build_field_maps(FieldMaps* m, const float* base, const Layout& L);
+// x-chunks per CTA column for a tile height and resident CTAs per SM.
+int fd_step_grid_chunks(const Layout& L, int tyv, int minb);
 
-// Launch one fused step. snap_out / snap_in are SnapKind values; image selects
-// the imaging epilogue. Returns ST_OK or a negative status.
-int launch_fd_step(const Layout& L, const CUtensorMap& mcur, const CUtensorMap& mprev, const CUtensorMap& mc,
-                   StepArgs a, int snap_out, int snap_in, bool image, cudaStream_t st);
-int fd_step_grid_chunks(const Layout& L);
+// Launch one fused step. snap_out / snap_in are SnapKind values; epi: 0 = none,
+// 1 = imaging, 2 = gradient (needs msnap, the snapshot store's map).
+int launch_fd_step(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
+                   StepArgs a, int snap_out, int snap_in, int epi, const CUtensorMap* msnap, cudaStream_t st);
+// 4-D map over a snapshot store for the gradient step's halo tile.
+int build_snap_map_grad(CUtensorMap* m, const void* base, int kind, const Layout& L, long long nt);
 
 // Small kernels.
 int launch_add_point(float* f, long long idx, float val, unsigned* amax_slot, cudaStream_t st);

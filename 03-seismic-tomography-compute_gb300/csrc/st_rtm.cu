@@ -93,10 +93,8 @@ int shot_forward_impl(st_solver* s, const st_shot* shot, float* seis, int snap_k
     for (int t = 0; t < nt; ++t) {
         StepArgs a = base_args(s, nullptr);
         float wn = 0.0f;
-        if (t + 1 < nt && finite_sample(shot->wavelet, shot->wavelet_len, t + 1, &wn)) {
-            a.inj_idx = src;
-            a.inj_val = wn;
-        }
+        if (t + 1 < nt && finite_sample(shot->wavelet, shot->wavelet_len, t + 1, &wn))
+            set_injection(a, shot->src_ix, shot->src_iy, shot->src_iz, wn);
         if (nrec > 0 && seis) {
             set_receivers(a, R);
             a.seis_row = seis + (size_t)t * (size_t)nrec;
@@ -106,7 +104,7 @@ int shot_forward_impl(st_solver* s, const st_shot* shot, float* seis, int snap_k
             a.amax_cur = amax + t;
             a.amax_next = amax + t + 1;
         }
-        ST_TRY(fused_step(s, a, snap_kind, SNAP_NONE, false));
+        ST_TRY(fused_step(s, a, snap_kind, SNAP_NONE, 0, nullptr));
     }
     return ST_OK;
 }
@@ -157,7 +155,7 @@ int rtm_backward_impl(st_solver* s, const st_shot* shot, const float* data, int 
             a.image = image;
             a.illum = illum;
         }
-        ST_TRY(fused_step(s, a, SNAP_NONE, imaging ? snap_kind : SNAP_NONE, imaging));
+        ST_TRY(fused_step(s, a, SNAP_NONE, imaging ? snap_kind : SNAP_NONE, imaging ? 1 : 0, nullptr));
         if (src_trace) {
             probe_kernel<<<1, 1, 0, s->stream>>>(s->f[s->ic], s->c, src, a.force_row, q_src, src_trace + t);
     ::stg::count_launch();

@@ -200,7 +200,7 @@ StepArgs base_args(st_solver* s, float* out) {
     a.amp = (float)s->amp_limit;
     a.sw = s->sw;
     a.dtab = s->dtab;
-    a.inj_idx = -1;
+    a.inj_x = -1;
     a.flags = s->flags;
     a.rsx = a.rsy = 1;
     return a;
@@ -208,9 +208,9 @@ StepArgs base_args(st_solver* s, float* out) {
 
 // One fused step out = f[in] from cur = f[ic], prev = f[ip]; then rotates the
 // roles so cur = out, prev = old cur, third = old prev.
-int fused_step(st_solver* s, StepArgs a, int snap_out, int snap_in, bool image) {
+int fused_step(st_solver* s, StepArgs a, int snap_out, int snap_in, int epi, const CUtensorMap* msnap) {
     a.out = s->f[s->in];
-    ST_TRY(launch_fd_step(s->L, s->map_cur[s->ic], s->map_ctr[s->ip], s->map_c, a, snap_out, snap_in, image,
+    ST_TRY(launch_fd_step(s->L, s->maps[s->ic], s->maps[s->ip], s->map_c, a, snap_out, snap_in, epi, msnap,
                           s->stream));
     const int old_c = s->ic, old_p = s->ip, old_n = s->in;
     s->ic = old_n;
@@ -276,7 +276,7 @@ int health_check(st_solver* s, int timestep, int* result) {
 int one_reference_step(st_solver* s, int timestep) {
     ST_TRY(refresh_coeff(s));
     StepArgs a = base_args(s, nullptr);
-    ST_TRY(fused_step(s, a, SNAP_NONE, SNAP_NONE, false));
+    ST_TRY(fused_step(s, a, SNAP_NONE, SNAP_NONE, 0, nullptr));
     unsigned fl = 0;
     ST_TRY(read_flags(s, &fl));
     int health = ST_OK;
@@ -400,11 +400,8 @@ int st_solver_create(const st_grid_params* grid, const st_solver_config* cfg, in
         ST_CUDA(cudaMemcpy(s->dtab, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice));
     }
     ST_TRY(zero_fields(s.get()));
-    for (int k = 0; k < 3; ++k) {
-        ST_TRY(build_stencil_map_cur(&s->map_cur[k], s->f[k], s->L));
-        ST_TRY(build_stencil_map_ctr(&s->map_ctr[k], s->f[k], s->L));
-    }
-    ST_TRY(build_stencil_map_ctr(&s->map_c, s->c, s->L));
+    for (int k = 0; k < 3; ++k) ST_TRY(build_field_maps(&s->maps[k], s->f[k], s->L));
+    ST_TRY(build_field_maps(&s->map_c, s->c, s->L));
     ST_CUDA(cudaStreamSynchronize(s->stream));
     *out = s.release();
     return ST_OK;
@@ -501,11 +498,8 @@ int st_solver_forward_propagate(st_solver* s, const double* wavelet, int64_t len
         const bool snap = (t % si == 0);
         float wn = 0.0f;
         const bool inj = t + 1 < nt && finite_sample(wavelet, len, t + 1, &wn);
-        if (inj && !snap) {
-            a.inj_idx = src;
-            a.inj_val = wn;
-        }
-        ST_TRY(fused_step(s, a, SNAP_NONE, SNAP_NONE, false));
+        if (inj && !snap) set_injection(a, s->L.nx / 2, s->L.ny / 2, s->L.nz / 2, wn);
+        ST_TRY(fused_step(s, a, SNAP_NONE, SNAP_NONE, 0, nullptr));
         if (snap) {
             ST_TRY(save_snapshot_dev(s));
             if (inj) ST_TRY(launch_add_point(s->f[s->ic], src, wn, nullptr, s->stream));
@@ -533,11 +527,9 @@ int st_solver_adjoint_propagate(st_solver* s, const double* residual, int64_t le
     for (int t = nt - 1; t >= 0; --t) {
         StepArgs a = base_args(s, nullptr);
         float wn = 0.0f;
-        if (t - 1 >= 0 && finite_sample(residual, len, t - 1, &wn)) {
-            a.inj_idx = src;
-            a.inj_val = wn;
-        }
-        ST_TRY(fused_step(s, a, SNAP_NONE, SNAP_NONE, false));
+        if (t - 1 >= 0 && finite_sample(residual, len, t - 1, &wn))
+            set_injection(a, s->L.nx / 2, s->L.ny / 2, s->L.nz / 2, wn);
+        ST_TRY(fused_step(s, a, SNAP_NONE, SNAP_NONE, 0, nullptr));
     }
     unsigned fl = 0;
     ST_TRY(read_flags(s, &fl));

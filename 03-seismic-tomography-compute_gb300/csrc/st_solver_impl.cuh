@@ -70,9 +70,8 @@ struct st_solver {
     unsigned* flags = nullptr;
     unsigned long long* counter = nullptr;
     double* dsum = nullptr;
-    CUtensorMap map_cur[3];
-    CUtensorMap map_ctr[3];
-    CUtensorMap map_c;
+    stg::FieldMaps maps[3];  // TMA maps of f[0..2]
+    stg::FieldMaps map_c;    // TMA maps of c
     bool coeff_dirty = true;
     std::vector<float*> snapshots;  // save_snapshot: interior FP32 copies
     st_fault_stats stats{};
@@ -97,10 +96,17 @@ int ensure_staging(st_solver* s);
 int refresh_coeff(st_solver* s);
 int read_flags(st_solver* s, unsigned* out);
 StepArgs base_args(st_solver* s, float* out);
-int fused_step(st_solver* s, StepArgs a, int snap_out, int snap_in, bool image);
+// epi: 0 none, 1 imaging, 2 gradient (msnap = the snapshot store's map)
+int fused_step(st_solver* s, StepArgs a, int snap_out, int snap_in, int epi, const CUtensorMap* msnap);
 int zero_fields(st_solver* s);
 long long dev_index(const st_solver* s, int64_t ix, int64_t iy, int64_t iz);
 bool finite_sample(const double* w, int64_t len, int64_t t, float* out);
+inline void set_injection(StepArgs& a, int64_t ix, int64_t iy, int64_t iz, float val) {
+    a.inj_x = (int)ix;
+    a.inj_y = (int)iy;
+    a.inj_z = (int)iz;
+    a.inj_val = val;
+}
 // Device scratch owned by the handle, grown on demand.
 int ensure_buffer(st_solver* s, void** buf, size_t* cap, size_t bytes);
 }  // namespace stg

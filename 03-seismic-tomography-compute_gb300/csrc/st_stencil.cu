@@ -19,39 +19,66 @@
 //   - BF16/FP16/FP32 snapshot store of the centre field with a per-snapshot
 //     scale (|max| tracked with one atomic per CTA),
 //   - zero-lag cross-correlation imaging image += f*a, illum += f*f with
-//     a = mu / c (RTMEngine::apply_image_condition, rtm/rtm_engine.cpp:24-57).
+//     a = mu / c (RTMEngine::apply_image_condition, rtm/rtm_engine.cpp:24-57),
+//   - the adjoint-state gradient grad_c += (mu / c) * L S of a forward
+//     snapshot S staged through TMA with its halo.
 //
-// Data movement: each CTA owns a TY x TZ (y,z) tile and marches along x (the
-// slowest axis), staging every x-plane of u (with a one-cell y/z halo), prev
-// and c in shared memory with TMA (cp.async.bulk.tensor, no multicast) in a
-// 4-deep mbarrier ring; u at x-1/x/x+1 rides in a register queue. HBM traffic
-// is 16 B per point (read u, prev, c; write out), plus the epilogue's bytes.
+// Data movement: each CTA owns a (16 or 32) x 64 (y,z) tile and marches along
+// x (the slowest axis), staging every x-plane of u (with a one-cell y/z halo),
+// prev and c in shared memory with TMA (cp.async.bulk.tensor, no multicast) in
+// a 3- or 4-deep mbarrier ring; u at x-1/x/x+1 rides in a register queue. HBM
+// traffic is 16 B per point (read u, prev, c; write out) plus the epilogue's.
 #include "st_kernels.cuh"
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstdarg>
+#include <cstdlib>
 #include <mutex>
+#include <type_traits>
 
 namespace stg {
 
 namespace {
 
-constexpr int TZ = FD_TZ;
-constexpr int TY = FD_TY;
-constexpr int TZ4 = TZ / 4;
-constexpr int NTHREADS = TZ4 * TY;  // 256
-constexpr int STAGES = 4;
+constexpr int TZ = FD_TZ;                     // 64 interior z per tile
+constexpr int TZ4 = TZ / 4;                   // threads along z (4 points each)
+constexpr int NTHREADS = TZ4 * 16;            // 256 threads: 16 thread rows x 16 z-groups
 constexpr int CUR_W = TZ + 8;
-constexpr int CUR_H = TY + 2;
-constexpr int CUR_BYTES = CUR_W * CUR_H * 4;
-constexpr int CUR_BYTES_PAD = ((CUR_BYTES + 127) / 128) * 128;
-constexpr int CTR_BYTES = TZ * TY * 4;
-constexpr int STAGE_BYTES = CUR_BYTES_PAD + 2 * CTR_BYTES;
-constexpr int STAGE_TX = CUR_BYTES + 2 * CTR_BYTES;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 128;
-constexpr int MIN_BLOCKS = 4;
+constexpr int DTAB_MAX = 512;                 // sponge widths up to this use a shared-memory table
+constexpr int EXTRA_BYTES = 128 + DTAB_MAX * 4;
+constexpr int SM_SMEM = 232448;               // shared memory per SM (227 KB usable per CTA)
 constexpr unsigned FULL = 0xffffffffu;
+
+enum Epilogue : int { EPI_NONE = 0, EPI_IMAGE = 1, EPI_GRAD = 2 };
+
+// Per-variant tiling. Forward variants give each thread 2 adjacent rows
+// (32-row tiles, 2 CTAs per SM): fewer instructions per point. The imaging
+// and gradient variants, whose epilogues read and write global memory
+// directly, give each thread 1 row (16-row tiles) so more warps per SM hide
+// those accesses. The gradient variant also stages the forward snapshot tile
+// with its halo (box starting 16 bytes left of the tile), in a 3-deep ring.
+template <int EPI, int SNAP_IN>
+struct Geo {
+    static constexpr int RPT = EPI == EPI_NONE ? 2 : 1;  // rows per thread
+    static constexpr int TYV = 16 * RPT;                 // tile rows
+    static constexpr int CUR_H = TYV + 2;
+    static constexpr int CUR_BYTES = CUR_W * CUR_H * 4;
+    static constexpr int CUR_BYTES_PAD = ((CUR_BYTES + 127) / 128) * 128;
+    static constexpr int CTR_BYTES = TZ * TYV * 4;
+    static constexpr int STAGES = EPI == EPI_GRAD ? 3 : 4;
+    static constexpr int SES = EPI == EPI_GRAD ? snap_bytes(SNAP_IN) : 0;
+    static constexpr int SW = EPI == EPI_GRAD ? (SES == 2 ? TZ + 16 : TZ + 8) : 0;
+    static constexpr int SOFF = EPI == EPI_GRAD ? (SES == 2 ? 8 : 4) : 0;
+    static constexpr int SNAP_TILE = SW * CUR_H * SES;
+    static constexpr int SNAP_TILE_PAD = ((SNAP_TILE + 127) / 128) * 128;
+    static constexpr int STAGE_BYTES = CUR_BYTES_PAD + 2 * CTR_BYTES + SNAP_TILE_PAD;
+    static constexpr int STAGE_TX = CUR_BYTES + 2 * CTR_BYTES + SNAP_TILE;
+    static constexpr int SMEM = STAGES * STAGE_BYTES + EXTRA_BYTES;
+    static constexpr int FIT = SM_SMEM / (SMEM + 1024);
+    static constexpr int MINB = FIT < 4 ? FIT : 4;       // resident CTAs per SM
+};
 
 template <int K>
 __device__ __forceinline__ float snap_load(const void* p, long long i) {
@@ -67,143 +94,304 @@ __device__ __forceinline__ void snap_store(void* p, long long i, float v) {
     else reinterpret_cast<float*>(p)[i] = v;
 }
 
-// Four consecutive values (8 B aligned for 16-bit kinds, 16 B for FP32).
+// Four consecutive snapshot values: 8 B for the 16-bit kinds, 16 B for FP32.
 template <int K>
-__device__ __forceinline__ void snap_store4(void* p, long long i, float4 v) {
+struct Snap4 {
+    using T = typename std::conditional<K == SNAP_FP32, float4, uint2>::type;
+};
+
+template <int K>
+__device__ __forceinline__ void snap_store4(void* p, long long i, const float v[4]) {
     if constexpr (K == SNAP_BF16) {
-        __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y), b = __floats2bfloat162_rn(v.z, v.w);
+        __nv_bfloat162 a = __floats2bfloat162_rn(v[0], v[1]), b = __floats2bfloat162_rn(v[2], v[3]);
         uint2 w;
         w.x = *reinterpret_cast<unsigned*>(&a);
         w.y = *reinterpret_cast<unsigned*>(&b);
         *reinterpret_cast<uint2*>(reinterpret_cast<__nv_bfloat16*>(p) + i) = w;
     } else if constexpr (K == SNAP_FP16) {
-        __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
+        __half2 a = __floats2half2_rn(v[0], v[1]), b = __floats2half2_rn(v[2], v[3]);
         uint2 w;
         w.x = *reinterpret_cast<unsigned*>(&a);
         w.y = *reinterpret_cast<unsigned*>(&b);
         *reinterpret_cast<uint2*>(reinterpret_cast<__half*>(p) + i) = w;
     } else {
-        *reinterpret_cast<float4*>(reinterpret_cast<float*>(p) + i) = v;
+        *reinterpret_cast<float4*>(reinterpret_cast<float*>(p) + i) = make_float4(v[0], v[1], v[2], v[3]);
     }
 }
 
 template <int K>
-__device__ __forceinline__ float4 snap_load4(const void* p, long long i) {
+__device__ __forceinline__ typename Snap4<K>::T snap_raw4(const void* p, long long i) {
+    if constexpr (K == SNAP_FP32) return *reinterpret_cast<const float4*>(reinterpret_cast<const float*>(p) + i);
+    else return *reinterpret_cast<const uint2*>(reinterpret_cast<const unsigned short*>(p) + i);
+}
+
+template <int K>
+__device__ __forceinline__ void snap_unpack4(const typename Snap4<K>::T& w, float f[4]) {
     if constexpr (K == SNAP_BF16) {
-        uint2 w = *reinterpret_cast<const uint2*>(reinterpret_cast<const __nv_bfloat16*>(p) + i);
-        __nv_bfloat162 a = *reinterpret_cast<__nv_bfloat162*>(&w.x), b = *reinterpret_cast<__nv_bfloat162*>(&w.y);
-        float2 fa = __bfloat1622float2(a), fb = __bfloat1622float2(b);
-        return make_float4(fa.x, fa.y, fb.x, fb.y);
+        uint2 ww = w;
+        const float2 a = __bfloat1622float2(*reinterpret_cast<__nv_bfloat162*>(&ww.x));
+        const float2 b = __bfloat1622float2(*reinterpret_cast<__nv_bfloat162*>(&ww.y));
+        f[0] = a.x; f[1] = a.y; f[2] = b.x; f[3] = b.y;
     } else if constexpr (K == SNAP_FP16) {
-        uint2 w = *reinterpret_cast<const uint2*>(reinterpret_cast<const __half*>(p) + i);
-        __half2 a = *reinterpret_cast<__half2*>(&w.x), b = *reinterpret_cast<__half2*>(&w.y);
-        float2 fa = __half22float2(a), fb = __half22float2(b);
-        return make_float4(fa.x, fa.y, fb.x, fb.y);
+        uint2 ww = w;
+        const float2 a = __half22float2(*reinterpret_cast<__half2*>(&ww.x));
+        const float2 b = __half22float2(*reinterpret_cast<__half2*>(&ww.y));
+        f[0] = a.x; f[1] = a.y; f[2] = b.x; f[3] = b.y;
     } else {
-        return *reinterpret_cast<const float4*>(reinterpret_cast<const float*>(p) + i);
+        f[0] = w.x; f[1] = w.y; f[2] = w.z; f[3] = w.w;
     }
 }
 
-__device__ __forceinline__ float f4get(const float4& v, int k) {
-    return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
-}
-__device__ __forceinline__ void f4set(float4& v, int k, float x) {
-    if (k == 0) v.x = x;
-    else if (k == 1) v.y = x;
-    else if (k == 2) v.z = x;
-    else v.w = x;
+// Shared-memory snapshot value (element offset e of a tile) as float.
+template <int K>
+__device__ __forceinline__ float snap_smem1(const unsigned char* tile, int e) {
+    if constexpr (K == SNAP_BF16) return __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(tile)[e]);
+    else if constexpr (K == SNAP_FP16) return __half2float(reinterpret_cast<const __half*>(tile)[e]);
+    else return reinterpret_cast<const float*>(tile)[e];
 }
 
-// The reference update of one point with its NaN/Inf guards
-// (wave_equation.cpp:342-399). `upd` is the damped previous value.
-__device__ __forceinline__ float point_update(float u, float upd, float xm, float xp, float ym, float yp, float zm,
-                                              float zp, float c, float ax, float ay, float az, float amp,
-                                              bool& fired) {
-    const float sx = xp + xm, sy = yp + ym, sz = zp + zm;
-    const float probe = (sx + sy) + (sz + u) + upd;
-    if (isfinite(probe)) {
-        // all eight inputs are finite (any NaN/Inf would propagate into probe)
-        const float lap = fmaf(-2.0f, u, sx) * ax + fmaf(-2.0f, u, sy) * ay + fmaf(-2.0f, u, sz) * az;
-        float nv = fmaf(2.0f, u, -upd) + c * lap;
-        if (!isfinite(nv)) {
-            nv = u;
-            fired = true;
-        }
-        return fminf(fmaxf(nv, -amp), amp);
+// Four consecutive shared-memory snapshot values at element offset e (aligned).
+template <int K>
+__device__ __forceinline__ void snap_smem4(const unsigned char* tile, int e, float f[4]) {
+    if constexpr (K == SNAP_FP32) {
+        const float4 v = *reinterpret_cast<const float4*>(reinterpret_cast<const float*>(tile) + e);
+        f[0] = v.x; f[1] = v.y; f[2] = v.z; f[3] = v.w;
+    } else {
+        const uint2 w = *reinterpret_cast<const uint2*>(reinterpret_cast<const unsigned short*>(tile) + e);
+        snap_unpack4<K>(w, f);
     }
-    // slow path: a non-finite input, or a finite sum that overflowed
+}
+
+__device__ __forceinline__ void f4_to(const float4& v, float a[4]) {
+    a[0] = v.x;
+    a[1] = v.y;
+    a[2] = v.z;
+    a[3] = v.w;
+}
+
+// The update of one point: out = 2u - upd + c * L u, upd = D * prev.
+__device__ __forceinline__ float update_fast(float u, float upd, float xm, float xp, float ym, float yp, float zm,
+                                             float zp, float c, float ax, float ay, float az) {
+    const float lap = fmaf(-2.0f, u, xp + xm) * ax + fmaf(-2.0f, u, yp + ym) * ay + fmaf(-2.0f, u, zp + zm) * az;
+    return fmaf(c, lap, fmaf(2.0f, u, -upd));
+}
+
+// The reference's guarded update (wave_equation.cpp:342-399), taken only when
+// the fast result is non-finite or beyond the amplitude limit. A non-finite
+// input always makes the fast result non-finite (c, 1/d^2 > 0), so the fast
+// path is exact whenever it is taken.
+__device__ __noinline__ float update_guarded(float u, float upd, float xm, float xp, float ym, float yp, float zm,
+                                             float zp, float c, float ax, float ay, float az, float amp,
+                                             int* fired) {
     if (!isfinite(u) || !isfinite(upd)) {
-        fired = true;
+        *fired = 1;
         return 0.0f;
     }
     if (!isfinite(xm) || !isfinite(xp) || !isfinite(ym) || !isfinite(yp) || !isfinite(zm) || !isfinite(zp)) {
-        fired = true;
+        *fired = 1;
         return u;
     }
-    const float lap = ((xp - 2.0f * u) + xm) * ax + ((yp - 2.0f * u) + ym) * ay + ((zp - 2.0f * u) + zm) * az;
-    float nv = (2.0f * u - upd) + c * lap;
+    float nv = update_fast(u, upd, xm, xp, ym, yp, zm, zp, c, ax, ay, az);
     if (!isfinite(nv)) {
         nv = u;
-        fired = true;
+        *fired = 1;
     }
     return fminf(fmaxf(nv, -amp), amp);
 }
 
-template <int SNAP_OUT, int SNAP_IN, bool IMAGE>
-__global__ void __launch_bounds__(NTHREADS, MIN_BLOCKS)
+// Per-row bookkeeping of one thread (4 consecutive z of one y row).
+struct RowCtx {
+    int iy;
+    bool active;
+    int dy;      // sponge distance along y
+    int iry;     // receiver y index, -1 if the row holds no receiver
+    bool inj;    // the fused injection point lies in this row
+};
+
+// Update of the 4 points of one row of plane x and its fused epilogue.
+// fin: imaging -> dequantised forward snapshot; gradient -> L(snapshot) (dequantised).
+template <int SNAP_OUT, int SNAP_IN, int EPI>
+__device__ __forceinline__ void process_row(const StepArgs& a, const RowCtx& R, int x, int zvalid, const int dz[4],
+                                            bool zfar, int dxx, const float* dtab, const float um[4],
+                                            const float u0[4], const float up[4], const float ym[4],
+                                            const float yp[4], float zm0, float zp3, const float pv[4],
+                                            const float cv[4], int rk, int irx, int inj_k, float snap_inv,
+                                            float& amax, int* fired, long long obase, long long cbase,
+                                            const float fin[4], const float4& acc0, const float4& acc1,
+                                            bool vec_acc) {
+    float D[4];
+    const int dxy = min(R.dy, dxx);
+    if (zfar && dxy >= a.sw) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) D[k] = 1.0f;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int d = min(dxy, dz[k]);
+            D[k] = (d >= 0 && d < a.sw) ? dtab[d] : 1.0f;
+        }
+    }
+    float res[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float zm = k == 0 ? zm0 : u0[k - 1];
+        const float zp = k == 3 ? zp3 : u0[k + 1];
+        const float upd = D[k] * pv[k];
+        float nv = update_fast(u0[k], upd, um[k], up[k], ym[k], yp[k], zm, zp, cv[k], a.ax, a.ay, a.az);
+        if (!(fabsf(nv) <= a.amp))
+            nv = update_guarded(u0[k], upd, um[k], up[k], ym[k], yp[k], zm, zp, cv[k], a.ax, a.ay, a.az, a.amp,
+                                fired);
+        res[k] = nv;
+    }
+    if (rk >= 0 && irx >= 0 && R.iry >= 0) {
+        const int q = irx * a.rny + R.iry;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k == rk) {
+                if (a.seis_row) a.seis_row[q] = res[k];
+                if (a.force_row) res[k] = fmaf(cv[k], a.force_row[q], res[k]);
+            }
+    }
+    if (R.inj && x == a.inj_x) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k == inj_k) res[k] += a.inj_val;
+    }
+    if (!R.active) return;
+    if (zvalid == 4) {
+        *reinterpret_cast<float4*>(a.out + obase) = make_float4(res[0], res[1], res[2], res[3]);
+    } else {
+        for (int k = 0; k < zvalid; ++k) a.out[obase + k] = res[k];
+    }
+    if constexpr (SNAP_OUT != SNAP_NONE) {
+        float q[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) q[k] = u0[k] * snap_inv;
+        if (zvalid == 4 && (a.nz & 3) == 0) {
+            snap_store4<SNAP_OUT>(a.snap_out, cbase, q);
+        } else {
+            for (int k = 0; k < zvalid; ++k) snap_store<SNAP_OUT>(a.snap_out, cbase + k, q[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < zvalid) amax = fmaxf(amax, fabsf(res[k]));
+    }
+    if constexpr (EPI == EPI_IMAGE) {
+        if (vec_acc) {
+            float im[4], il[4];
+            f4_to(acc0, im);
+            f4_to(acc1, il);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                float f = fin[k];
+                float ad = u0[k] / cv[k];
+                if (!isfinite(f)) f = 0.0f;
+                if (!isfinite(ad)) ad = 0.0f;
+                im[k] = fmaf(f, ad, im[k]);
+                il[k] = fmaf(f, f, il[k]);
+            }
+            *reinterpret_cast<float4*>(a.image + cbase) = make_float4(im[0], im[1], im[2], im[3]);
+            *reinterpret_cast<float4*>(a.illum + cbase) = make_float4(il[0], il[1], il[2], il[3]);
+        } else {
+            const float sc = __uint_as_float(*a.amax_in) / SNAP_QMAX;
+            for (int k = 0; k < zvalid; ++k) {
+                float f = snap_load<SNAP_IN>(a.snap_in, cbase + k) * sc;
+                float ad = u0[k] / cv[k];
+                if (!isfinite(f)) f = 0.0f;
+                if (!isfinite(ad)) ad = 0.0f;
+                a.image[cbase + k] += f * ad;
+                a.illum[cbase + k] += f * f;
+            }
+        }
+    }
+    if constexpr (EPI == EPI_GRAD) {
+        if (vec_acc) {
+            float g[4];
+            f4_to(acc0, g);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) g[k] = fmaf(u0[k] / cv[k], fin[k], g[k]);
+            *reinterpret_cast<float4*>(a.grad + cbase) = make_float4(g[0], g[1], g[2], g[3]);
+        } else {
+            for (int k = 0; k < zvalid; ++k) a.grad[cbase + k] += (u0[k] / cv[k]) * fin[k];
+        }
+    }
+}
+
+template <int SNAP_OUT, int SNAP_IN, int EPI>
+__global__ void __launch_bounds__(NTHREADS, (Geo<EPI, SNAP_IN>::MINB))
     fd_step_kernel(const __grid_constant__ CUtensorMap map_cur, const __grid_constant__ CUtensorMap map_prev,
-                   const __grid_constant__ CUtensorMap map_c, const StepArgs a) {
+                   const __grid_constant__ CUtensorMap map_c, const __grid_constant__ CUtensorMap map_snap,
+                   const StepArgs a) {
+    using G = Geo<EPI, SNAP_IN>;
+    constexpr int STAGES = G::STAGES;
+    constexpr int RPT = G::RPT;
+    constexpr int TYV = G::TYV;
     extern __shared__ __align__(128) unsigned char smem[];
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
-    float* red = reinterpret_cast<float*>(smem + STAGES * STAGE_BYTES + 64);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + STAGES * G::STAGE_BYTES);
+    float* red = reinterpret_cast<float*>(smem + STAGES * G::STAGE_BYTES + 64);
+    float* dtab_s = reinterpret_cast<float*>(smem + STAGES * G::STAGE_BYTES + 128);
 
     const int tid = threadIdx.x;
     const int tz4 = tid % TZ4;
-    const int ty = tid / TZ4;
+    const int yp2 = tid / TZ4;  // thread row within the tile (owns rows RPT*yp2 ..)
     const int z0 = blockIdx.x * TZ;
-    const int y0 = blockIdx.y * TY;
+    const int y0 = blockIdx.y * TYV;
     const int xa = blockIdx.z * a.x_chunk;
     const int xb = min(xa + a.x_chunk, a.nx);
     if (xa >= xb) return;  // uniform over the CTA
     const int nplanes = xb - xa + 2;
 
-    const int iy = y0 + ty;
     const int iz0 = z0 + 4 * tz4;
     const int zvalid = min(4, a.nz - iz0);
-    const bool active = (iy < a.ny) && (zvalid > 0);
-
-    // sponge distances: y part now, z part per element, x part per plane
-    const int dy = min(iy, a.ny - 1 - iy);
-    int dz4[4];
+    int dz[4];
+    bool zfar = true;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) dz4[k] = min(iz0 + k, a.nz - 1 - (iz0 + k));
-
-    // receiver bookkeeping for this thread's (y, z-group)
-    int rk = -1, iry = -1;
-    if ((a.seis_row || a.force_row) && active) {
-        const int kk = a.rz - iz0;
-        const int yy = iy - a.ry0;
-        if (kk >= 0 && kk < zvalid && yy >= 0 && yy % a.rsy == 0 && yy / a.rsy < a.rny) {
-            rk = kk;
-            iry = yy / a.rsy;
-        }
+    for (int k = 0; k < 4; ++k) {
+        dz[k] = min(iz0 + k, a.nz - 1 - (iz0 + k));
+        zfar = zfar && dz[k] >= a.sw;
     }
+    RowCtx RA, RB;
+    RA.iy = y0 + RPT * yp2;
+    RB.iy = RA.iy + 1;
+    RA.active = RA.iy < a.ny && zvalid > 0;
+    RB.active = RPT == 2 && RB.iy < a.ny && zvalid > 0;
+    RA.dy = min(RA.iy, a.ny - 1 - RA.iy);
+    RB.dy = min(RB.iy, a.ny - 1 - RB.iy);
+    int rk = -1;
+    RA.iry = RB.iry = -1;
+    if (a.seis_row || a.force_row) {
+        const int kk = a.rz - iz0;
+        if (kk >= 0 && kk < zvalid) rk = kk;
+        const int ya = RA.iy - a.ry0, yb = RB.iy - a.ry0;
+        if (RA.active && ya >= 0 && ya % a.rsy == 0 && ya / a.rsy < a.rny) RA.iry = ya / a.rsy;
+        if (RPT == 2 && RB.active && yb >= 0 && yb % a.rsy == 0 && yb / a.rsy < a.rny) RB.iry = yb / a.rsy;
+    }
+    const int inj_k = (a.inj_x >= 0) ? a.inj_z - iz0 : -1;
+    RA.inj = a.inj_x >= 0 && a.inj_y == RA.iy && inj_k >= 0 && inj_k < zvalid;
+    RB.inj = RPT == 2 && a.inj_x >= 0 && a.inj_y == RB.iy && inj_k >= 0 && inj_k < zvalid;
 
     float snap_inv = 0.0f;
     if constexpr (SNAP_OUT != SNAP_NONE) {
         const float m = __uint_as_float(*a.amax_cur);
         snap_inv = m > 0.0f ? SNAP_QMAX / m : 0.0f;
     }
-    float snap_in_scale = 1.0f;
-    if constexpr (IMAGE) {
-        const float m = __uint_as_float(*a.amax_in);
-        snap_in_scale = m / SNAP_QMAX;
-    }
+    float snap_scale = 1.0f;
+    const bool vec_acc = EPI != EPI_NONE && (a.nz & 3) == 0 && zvalid == 4;
+    if constexpr (EPI != EPI_NONE) snap_scale = __uint_as_float(*a.amax_in) / SNAP_QMAX;
 
-    auto cur_tile = [&](int s) { return reinterpret_cast<float*>(smem + s * STAGE_BYTES); };
-    auto prev_tile = [&](int s) { return reinterpret_cast<float*>(smem + s * STAGE_BYTES + CUR_BYTES_PAD); };
+    const bool tab_smem = a.sw <= DTAB_MAX;
+    if (tab_smem)
+        for (int i = tid; i < a.sw; i += NTHREADS) dtab_s[i] = a.dtab[i];
+    const float* dtab = tab_smem ? dtab_s : a.dtab;
+
+    auto cur_tile = [&](int s) { return reinterpret_cast<float*>(smem + s * G::STAGE_BYTES); };
+    auto prev_tile = [&](int s) { return reinterpret_cast<float*>(smem + s * G::STAGE_BYTES + G::CUR_BYTES_PAD); };
     auto c_tile = [&](int s) {
-        return reinterpret_cast<float*>(smem + s * STAGE_BYTES + CUR_BYTES_PAD + CTR_BYTES);
+        return reinterpret_cast<float*>(smem + s * G::STAGE_BYTES + G::CUR_BYTES_PAD + G::CTR_BYTES);
+    };
+    auto snap_tile = [&](int s) {
+        return reinterpret_cast<const unsigned char*>(smem + s * G::STAGE_BYTES + G::CUR_BYTES_PAD +
+                                                      2 * G::CTR_BYTES);
     };
 
     if (tid == 0) {
@@ -216,10 +404,13 @@ __global__ void __launch_bounds__(NTHREADS, MIN_BLOCKS)
     auto issue = [&](int i) {
         const int s = i % STAGES;
         const int xd = xa + i;
-        mbar_arrive_expect_tx(&bar[s], STAGE_TX);
+        mbar_arrive_expect_tx(&bar[s], G::STAGE_TX);
         tma_load_3d(cur_tile(s), &map_cur, &bar[s], z0, y0, xd);
         tma_load_3d(prev_tile(s), &map_prev, &bar[s], z0 + Layout::ZOFF, y0 + 1, xd);
         tma_load_3d(c_tile(s), &map_c, &bar[s], z0 + Layout::ZOFF, y0 + 1, xd);
+        if constexpr (EPI == EPI_GRAD)
+            tma_load_4d(const_cast<unsigned char*>(snap_tile(s)), &map_snap, &bar[s], z0 - G::SOFF, y0 - 1, xd - 1,
+                        a.snap_t);
     };
     int issued = 0;
     if (tid == 0) {
@@ -227,100 +418,158 @@ __global__ void __launch_bounds__(NTHREADS, MIN_BLOCKS)
         for (int i = 0; i < issued; ++i) issue(i);
     }
 
-    const int crow = (ty + 1) * CUR_W + 4 * tz4 + 4;  // centre float4 of this thread in a cur tile
-    const int ctr = ty * TZ + 4 * tz4;                 // its float4 in prev / c tiles
-    float4 um = make_float4(0.f, 0.f, 0.f, 0.f), u0 = um, up = um;
+    const int rowA = (RPT * yp2 + 1) * CUR_W + 4 * tz4 + 4;  // centre of row A in a cur tile
+    const int rowB = rowA + CUR_W;
+    const int ctrA = (RPT * yp2) * TZ + 4 * tz4;              // row A in prev / c tiles
+    const int ctrB = ctrA + TZ;
+    const int srowA = (RPT * yp2 + 1) * G::SW + 4 * tz4 + G::SOFF;  // row A in a snapshot tile
+    float umA[4] = {0, 0, 0, 0}, u0A[4] = {0, 0, 0, 0}, umB[4] = {0, 0, 0, 0}, u0B[4] = {0, 0, 0, 0};
+    float smA[4] = {0, 0, 0, 0};  // snapshot centres of plane x-1 (gradient)
     float amax_local = 0.0f;
-    bool fired = false;
+    int fired = 0;
     int timed_out = 0;
-    int i = 0;
 
+    // epilogue operands of the next plane, loaded one plane ahead
+    using SR = typename Snap4<(SNAP_IN == SNAP_NONE ? SNAP_FP32 : SNAP_IN)>::T;
+    SR snA{}, snB{};
+    float4 a0A{}, a0B{}, a1A{}, a1B{};
+    // Imaging loads its operands at use (more resident warps hide them better
+    // than holding them in registers a plane ahead); the gradient prefetches
+    // its single accumulator.
+    constexpr bool kPrefetch = EPI == EPI_GRAD;
+    auto prefetch = [&](int x) {
+        if constexpr (EPI != EPI_NONE) {
+            if (!vec_acc || x >= xb) return;
+            const long long ca = ((long long)x * a.ny + RA.iy) * a.nz + iz0;
+            const long long cb = ca + a.nz;
+            if constexpr (EPI == EPI_IMAGE) {
+                if (RA.active) {
+                    snA = snap_raw4<SNAP_IN>(a.snap_in, ca);
+                    a0A = *reinterpret_cast<const float4*>(a.image + ca);
+                    a1A = *reinterpret_cast<const float4*>(a.illum + ca);
+                }
+                if (RPT == 2 && RB.active) {
+                    snB = snap_raw4<SNAP_IN>(a.snap_in, cb);
+                    a0B = *reinterpret_cast<const float4*>(a.image + cb);
+                    a1B = *reinterpret_cast<const float4*>(a.illum + cb);
+                }
+            } else {
+                if (RA.active) a0A = *reinterpret_cast<const float4*>(a.grad + ca);
+                if (RPT == 2 && RB.active) a0B = *reinterpret_cast<const float4*>(a.grad + cb);
+            }
+        }
+    };
+    if constexpr (kPrefetch) prefetch(xa);
+
+    int i = 0;
     for (; i < nplanes; ++i) {
         const int s = i % STAGES;
         if (!mbar_wait_bounded(&bar[s], (i / STAGES) & 1, a.timeout_ns)) timed_out = 1;
-        up = *reinterpret_cast<const float4*>(cur_tile(s) + crow);
+        float upA[4], upB[4] = {0, 0, 0, 0};
+        f4_to(*reinterpret_cast<const float4*>(cur_tile(s) + rowA), upA);
+        if constexpr (RPT == 2) f4_to(*reinterpret_cast<const float4*>(cur_tile(s) + rowB), upB);
         if (i >= 2) {
             const int sp = (i - 1) % STAGES;
             const int x = xa + i - 2;
             const float* T = cur_tile(sp);
-            const float4 ym = *reinterpret_cast<const float4*>(T + crow - CUR_W);
-            const float4 yp = *reinterpret_cast<const float4*>(T + crow + CUR_W);
-            float zm0 = __shfl_up_sync(FULL, u0.w, 1, TZ4);
-            float zp3 = __shfl_down_sync(FULL, u0.x, 1, TZ4);
-            if (tz4 == 0) zm0 = T[crow - 1];
-            if (tz4 == TZ4 - 1) zp3 = T[crow + 4];
-            const float4 pv = *reinterpret_cast<const float4*>(prev_tile(sp) + ctr);
-            const float4 cv = *reinterpret_cast<const float4*>(c_tile(sp) + ctr);
-            const int dxy = min(dy, min(x, a.nx - 1 - x));
-            const long long obase = (long long)(x + 1) * a.plane + (long long)(iy + 1) * a.NZP + iz0 + Layout::ZOFF;
-            const long long cbase = ((long long)x * a.ny + iy) * a.nz + iz0;  // compact interior index
+            // y neighbours: row A's y- from the tile; with two rows, row A's y+ is
+            // row B's centre and row B's y- is row A's centre
+            float ymA[4], ypA[4], ypB[4] = {0, 0, 0, 0}, pvA[4], pvB[4] = {0, 0, 0, 0}, cvA[4],
+                cvB[4] = {0, 0, 0, 0};
+            f4_to(*reinterpret_cast<const float4*>(T + rowA - CUR_W), ymA);
+            if constexpr (RPT == 2) {
+                f4_to(*reinterpret_cast<const float4*>(T + rowB + CUR_W), ypB);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) ypA[k] = u0B[k];
+            } else {
+                f4_to(*reinterpret_cast<const float4*>(T + rowA + CUR_W), ypA);
+            }
+            f4_to(*reinterpret_cast<const float4*>(prev_tile(sp) + ctrA), pvA);
+            f4_to(*reinterpret_cast<const float4*>(c_tile(sp) + ctrA), cvA);
+            if constexpr (RPT == 2) {
+                f4_to(*reinterpret_cast<const float4*>(prev_tile(sp) + ctrB), pvB);
+                f4_to(*reinterpret_cast<const float4*>(c_tile(sp) + ctrB), cvB);
+            }
+            float zmA = __shfl_up_sync(FULL, u0A[3], 1, TZ4);
+            float zpA = __shfl_down_sync(FULL, u0A[0], 1, TZ4);
+            float zmB = 0.0f, zpB = 0.0f;
+            if constexpr (RPT == 2) {
+                zmB = __shfl_up_sync(FULL, u0B[3], 1, TZ4);
+                zpB = __shfl_down_sync(FULL, u0B[0], 1, TZ4);
+            }
+            if (tz4 == 0) {
+                zmA = T[rowA - 1];
+                if constexpr (RPT == 2) zmB = T[rowB - 1];
+            }
+            if (tz4 == TZ4 - 1) {
+                zpA = T[rowA + 4];
+                if constexpr (RPT == 2) zpB = T[rowB + 4];
+            }
+            const int dxx = min(x, a.nx - 1 - x);
             int irx = -1;
             if (rk >= 0) {
                 const int xx = x - a.rx0;
                 if (xx >= 0 && xx % a.rsx == 0 && xx / a.rsx < a.rnx) irx = xx / a.rsx;
             }
-            float4 res;
+            const long long obA = (long long)(x + 1) * a.plane + (long long)(RA.iy + 1) * a.NZP + iz0 + Layout::ZOFF;
+            const long long cbA = ((long long)x * a.ny + RA.iy) * a.nz + iz0;
+            float finA[4] = {0, 0, 0, 0}, finB[4] = {0, 0, 0, 0};
+            if constexpr (!kPrefetch) prefetch(x);  // operands of this plane, at use
+            if constexpr (EPI == EPI_IMAGE) {
+                snap_unpack4<SNAP_IN>(snA, finA);
+                if constexpr (RPT == 2) snap_unpack4<SNAP_IN>(snB, finB);
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float u = f4get(u0, k);
-                const float zm = k == 0 ? zm0 : f4get(u0, k - 1);
-                const float zp = k == 3 ? zp3 : f4get(u0, k + 1);
-                const int d = min(dxy, dz4[k]);
-                const float D = (d >= 0 && d < a.sw) ? __ldg(a.dtab + d) : 1.0f;
-                const float c = f4get(cv, k);
-                float nv = point_update(u, D * f4get(pv, k), f4get(um, k), f4get(up, k), f4get(ym, k), f4get(yp, k),
-                                        zm, zp, c, a.ax, a.ay, a.az, a.amp, fired);
-                if (k == rk && irx >= 0) {
-                    const int q = irx * a.rny + iry;
-                    if (a.seis_row) a.seis_row[q] = nv;
-                    if (a.force_row) nv += c * a.force_row[q];
+                for (int k = 0; k < 4; ++k) {
+                    finA[k] *= snap_scale;
+                    finB[k] *= snap_scale;
                 }
-                if (obase + k == a.inj_idx) nv += a.inj_val;
-                f4set(res, k, nv);
             }
-            if (active) {
-                if (zvalid == 4) {
-                    *reinterpret_cast<float4*>(a.out + obase) = res;
-                } else {
-                    for (int k = 0; k < zvalid; ++k) a.out[obase + k] = f4get(res, k);
+            if constexpr (EPI == EPI_GRAD) {
+                // 7-point Laplacian of the forward snapshot V_t (zero halo from the TMA fill);
+                // the gradient variant runs one row per thread
+                const unsigned char* S = snap_tile(sp);
+                const unsigned char* Sn = snap_tile(s);
+                float s0A[4], spA[4], symA[4], sypA[4];
+                snap_smem4<SNAP_IN>(S, srowA, s0A);
+                snap_smem4<SNAP_IN>(Sn, srowA, spA);
+                snap_smem4<SNAP_IN>(S, srowA - G::SW, symA);
+                snap_smem4<SNAP_IN>(S, srowA + G::SW, sypA);
+                float szmA = __shfl_up_sync(FULL, s0A[3], 1, TZ4);
+                float szpA = __shfl_down_sync(FULL, s0A[0], 1, TZ4);
+                if (tz4 == 0) szmA = snap_smem1<SNAP_IN>(S, srowA - 1);
+                if (tz4 == TZ4 - 1) szpA = snap_smem1<SNAP_IN>(S, srowA + 4);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float zm_ = k == 0 ? szmA : s0A[k - 1], zp_ = k == 3 ? szpA : s0A[k + 1];
+                    finA[k] = snap_scale * (fmaf(-2.0f, s0A[k], spA[k] + smA[k]) * a.ax +
+                                            fmaf(-2.0f, s0A[k], sypA[k] + symA[k]) * a.ay +
+                                            fmaf(-2.0f, s0A[k], zp_ + zm_) * a.az);
+                    smA[k] = s0A[k];
                 }
-                if constexpr (SNAP_OUT != SNAP_NONE) {
-                    float4 q = make_float4(u0.x * snap_inv, u0.y * snap_inv, u0.z * snap_inv, u0.w * snap_inv);
-                    if (zvalid == 4 && (a.nz & 3) == 0) {
-                        snap_store4<SNAP_OUT>(a.snap_out, cbase, q);
-                    } else {
-                        for (int k = 0; k < zvalid; ++k) snap_store<SNAP_OUT>(a.snap_out, cbase + k, f4get(q, k));
-                    }
-                    for (int k = 0; k < zvalid; ++k) amax_local = fmaxf(amax_local, fabsf(f4get(res, k)));
-                }
-                if constexpr (IMAGE) {
-                    const bool vec = zvalid == 4 && (a.nz & 3) == 0;
-                    float4 fv;
-                    if (vec) fv = snap_load4<SNAP_IN>(a.snap_in, cbase);
-                    float4 im = vec ? *reinterpret_cast<const float4*>(a.image + cbase) : make_float4(0, 0, 0, 0);
-                    float4 il = vec ? *reinterpret_cast<const float4*>(a.illum + cbase) : make_float4(0, 0, 0, 0);
-                    for (int k = 0; k < zvalid; ++k) {
-                        float f = (vec ? f4get(fv, k) : snap_load<SNAP_IN>(a.snap_in, cbase + k)) * snap_in_scale;
-                        float ad = f4get(u0, k) / f4get(cv, k);
-                        if (!isfinite(f)) f = 0.0f;
-                        if (!isfinite(ad)) ad = 0.0f;
-                        if (vec) {
-                            f4set(im, k, fmaf(f, ad, f4get(im, k)));
-                            f4set(il, k, fmaf(f, f, f4get(il, k)));
-                        } else {
-                            a.image[cbase + k] += f * ad;
-                            a.illum[cbase + k] += f * f;
-                        }
-                    }
-                    if (vec) {
-                        *reinterpret_cast<float4*>(a.image + cbase) = im;
-                        *reinterpret_cast<float4*>(a.illum + cbase) = il;
-                    }
-                }
+            }
+            const float4 a0A0 = a0A, a1A0 = a1A, a0B0 = a0B, a1B0 = a1B;
+            if constexpr (kPrefetch) prefetch(x + 1);
+            process_row<SNAP_OUT, SNAP_IN, EPI>(a, RA, x, zvalid, dz, zfar, dxx, dtab, umA, u0A, upA, ymA, ypA, zmA,
+                                                zpA, pvA, cvA, rk, irx, inj_k, snap_inv, amax_local, &fired, obA,
+                                                cbA, finA, a0A0, a1A0, vec_acc);
+            if constexpr (RPT == 2)
+                process_row<SNAP_OUT, SNAP_IN, EPI>(a, RB, x, zvalid, dz, zfar, dxx, dtab, umB, u0B, upB, u0A, ypB,
+                                                    zmB, zpB, pvB, cvB, rk, irx, inj_k, snap_inv, amax_local, &fired,
+                                                    obA + a.NZP, cbA + a.nz, finB, a0B0, a1B0, vec_acc);
+        } else if constexpr (EPI == EPI_GRAD) {
+            if (i == 1) {
+                // snapshot centres of plane xa-1 (zero outside the domain)
+                const unsigned char* S = snap_tile((i - 1) % STAGES);
+                snap_smem4<SNAP_IN>(S, srowA, smA);
             }
         }
-        um = u0;
-        u0 = up;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            umA[k] = u0A[k];
+            u0A[k] = upA[k];
+            umB[k] = u0B[k];
+            u0B[k] = upB[k];
+        }
         // every thread is done with the slot of plane i-1: refill it
         if (__syncthreads_or(timed_out)) break;
         if (tid == 0 && i >= 1 && issued < nplanes) issue(issued++);
@@ -348,20 +597,27 @@ __global__ void __launch_bounds__(NTHREADS, MIN_BLOCKS)
     }
 }
 
-template <int SO, int SI, bool IM>
-int launch_variant(dim3 grid, const CUtensorMap& mcur, const CUtensorMap& mprev, const CUtensorMap& mc,
-                   const StepArgs& a, cudaStream_t st) {
+template <int SO, int SI, int EPI>
+int launch_variant(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
+                   const CUtensorMap& msnap, StepArgs a, cudaStream_t st) {
+    using G = Geo<EPI, SI>;
+    constexpr int SMEM = G::SMEM;
+    constexpr int ti = G::RPT == 2 ? 1 : 0;  // which tile height the maps were built for
     static bool configured = false;
     static std::mutex mu;
     {
         std::lock_guard<std::mutex> lk(mu);
         if (!configured) {
-            ST_CUDA(cudaFuncSetAttribute(fd_step_kernel<SO, SI, IM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         SMEM_BYTES));
+            ST_CUDA(cudaFuncSetAttribute(fd_step_kernel<SO, SI, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         SMEM));
             configured = true;
         }
     }
-    fd_step_kernel<SO, SI, IM><<<grid, NTHREADS, SMEM_BYTES, st>>>(mcur, mprev, mc, a);
+    const int chunks = fd_step_grid_chunks(L, G::TYV, G::MINB);
+    a.x_chunk = (int)((L.nx + chunks - 1) / chunks);
+    const int nch = (int)((L.nx + a.x_chunk - 1) / a.x_chunk);
+    dim3 grid((unsigned)((L.nz + TZ - 1) / TZ), (unsigned)((L.ny + G::TYV - 1) / G::TYV), (unsigned)nch);
+    fd_step_kernel<SO, SI, EPI><<<grid, NTHREADS, SMEM, st>>>(mcur.cur[ti], mprev.ctr[ti], mc.ctr[ti], msnap, a);
     ::stg::count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
@@ -539,50 +795,83 @@ int grid_for(long long n, int threads = 256) {
 
 // ---------------------------------------------------------------- host side
 
-int build_stencil_map_cur(CUtensorMap* m, const float* base, const Layout& L) {
-    return make_field_map(m, base, L, TZ + 8, TY + 2);
-}
-int build_stencil_map_ctr(CUtensorMap* m, const float* base, const Layout& L) {
-    return make_field_map(m, base, L, TZ, TY);
-}
-
-int fd_step_grid_chunks(const Layout& L) {
-    const long long gx = (L.nz + TZ - 1) / TZ, gy = (L.ny + TY - 1) / TY;
-    // one resident wave: every CTA marches its x-chunk from start to end
-    const long long target = (long long)num_sms() * MIN_BLOCKS;
-    long long chunks = target / (gx * gy);
-    chunks = std::max<long long>(1, std::min<long long>(chunks, L.nx));
-    return (int)chunks;
+int build_field_maps(FieldMaps* m, const float* base, const Layout& L) {
+    for (int t = 0; t < 2; ++t) {
+        const int rows = 16 << t;
+        ST_TRY(make_field_map(&m->cur[t], base, L, TZ + 8, rows + 2));
+        ST_TRY(make_field_map(&m->ctr[t], base, L, TZ, rows));
+    }
+    return ST_OK;
 }
 
-int launch_fd_step(const Layout& L, const CUtensorMap& mcur, const CUtensorMap& mprev, const CUtensorMap& mc,
-                   StepArgs a, int snap_out, int snap_in, bool image, cudaStream_t st) {
-    const int chunks = fd_step_grid_chunks(L);
-    a.x_chunk = (int)((L.nx + chunks - 1) / chunks);
-    const int nch = (int)((L.nx + a.x_chunk - 1) / a.x_chunk);
-    dim3 grid((unsigned)((L.nz + TZ - 1) / TZ), (unsigned)((L.ny + TY - 1) / TY), (unsigned)nch);
+int fd_step_grid_chunks(const Layout& L, int tyv, int minb) {
+    const long long gx = (L.nz + TZ - 1) / TZ, gy = (L.ny + tyv - 1) / tyv;
+    const long long tiles = gx * gy;
+    // tuning override: SEISMIC_GB300_XCHUNKS=<chunks> (1..nx)
+    if (const char* env = std::getenv("SEISMIC_GB300_XCHUNKS")) {
+        const long long v = std::atoll(env);
+        if (v >= 1) return (int)std::min<long long>(v, L.nx);
+    }
+    // Split the x range into chunks so that the CTA count fills whole waves of
+    // resident CTAs (SMs x resident CTAs per SM); each chunk re-reads two halo
+    // planes, a cost weighed in against shorter chunks.
+    const double slots = (double)num_sms() * minb;
+    long long best = 1;
+    double best_eff = -1.0;
+    const long long max_chunks = std::max<long long>(1, std::min<long long>(L.nx / 4, 256));
+    for (long long ch = 1; ch <= max_chunks; ++ch) {
+        const double waves = (double)(tiles * ch) / slots;
+        const double fill = waves / std::ceil(waves);
+        const double len = std::ceil((double)L.nx / (double)ch);
+        const double eff = fill / (1.0 + 2.0 / len);
+        if (eff > best_eff + 1e-9) {
+            best_eff = eff;
+            best = ch;
+        }
+    }
+    return (int)best;
+}
+
+int launch_fd_step(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
+                   StepArgs a, int snap_out, int snap_in, int epi, const CUtensorMap* msnap, cudaStream_t st) {
     a.nx = (int)L.nx;
     a.ny = (int)L.ny;
     a.nz = (int)L.nz;
     a.NZP = (int)L.NZP;
     a.plane = L.plane;
     if (a.timeout_ns == 0) a.timeout_ns = 2000000000ull;
-    if (image) {
+    const CUtensorMap& ms = msnap ? *msnap : mc.ctr[0];  // unused unless epi == gradient
+    if (epi == EPI_IMAGE) {
         ST_CHECK(snap_out == SNAP_NONE, ST_ERR_ARG, "imaging step cannot also store snapshots");
         switch (snap_in) {
-            case SNAP_BF16: return launch_variant<SNAP_NONE, SNAP_BF16, true>(grid, mcur, mprev, mc, a, st);
-            case SNAP_FP16: return launch_variant<SNAP_NONE, SNAP_FP16, true>(grid, mcur, mprev, mc, a, st);
-            case SNAP_FP32: return launch_variant<SNAP_NONE, SNAP_FP32, true>(grid, mcur, mprev, mc, a, st);
+            case SNAP_BF16: return launch_variant<SNAP_NONE, SNAP_BF16, EPI_IMAGE>(L, mcur, mprev, mc, ms, a, st);
+            case SNAP_FP16: return launch_variant<SNAP_NONE, SNAP_FP16, EPI_IMAGE>(L, mcur, mprev, mc, ms, a, st);
+            case SNAP_FP32: return launch_variant<SNAP_NONE, SNAP_FP32, EPI_IMAGE>(L, mcur, mprev, mc, ms, a, st);
             default: ST_CHECK(false, ST_ERR_ARG, "imaging step needs a snapshot kind");
         }
     }
+    if (epi == EPI_GRAD) {
+        ST_CHECK(snap_out == SNAP_NONE && msnap, ST_ERR_ARG, "gradient step needs a snapshot map and no store");
+        switch (snap_in) {
+            case SNAP_BF16: return launch_variant<SNAP_NONE, SNAP_BF16, EPI_GRAD>(L, mcur, mprev, mc, ms, a, st);
+            case SNAP_FP16: return launch_variant<SNAP_NONE, SNAP_FP16, EPI_GRAD>(L, mcur, mprev, mc, ms, a, st);
+            case SNAP_FP32: return launch_variant<SNAP_NONE, SNAP_FP32, EPI_GRAD>(L, mcur, mprev, mc, ms, a, st);
+            default: ST_CHECK(false, ST_ERR_ARG, "gradient step needs a snapshot kind");
+        }
+    }
     switch (snap_out) {
-        case SNAP_NONE: return launch_variant<SNAP_NONE, SNAP_NONE, false>(grid, mcur, mprev, mc, a, st);
-        case SNAP_BF16: return launch_variant<SNAP_BF16, SNAP_NONE, false>(grid, mcur, mprev, mc, a, st);
-        case SNAP_FP16: return launch_variant<SNAP_FP16, SNAP_NONE, false>(grid, mcur, mprev, mc, a, st);
-        case SNAP_FP32: return launch_variant<SNAP_FP32, SNAP_NONE, false>(grid, mcur, mprev, mc, a, st);
+        case SNAP_NONE: return launch_variant<SNAP_NONE, SNAP_NONE, EPI_NONE>(L, mcur, mprev, mc, ms, a, st);
+        case SNAP_BF16: return launch_variant<SNAP_BF16, SNAP_NONE, EPI_NONE>(L, mcur, mprev, mc, ms, a, st);
+        case SNAP_FP16: return launch_variant<SNAP_FP16, SNAP_NONE, EPI_NONE>(L, mcur, mprev, mc, ms, a, st);
+        case SNAP_FP32: return launch_variant<SNAP_FP32, SNAP_NONE, EPI_NONE>(L, mcur, mprev, mc, ms, a, st);
         default: ST_CHECK(false, ST_ERR_ARG, "bad snapshot kind %d", snap_out);
     }
+}
+
+int build_snap_map_grad(CUtensorMap* m, const void* base, int kind, const Layout& L, long long nt) {
+    // the gradient variant uses 16-row tiles (one row per thread)
+    const int bz = snap_bytes(kind) == 2 ? TZ + 16 : TZ + 8;
+    return make_snap_map(m, base, kind, L, nt, bz, 16 + 2);
 }
 
 int launch_add_point(float* f, long long idx, float val, unsigned* amax_slot, cudaStream_t st) {
@@ -691,6 +980,28 @@ int get_encode_tiled(EncodeTiledFn* out) {
         fn = reinterpret_cast<EncodeTiledFn>(p);
     }
     *out = fn;
+    return ST_OK;
+}
+
+int make_snap_map(CUtensorMap* map, const void* base, int kind, const Layout& L, long long nt, int bz, int by) {
+    EncodeTiledFn enc = nullptr;
+    ST_TRY(get_encode_tiled(&enc));
+    const int es = snap_bytes(kind);
+    ST_CHECK(es > 0, ST_ERR_ARG, "bad snapshot kind %d", kind);
+    ST_CHECK((reinterpret_cast<uintptr_t>(base) & 15) == 0, ST_ERR_ARG, "snapshot store not 16-byte aligned");
+    ST_CHECK((L.nz * es) % 16 == 0, ST_ERR_UNSUPPORTED,
+             "gradient snapshots need nz*%d bytes to be a multiple of 16 (nz=%lld)", es, (long long)L.nz);
+    const CUtensorMapDataType dt = kind == SNAP_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                   : kind == SNAP_FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                       : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    cuuint64_t dims[4] = {(cuuint64_t)L.nz, (cuuint64_t)L.ny, (cuuint64_t)L.nx, (cuuint64_t)std::max<long long>(nt, 1)};
+    cuuint64_t strides[3] = {(cuuint64_t)(L.nz * es), (cuuint64_t)(L.ny * L.nz * es),
+                             (cuuint64_t)(L.nx * L.ny * L.nz * es)};
+    cuuint32_t box[4] = {(cuuint32_t)bz, (cuuint32_t)by, 1, 1};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult r = enc(map, dt, 4, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    ST_CHECK(r == CUDA_SUCCESS, ST_ERR_CUDA, "cuTensorMapEncodeTiled (snapshots) failed (%d)", (int)r);
     return ST_OK;
 }
 

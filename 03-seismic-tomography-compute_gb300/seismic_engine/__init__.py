@@ -16,6 +16,7 @@ from .fields import check_field_health, clamp_field_safe, repair_field_nan  # no
 from .config import (  # noqa: F401
     InversionConfig, ModelConfig, TomographyConfig, load_config,
 )
+from .rtm import RTMConfig, RTMEngine, RTMImageCondition, SliceAxis, SliceSpec  # noqa: F401
 from . import workloads  # noqa: F401
 
 __version__ = "1.2.0+gb300"

@@ -109,6 +109,16 @@ SIGNATURES = {
     "st_shot_adjoint": [_vp, C.POINTER(ShotC), _vp, _vp],
     "st_rtm_shot": [_vp, C.POINTER(ShotC), _vp, C.c_int, _vp, _vp, _vp, _vp, _vp],
     "st_rtm_shot_host": [_vp, _d, C.c_int64, C.POINTER(ShotC), _f, C.c_int, _d, _d, _d],
+    "st_rtm_engine_create": [C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
+                             C.POINTER(_vp)],
+    "st_rtm_engine_destroy": [_vp],
+    "st_rtm_engine_apply_image_condition": [_vp, _d, _d, C.c_int64, C.c_int64, C.c_int64],
+    "st_rtm_engine_finalize_image": [_vp],
+    "st_rtm_engine_reset_image": [_vp],
+    "st_rtm_engine_result": [_vp, _d, _d, _d],
+    "st_solver_set_velocity_device": [_vp, _vp],
+    "st_shot_gradient": [_vp, C.POINTER(ShotC), _vp, C.c_int, _vp],
+    "st_fwi_gradient": [_vp, C.POINTER(ShotC), _vp, C.c_int, _vp, _d, _vp],
     # sparse
     "st_csr_create": [C.c_int64, C.c_int64, C.c_int64, C.c_int, C.POINTER(_vp)],
     "st_csr_destroy": [_vp],

@@ -1,0 +1,73 @@
+"""Full-waveform-inversion face: the velocity -> seismogram map as a
+torch.autograd.Function whose backward is the GPU library's exact discrete
+adjoint (st_shot_gradient), and the L2 misfit + gradient of a set of shots
+(st_fwi_gradient). Velocities are torch CUDA tensors (nx, ny, nz), z fastest.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _lib
+from ._lib import call
+from .wave import WaveEquationSolver, _shot_c
+
+
+def set_velocity_device(solver: WaveEquationSolver, vel: torch.Tensor):
+    v = vel.detach().to(device="cuda", dtype=torch.float32).contiguous()
+    call("st_solver_set_velocity_device", solver.handle, v.data_ptr())
+    torch.cuda.current_stream().synchronize()
+
+
+def shot_gradient(solver, src, wavelet, nt, rec, adj_src, grad_v, snap_kind=_lib.ST_SNAP_FP32):
+    """grad_v += d<F(v), adj_src>/dv for one shot (device tensors)."""
+    shot, _keep = _shot_c(src, wavelet, nt, rec)
+    return call("st_shot_gradient", solver.handle, C.byref(shot), adj_src.data_ptr(), int(snap_kind),
+                grad_v.data_ptr())
+
+
+def fwi_gradient(solver, src, wavelet, nt, rec, d_obs, grad_v=None, snap_kind=_lib.ST_SNAP_FP32, residual=None):
+    """L2 misfit 1/2 sum (F(v) - d_obs)^2 of one shot (FP64) and, when grad_v is
+    given, grad_v += its gradient."""
+    shot, _keep = _shot_c(src, wavelet, nt, rec)
+    m = C.c_double(0.0)
+    call("st_fwi_gradient", solver.handle, C.byref(shot), d_obs.data_ptr(), int(snap_kind),
+         grad_v.data_ptr() if grad_v is not None else None, C.byref(m),
+         residual.data_ptr() if residual is not None else None)
+    return m.value
+
+
+class SeismicModeling(torch.autograd.Function):
+    """d = F(v): seismograms [n_shots, nt, nrec] of every shot for velocity v.
+    backward: the exact adjoint of the discrete forward map (fused GPU
+    kernel), forward snapshots recomputed and stored with snap_kind."""
+
+    @staticmethod
+    def forward(ctx, vel, solver, shots, nt, snap_kind):
+        from .wave import shot_forward
+        set_velocity_device(solver, vel)
+        nrec = shots[0].rec.count
+        out = torch.zeros((len(shots), nt, nrec), device="cuda", dtype=torch.float32)
+        for i, sh in enumerate(shots):
+            shot_forward(solver, sh.src, sh.wavelet, nt, sh.rec, seis=out[i])
+        torch.cuda.synchronize()
+        ctx.save_for_backward(vel)
+        ctx.solver, ctx.shots, ctx.nt, ctx.snap_kind = solver, shots, nt, snap_kind
+        return out.to(vel.dtype)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        (vel,) = ctx.saved_tensors
+        solver = ctx.solver
+        set_velocity_device(solver, vel)
+        g = torch.zeros(vel.shape, device="cuda", dtype=torch.float32)
+        go = grad_out.to(dtype=torch.float32).contiguous()
+        for i, sh in enumerate(ctx.shots):
+            shot_gradient(solver, sh.src, sh.wavelet, ctx.nt, sh.rec, go[i].contiguous(), g, ctx.snap_kind)
+        torch.cuda.synchronize()
+        return g.to(vel.dtype), None, None, None, None
+
+
+def modeling(vel: torch.Tensor, solver: WaveEquationSolver, shots, nt: int, snap_kind=_lib.ST_SNAP_FP32):
+    return SeismicModeling.apply(vel, solver, shots, nt, snap_kind)

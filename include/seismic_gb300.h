@@ -212,6 +212,42 @@ int st_rtm_shot(st_solver* s, const st_shot* shot, const float* data, int snap_k
 int st_rtm_shot_host(st_solver* s, const double* vp, int64_t vp_count, const st_shot* shot, const float* data_host,
                      int snap_kind, double* image_host, double* illum_host, double* refl_host);
 
+/* -------------------------------------------------- seismic::RTMEngine face */
+/* The imaging condition on caller-provided FP64 halo-padded fields, FP64
+ * accumulators on the device. */
+typedef struct st_rtm_engine st_rtm_engine;
+/* Replaces RTMEngine::RTMEngine (rtm/rtm_engine.cpp:8-16). */
+int st_rtm_engine_create(int64_t nx, int64_t ny, int64_t nz, double dx, double dy, double dz, int halo_width,
+                         int device, st_rtm_engine** out);
+int st_rtm_engine_destroy(st_rtm_engine* e);
+/* Replaces apply_image_condition (rtm_engine.cpp:24-57): image += f*a,
+ * illumination += f*f over the interior, non-finite values taken as 0. */
+int st_rtm_engine_apply_image_condition(st_rtm_engine* e, const double* forward_wavefield,
+                                        const double* adjoint_wavefield, int64_t ny_padded, int64_t nz_padded,
+                                        int64_t step_idx);
+/* Replace finalize_image / reset_image / result() (rtm_engine.cpp:170-190, rtm_engine.h:52). */
+int st_rtm_engine_finalize_image(st_rtm_engine* e);
+int st_rtm_engine_reset_image(st_rtm_engine* e);
+int st_rtm_engine_result(st_rtm_engine* e, double* image, double* illumination, double* reflectivity);
+
+/* ------------------------------------------------------ FWI gradients */
+/* Sets the model from a device FP32 interior velocity (nx*ny*nz, x slowest);
+ * the host copy (reference layout, edge-replicated halo) is refreshed too. */
+int st_solver_set_velocity_device(st_solver* s, const float* vel);
+/* Gradient of <seismograms, adj_src> with respect to the velocity for one
+ * shot: forward with snapshot store (snap_kind BF16/FP16/FP32), then the
+ * exact discrete adjoint forced by adj_src (device FP32 [nt][nrec]) with the
+ * fused epilogue grad_c += lambda_t * L S_t; grad_v (device FP32 interior)
+ * receives += dJ/dv = grad_c * 2 v dt^2. No reference counterpart (the
+ * reference's adjoint-state gradient, seismic_tomography/gradient.py:24-40,
+ * is a pointwise formula). Needs nz * snapshot bytes divisible by 16. */
+int st_shot_gradient(st_solver* s, const st_shot* shot, const float* adj_src, int snap_kind, float* grad_v);
+/* L2 FWI for one shot: misfit += 1/2 sum (d - d_obs)^2 (FP64) and, when
+ * grad_v != NULL, grad_v += its velocity gradient; residual (device FP32
+ * [nt][nrec], may be NULL) receives d - d_obs. */
+int st_fwi_gradient(st_solver* s, const st_shot* shot, const float* d_obs, int snap_kind, float* grad_v,
+                    double* misfit, float* residual);
+
 /* ------------------------------------------------ seismic::CSRMatrix face */
 /* Device CSR: int64 row pointers, int32 column indices, FP32 values. Host
  * entry points take the reference's int64 indices and FP64 values. */

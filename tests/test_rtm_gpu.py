@@ -66,6 +66,22 @@ def test_adjoint_dot_product_and_trace(se, oracle, coincident):
     assert rel(tr, ref["src_adj"][:, 0]) < 1e-4
 
 
+def test_rtm_engine_matches_reference_fixture(se, golden_dir):
+    """RTMEngine face: the reference's own imaging-condition outputs (FP64)."""
+    g = np.load(os.path.join(golden_dir, "rtm_small.npz"))
+    nx, ny, nz = (int(v) for v in g["n"])
+    e = se.RTMEngine(nx, ny, nz, 10.0, 10.0, 10.0, 1)
+    for t in range(g["fwd"].shape[0]):
+        e.apply_image_condition(g["fwd"][t], g["adj"][t], ny + 2, nz + 2, t)
+    e.finalize_image()
+    r = e.result()
+    np.testing.assert_allclose(r.image, g["image"], rtol=1e-13, atol=1e-13)
+    np.testing.assert_allclose(r.illumination, g["illum"], rtol=1e-13, atol=1e-13)
+    np.testing.assert_allclose(r.reflectivity, g["refl"], rtol=1e-12, atol=1e-12)
+    e.reset_image()
+    assert not e.result().image.any()
+
+
 def rtm_case(se, oracle, n=(28, 24, 32), nt=90):
     w = se.workloads.small_case(n=n, nt=nt, seed=12, sponge_width=5)
     shot = w.shots[0]
