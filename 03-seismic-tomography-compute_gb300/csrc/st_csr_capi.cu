@@ -51,6 +51,19 @@ struct Scratch {
     }
 };
 
+}  // namespace
+
+namespace stg {
+// The matrix, device and stream of a handle (for solver variants in other files).
+const DevCsr* csr_matrix_of(const st_csr* m, int* device, cudaStream_t* stream) {
+    *device = m->device;
+    *stream = m->stream;
+    return &m->A;
+}
+}  // namespace stg
+
+namespace {
+
 #define ST_ALLOC(ok) ST_CHECK(static_cast<bool>(ok), ST_ERR_ALLOC, "device allocation failed")
 
 int make_handle(int device, st_csr** out) {

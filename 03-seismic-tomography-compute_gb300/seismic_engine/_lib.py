@@ -139,6 +139,7 @@ SIGNATURES = {
     "st_csr_clone": [_vp, C.POINTER(_vp)],
     "st_cg": [_vp, _d, C.c_int64, C.c_int, C.c_double, C.c_int, _d, C.POINTER(C.c_int), _d],
     "st_cg_device": [_vp, _vp, _vp, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int), _d],
+    "st_cg_device_static": [_vp, _vp, _vp, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int), _d],
     "st_normal_cg_device": [_vp, _vp, C.c_double, C.c_int, C.c_double, C.c_int, _vp, _vp, C.POINTER(C.c_int), _d,
                             _d],
     "st_dot": [_d, _d, C.c_int64, C.c_int, _d],

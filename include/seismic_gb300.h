@@ -303,6 +303,23 @@ int st_cg(st_csr* A, const double* b, int64_t nb, int max_iter, double tol, int 
           double* final_rel);
 int st_cg_device(st_csr* A, const float* b, float* x, int max_iter, double tol, int jacobi, int* iters,
                  double* final_rel);
+/* CG without any device allocation (no reference counterpart). Same solver
+ * and arguments as st_cg_device, for callers that cannot allocate device
+ * memory while they run: services that hand all device memory to their own
+ * pool at start-up, plugin hosts that forbid allocation after
+ * initialisation, real-time loops that cannot risk an allocator stall or an
+ * out-of-memory failure mid-run. Its scratch (5 FP32 vectors of
+ * ST_CG_STATIC_MAX_N floats, 20 MiB) is one file-scope device array that
+ * every GPU loading this library keeps until the process exits.
+ *  - Systems larger than ST_CG_STATIC_MAX_N unknowns are refused (ST_ERR_ARG).
+ *  - The first call on a device looks up the array's device address; make
+ *    that first call before any stream capture on that device.
+ *  - All calls on a device share the array, so calls that overlap on the GPU
+ *    (other host threads, other streams) race; serialise them. The array keeps
+ *    the last call's contents; the solver re-initialises everything it reads. */
+#define ST_CG_STATIC_MAX_N 1048576
+int st_cg_device_static(st_csr* A, const float* b, float* x, int max_iter, double tol, int jacobi, int* iters,
+                        double* final_rel);
 /* Tomography solve: (A^T A + lam I) x = A^T d for a rectangular A (no
  * reference counterpart), Jacobi diagonal = column sums of A^2 + lam when
  * jacobi != 0. rhs (may be NULL) receives A^T d; true_rel (may be NULL) the
