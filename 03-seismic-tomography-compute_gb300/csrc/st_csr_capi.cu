@@ -188,6 +188,35 @@ int st_csr_build_fd_stencil_7point(st_csr* m, int64_t nx, int64_t ny, int64_t nz
     return ST_OK;
 }
 
+int st_csr_build_ray_matrix(st_csr* m, int64_t n_rays, const double* endpoints, int on_device, int64_t nx,
+                            int64_t ny, int64_t nz, double cell_size, int64_t* nnz) {
+    ST_CHECK(m && (endpoints || n_rays == 0), ST_ERR_ARG, "null argument");
+    ST_CHECK(n_rays >= 0 && n_rays < (1ll << 31), ST_ERR_ARG, "ray count out of range (%lld)", (long long)n_rays);
+    ST_CHECK(nx > 0 && ny > 0 && nz > 0 && nx < (1 << 20) && ny < (1 << 20) && nz < (1 << 20), ST_ERR_ARG,
+             "bad grid extents");
+    ST_CUDA(cudaSetDevice(m->device));
+    Scratch sc;
+    const double* dends = endpoints;
+    if (!on_device && n_rays > 0) {
+        double* e = sc.get<double>((size_t)(6 * n_rays));
+        ST_ALLOC(e);
+        ST_CUDA(cudaMemcpyAsync(e, endpoints, (size_t)n_rays * 6 * 8, cudaMemcpyHostToDevice, m->stream));
+        dends = e;
+    }
+    DevCsr out;
+    long long total = 0;
+    int rc = build_ray_csr(n_rays, dends, (int)nx, (int)ny, (int)nz, cell_size, &out, &total, m->stream);
+    if (rc < 0) {
+        out.release();
+        return rc;
+    }
+    m->A.release();
+    drop_transpose(m);
+    m->A = out;
+    if (nnz) *nnz = total;
+    return ST_OK;
+}
+
 int st_csr_shape(st_csr* m, int64_t out[3]) {
     ST_CHECK(m && out, ST_ERR_ARG, "null argument");
     out[0] = m->A.rows;

@@ -274,4 +274,56 @@ int st_fwi_gradient(st_solver* s, const st_shot* shot, const float* d_obs, int s
     return (fl & FLAG_GUARD) ? ST_NAN_DETECTED_AND_REPAIRED : ST_OK;
 }
 
+int st_shot_gradient_checkpointed(st_solver* s, const st_shot* shot, const float* adj_src, int snap_kind,
+                                  int segment_steps, int max_slots, float* grad_v, st_checkpoint_stats* stats) {
+    ST_TRY(check_grad_args(s, shot, snap_kind));
+    ST_CHECK(grad_v && (shot->rec.nx * shot->rec.ny == 0 || adj_src), ST_ERR_ARG, "null argument");
+    ST_CHECK(shot->nt >= 0, ST_ERR_ARG, "negative nt");
+    ST_CUDA(cudaSetDevice(s->device));
+    GradScratch g;
+    ST_TRY(gradient_scratch(s, shot, ST_SNAP_NONE, &g));
+    ST_TRY(checkpointed_adjoint(s, shot, snap_kind, segment_steps, max_slots, 2, adj_src, nullptr, nullptr, g.gc,
+                                nullptr, nullptr, stats));
+    ST_TRY(finish_gradient(s, g, grad_v));
+    unsigned fl = 0;
+    ST_TRY(read_flags(s, &fl));
+    return (fl & FLAG_GUARD) ? ST_NAN_DETECTED_AND_REPAIRED : ST_OK;
+}
+
+int st_fwi_gradient_checkpointed(st_solver* s, const st_shot* shot, const float* d_obs, int snap_kind,
+                                 int segment_steps, int max_slots, float* grad_v, double* misfit, float* residual,
+                                 st_checkpoint_stats* stats) {
+    if (!grad_v) return st_fwi_gradient(s, shot, d_obs, snap_kind, nullptr, misfit, residual);
+    ST_TRY(check_grad_args(s, shot, snap_kind));
+    const int64_t nrec = shot->rec.nx * shot->rec.ny;
+    ST_CHECK(nrec > 0 && d_obs, ST_ERR_ARG, "FWI needs receivers and observed data");
+    ST_CHECK(shot->nt >= 0, ST_ERR_ARG, "negative nt");
+    ST_CUDA(cudaSetDevice(s->device));
+    GradScratch g;
+    ST_TRY(gradient_scratch(s, shot, ST_SNAP_NONE, &g));
+    const long long nd = (long long)shot->nt * nrec;
+    ST_CUDA(cudaMemsetAsync(g.misfit, 0, sizeof(double), s->stream));
+    // the residual forces the adjoint: it is formed once every seismogram row
+    // has been sampled, just before the first adjoint segment
+    auto residual_step = [&]() -> int {
+        if (nd > 0) {
+            residual_kernel<<<nblocks(nd), 256, 0, s->stream>>>(g.seis, d_obs, nd, g.res, g.misfit);
+            count_launch();
+            ST_CUDA(cudaGetLastError());
+            if (residual)
+                ST_CUDA(cudaMemcpyAsync(residual, g.res, (size_t)nd * 4, cudaMemcpyDeviceToDevice, s->stream));
+        }
+        return ST_OK;
+    };
+    ST_TRY(checkpointed_adjoint(s, shot, snap_kind, segment_steps, max_slots, 2, g.res, nullptr, nullptr, g.gc, g.seis,
+                                residual_step, stats));
+    ST_TRY(finish_gradient(s, g, grad_v));
+    double h = 0.0;
+    ST_CUDA(cudaMemcpyAsync(&h, g.misfit, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    unsigned fl = 0;
+    ST_TRY(read_flags(s, &fl));
+    if (misfit) *misfit += h;
+    return (fl & FLAG_GUARD) ? ST_NAN_DETECTED_AND_REPAIRED : ST_OK;
+}
+
 }  // extern "C"

@@ -46,8 +46,9 @@ struct FieldMaps {
 constexpr int FD_TZ = 64;
 
 int build_field_maps(FieldMaps* m, const float* base, const Layout& L);
-// x-chunks per CTA column for a tile height and resident CTAs per SM.
-int fd_step_grid_chunks(const Layout& L, int tyv, int minb);
+// x-chunks per CTA column for a tile height and resident CTAs per SM, with at
+// least min_waves waves of resident CTAs when the grid allows it.
+int fd_step_grid_chunks(const Layout& L, int tyv, int minb, int min_waves);
 
 // Launch one fused step. snap_out / snap_in are SnapKind values; epi: 0 = none,
 // 1 = imaging, 2 = gradient (needs msnap, the snapshot store's map).

@@ -421,6 +421,7 @@ int st_solver_destroy(st_solver* s) {
     cudaFree(s->snap_buf);
     cudaFree(s->aux_buf);
     cudaFree(s->data_buf);
+    cudaFree(s->ckpt_buf);
     for (int k = 0; k < 3; ++k)
         if (s->ev[k]) cudaEventDestroy(s->ev[k]);
     if (s->stream) cudaStreamDestroy(s->stream);

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <functional>
 #include <vector>
 
 namespace stg {
@@ -83,6 +84,8 @@ struct st_solver {
     size_t aux_cap = 0;
     void* data_buf = nullptr;       // host-API staging of receiver data
     size_t data_cap = 0;
+    void* ckpt_buf = nullptr;       // checkpointed adjoint: working set, state slots, segment snapshots
+    size_t ckpt_cap = 0;
     // phase boundaries of the last shot-level call, recorded on `stream`:
     // [0] start, [1] forward done, [2] backward done
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
@@ -109,4 +112,10 @@ inline void set_injection(StepArgs& a, int64_t ix, int64_t iy, int64_t iz, float
 }
 // Device scratch owned by the handle, grown on demand.
 int ensure_buffer(st_solver* s, void** buf, size_t* cap, size_t bytes);
+// Checkpointed adjoint pass (st_checkpoint.cu). epi 1: image / illum get the
+// imaging condition; epi 2: grad_c the coefficient gradient. seis (may be
+// null) receives the forward seismograms before before_backward runs.
+int checkpointed_adjoint(st_solver* s, const st_shot* shot, int snap_kind, int segment_steps, int max_slots, int epi,
+                         const float* force, float* image, float* illum, float* grad_c, float* seis,
+                         const std::function<int()>& before_backward, st_checkpoint_stats* stats);
 }  // namespace stg

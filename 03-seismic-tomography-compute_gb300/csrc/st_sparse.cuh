@@ -93,6 +93,10 @@ template <class TI, class TV>
 int build_csr(long long rows, long long cols, long long n, const TI* r, const TI* c, const TV* v, bool pad,
               DevCsr* out, cudaStream_t st);
 int build_transpose(const DevCsr& A, DevCsr* T, cudaStream_t st);
+// Straight-ray path-length matrix (st_rays.cu): d_ends = device [nrays][6]
+// endpoints in cell units; total_nnz (may be null) receives the entry count.
+int build_ray_csr(long long nrays, const double* d_ends, int nx, int ny, int nz, double h, DevCsr* out,
+                  long long* total_nnz, cudaStream_t st);
 int launch_spmv(const DevCsr& A, const float* x, float* y, const float* add, float add_scale, const float* pdot,
                 double* dot_acc, const int* done, cudaStream_t st);
 int launch_f64_to_f32(const double* a, float* b, long long n, cudaStream_t st);

@@ -613,7 +613,10 @@ int launch_variant(const Layout& L, const FieldMaps& mcur, const FieldMaps& mpre
             configured = true;
         }
     }
-    const int chunks = fd_step_grid_chunks(L, G::TYV, G::MINB);
+    // The forward variants run best as one wave of long x-chunks; the imaging
+    // and gradient variants (one row per thread, more resident CTAs) keep more
+    // loads in flight with at least four waves of shorter chunks.
+    const int chunks = fd_step_grid_chunks(L, G::TYV, G::MINB, EPI == EPI_NONE ? 1 : 4);
     a.x_chunk = (int)((L.nx + chunks - 1) / chunks);
     const int nch = (int)((L.nx + a.x_chunk - 1) / a.x_chunk);
     dim3 grid((unsigned)((L.nz + TZ - 1) / TZ), (unsigned)((L.ny + G::TYV - 1) / G::TYV), (unsigned)nch);
@@ -804,7 +807,7 @@ int build_field_maps(FieldMaps* m, const float* base, const Layout& L) {
     return ST_OK;
 }
 
-int fd_step_grid_chunks(const Layout& L, int tyv, int minb) {
+int fd_step_grid_chunks(const Layout& L, int tyv, int minb, int min_waves) {
     const long long gx = (L.nz + TZ - 1) / TZ, gy = (L.ny + tyv - 1) / tyv;
     const long long tiles = gx * gy;
     // tuning override: SEISMIC_GB300_XCHUNKS=<chunks> (1..nx)
@@ -819,7 +822,9 @@ int fd_step_grid_chunks(const Layout& L, int tyv, int minb) {
     long long best = 1;
     double best_eff = -1.0;
     const long long max_chunks = std::max<long long>(1, std::min<long long>(L.nx / 4, 256));
-    for (long long ch = 1; ch <= max_chunks; ++ch) {
+    const long long need = min_waves > 1 ? (long long)std::ceil(min_waves * slots / (double)tiles) : 1;
+    const long long first = std::min<long long>(std::max<long long>(1, need), max_chunks);
+    for (long long ch = first; ch <= max_chunks; ++ch) {
         const double waves = (double)(tiles * ch) / slots;
         const double fill = waves / std::ceil(waves);
         const double len = std::ceil((double)L.nx / (double)ch);

@@ -9,7 +9,8 @@ All compute runs in libseismic_gb300.so (CUDA, sm_103a) through its C ABI
 from ._lib import SeismicError, load as load_library, lib_path  # noqa: F401
 from .wave import (  # noqa: F401
     FaultStats, GridParams, HealthStatus, PropagationResult, SolverConfig, StepResult, WaveEquationSolver,
-    WaveField, field_layout, rtm_shot, rtm_shot_host, shot_adjoint, shot_forward, shot_forward_host,
+    WaveField, field_layout, rtm_shot, rtm_shot_checkpointed, rtm_shot_host, shot_adjoint, shot_forward,
+    shot_forward_host,
 )
 from .sparse import CSRMatrix, SparseOps, compute_fd_stencil, normal_cg_device  # noqa: F401
 from .fields import check_field_health, clamp_field_safe, repair_field_nan  # noqa: F401

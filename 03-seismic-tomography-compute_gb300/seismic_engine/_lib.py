@@ -24,7 +24,7 @@ ST_ERR_TIMEOUT = -5
 ST_ERR_UNSUPPORTED = -6
 
 ST_FIELD_CURRENT, ST_FIELD_PREVIOUS, ST_FIELD_NEXT, ST_FIELD_VELOCITY = 0, 1, 2, 3
-ST_SNAP_NONE, ST_SNAP_BF16, ST_SNAP_FP16, ST_SNAP_FP32, ST_SNAP_CHECKPOINT = 0, 1, 2, 3, 4
+ST_SNAP_NONE, ST_SNAP_BF16, ST_SNAP_FP16, ST_SNAP_FP32 = 0, 1, 2, 3
 
 
 class SeismicError(RuntimeError):
@@ -59,6 +59,12 @@ class FaultStatsC(C.Structure):
 class ReceiverGridC(C.Structure):
     _fields_ = [("x0", C.c_int64), ("sx", C.c_int64), ("nx", C.c_int64),
                 ("y0", C.c_int64), ("sy", C.c_int64), ("ny", C.c_int64), ("z", C.c_int64)]
+
+
+class CheckpointStatsC(C.Structure):
+    _fields_ = [("forward_steps", C.c_int64), ("adjoint_steps", C.c_int64), ("state_copies", C.c_int64),
+                ("segments", C.c_int), ("segment_steps", C.c_int), ("slots_used", C.c_int),
+                ("device_bytes", C.c_int64)]
 
 
 class ShotC(C.Structure):
@@ -119,6 +125,12 @@ SIGNATURES = {
     "st_solver_set_velocity_device": [_vp, _vp],
     "st_shot_gradient": [_vp, C.POINTER(ShotC), _vp, C.c_int, _vp],
     "st_fwi_gradient": [_vp, C.POINTER(ShotC), _vp, C.c_int, _vp, _d, _vp],
+    "st_rtm_shot_checkpointed": [_vp, C.POINTER(ShotC), _vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp,
+                                 C.POINTER(CheckpointStatsC)],
+    "st_shot_gradient_checkpointed": [_vp, C.POINTER(ShotC), _vp, C.c_int, C.c_int, C.c_int, _vp,
+                                      C.POINTER(CheckpointStatsC)],
+    "st_fwi_gradient_checkpointed": [_vp, C.POINTER(ShotC), _vp, C.c_int, C.c_int, C.c_int, _vp, _d, _vp,
+                                     C.POINTER(CheckpointStatsC)],
     # sparse
     "st_csr_create": [C.c_int64, C.c_int64, C.c_int64, C.c_int, C.POINTER(_vp)],
     "st_csr_destroy": [_vp],
@@ -126,6 +138,7 @@ SIGNATURES = {
     "st_csr_build_from_triplets_device": [_vp, C.c_int64, C.c_int64, C.c_int64, _vp, _vp, _vp, C.c_int],
     "st_csr_build_fd_stencil_7point": [_vp, C.c_int64, C.c_int64, C.c_int64, _d, C.c_double, C.c_double,
                                        C.c_double, C.c_double, C.c_int],
+    "st_csr_build_ray_matrix": [_vp, C.c_int64, _vp, C.c_int, C.c_int64, C.c_int64, C.c_int64, C.c_double, _i64],
     "st_csr_shape": [_vp, _i64],
     "st_csr_get": [_vp, _i64, _i64, _d],
     "st_csr_device_arrays": [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)],

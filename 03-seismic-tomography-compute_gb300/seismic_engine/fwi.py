@@ -20,21 +20,43 @@ def set_velocity_device(solver: WaveEquationSolver, vel: torch.Tensor):
     torch.cuda.current_stream().synchronize()
 
 
-def shot_gradient(solver, src, wavelet, nt, rec, adj_src, grad_v, snap_kind=_lib.ST_SNAP_FP32):
-    """grad_v += d<F(v), adj_src>/dv for one shot (device tensors)."""
+def _ckpt(checkpoint):
+    """checkpoint: None (store every step) or (segment_steps, max_slots)."""
+    if checkpoint is None:
+        return None
+    seg, slots = checkpoint
+    return int(seg), int(slots)
+
+
+def shot_gradient(solver, src, wavelet, nt, rec, adj_src, grad_v, snap_kind=_lib.ST_SNAP_FP32, checkpoint=None):
+    """grad_v += d<F(v), adj_src>/dv for one shot (device tensors). With
+    checkpoint=(segment_steps, max_slots) the forward history is recomputed
+    from FP32 checkpoints instead of stored for every step."""
     shot, _keep = _shot_c(src, wavelet, nt, rec)
-    return call("st_shot_gradient", solver.handle, C.byref(shot), adj_src.data_ptr(), int(snap_kind),
-                grad_v.data_ptr())
+    ck = _ckpt(checkpoint)
+    if ck is None:
+        return call("st_shot_gradient", solver.handle, C.byref(shot), adj_src.data_ptr(), int(snap_kind),
+                    grad_v.data_ptr())
+    st = _lib.CheckpointStatsC()
+    call("st_shot_gradient_checkpointed", solver.handle, C.byref(shot), adj_src.data_ptr(), int(snap_kind), ck[0],
+         ck[1], grad_v.data_ptr(), C.byref(st))
+    return {k: getattr(st, k) for k, _ in _lib.CheckpointStatsC._fields_}
 
 
-def fwi_gradient(solver, src, wavelet, nt, rec, d_obs, grad_v=None, snap_kind=_lib.ST_SNAP_FP32, residual=None):
+def fwi_gradient(solver, src, wavelet, nt, rec, d_obs, grad_v=None, snap_kind=_lib.ST_SNAP_FP32, residual=None,
+                 checkpoint=None):
     """L2 misfit 1/2 sum (F(v) - d_obs)^2 of one shot (FP64) and, when grad_v is
-    given, grad_v += its gradient."""
+    given, grad_v += its gradient (checkpoint as in shot_gradient)."""
     shot, _keep = _shot_c(src, wavelet, nt, rec)
     m = C.c_double(0.0)
-    call("st_fwi_gradient", solver.handle, C.byref(shot), d_obs.data_ptr(), int(snap_kind),
-         grad_v.data_ptr() if grad_v is not None else None, C.byref(m),
-         residual.data_ptr() if residual is not None else None)
+    gv = grad_v.data_ptr() if grad_v is not None else None
+    rs = residual.data_ptr() if residual is not None else None
+    ck = _ckpt(checkpoint)
+    if ck is None:
+        call("st_fwi_gradient", solver.handle, C.byref(shot), d_obs.data_ptr(), int(snap_kind), gv, C.byref(m), rs)
+    else:
+        call("st_fwi_gradient_checkpointed", solver.handle, C.byref(shot), d_obs.data_ptr(), int(snap_kind), ck[0],
+             ck[1], gv, C.byref(m), rs, None)
     return m.value
 
 
@@ -44,7 +66,7 @@ class SeismicModeling(torch.autograd.Function):
     kernel), forward snapshots recomputed and stored with snap_kind."""
 
     @staticmethod
-    def forward(ctx, vel, solver, shots, nt, snap_kind):
+    def forward(ctx, vel, solver, shots, nt, snap_kind, checkpoint=None):
         from .wave import shot_forward
         set_velocity_device(solver, vel)
         nrec = shots[0].rec.count
@@ -53,7 +75,7 @@ class SeismicModeling(torch.autograd.Function):
             shot_forward(solver, sh.src, sh.wavelet, nt, sh.rec, seis=out[i])
         torch.cuda.synchronize()
         ctx.save_for_backward(vel)
-        ctx.solver, ctx.shots, ctx.nt, ctx.snap_kind = solver, shots, nt, snap_kind
+        ctx.solver, ctx.shots, ctx.nt, ctx.snap_kind, ctx.checkpoint = solver, shots, nt, snap_kind, checkpoint
         return out.to(vel.dtype)
 
     @staticmethod
@@ -64,10 +86,14 @@ class SeismicModeling(torch.autograd.Function):
         g = torch.zeros(vel.shape, device="cuda", dtype=torch.float32)
         go = grad_out.to(dtype=torch.float32).contiguous()
         for i, sh in enumerate(ctx.shots):
-            shot_gradient(solver, sh.src, sh.wavelet, ctx.nt, sh.rec, go[i].contiguous(), g, ctx.snap_kind)
+            shot_gradient(solver, sh.src, sh.wavelet, ctx.nt, sh.rec, go[i].contiguous(), g, ctx.snap_kind,
+                          checkpoint=ctx.checkpoint)
         torch.cuda.synchronize()
-        return g.to(vel.dtype), None, None, None, None
+        return g.to(vel.dtype), None, None, None, None, None
 
 
-def modeling(vel: torch.Tensor, solver: WaveEquationSolver, shots, nt: int, snap_kind=_lib.ST_SNAP_FP32):
-    return SeismicModeling.apply(vel, solver, shots, nt, snap_kind)
+def modeling(vel: torch.Tensor, solver: WaveEquationSolver, shots, nt: int, snap_kind=_lib.ST_SNAP_FP32,
+             checkpoint=None):
+    """Differentiable seismograms; checkpoint=(segment_steps, max_slots)
+    recomputes the forward history in backward instead of storing it."""
+    return SeismicModeling.apply(vel, solver, shots, nt, snap_kind, checkpoint)

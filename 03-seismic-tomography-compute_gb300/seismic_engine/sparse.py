@@ -84,6 +84,22 @@ class CSRMatrix:
         return self
 
     # ---- accessors (csr_matrix.h:32-38)
+    def build_ray_matrix(self, endpoints, nx: int, ny: int, nz: int, cell_size: float = 1.0) -> int:
+        """Straight-ray path-length matrix: row i = ray endpoints[i] =
+        (x0, y0, z0, x1, y1, z1) in cell units (numpy FP64 or a CUDA FP64
+        tensor); returns nnz."""
+        nnz = C.c_int64()
+        if hasattr(endpoints, "data_ptr"):
+            e = endpoints.contiguous()
+            assert e.dtype.is_floating_point and e.element_size() == 8 and e.is_cuda
+            call("st_csr_build_ray_matrix", self.handle, e.numel() // 6, e.data_ptr(), 1, nx, ny, nz,
+                 float(cell_size), C.byref(nnz))
+        else:
+            e = np.ascontiguousarray(endpoints, np.float64).reshape(-1)
+            call("st_csr_build_ray_matrix", self.handle, e.size // 6, e.ctypes.data, 0, nx, ny, nz,
+                 float(cell_size), C.byref(nnz))
+        return nnz.value
+
     def _shape(self):
         out = (C.c_int64 * 3)()
         call("st_csr_shape", self._h, out)

@@ -296,6 +296,25 @@ def rtm_shot(solver: WaveEquationSolver, src, wavelet, nt: int, rec, data, image
                 ptr(snap_amax), image.data_ptr(), illum.data_ptr(), ptr(refl))
 
 
+def _stats_dict(st) -> dict:
+    return {k: getattr(st, k) for k, _ in _lib.CheckpointStatsC._fields_}
+
+
+def rtm_shot_checkpointed(solver: WaveEquationSolver, src, wavelet, nt: int, rec, data, image, illum, refl=None,
+                          snap_kind: int = _lib.ST_SNAP_BF16, segment_steps: int = 100, max_slots: int = 1 << 30):
+    """rtm_shot without the nt-snapshot store: FP32 forward states are kept
+    at segment boundaries (at most max_slots of them, binomial schedule) and
+    each segment is recomputed into a segment_steps-snapshot buffer. Same
+    result as rtm_shot with the same snap_kind. Returns the schedule's
+    statistics (forward / adjoint steps run, state copies, device bytes)."""
+    shot, _keep = _shot_c(src, wavelet, nt, rec)
+    st = _lib.CheckpointStatsC()
+    call("st_rtm_shot_checkpointed", solver.handle, C.byref(shot), data.data_ptr(), snap_kind, int(segment_steps),
+         int(max_slots), image.data_ptr(), illum.data_ptr(), refl.data_ptr() if refl is not None else None,
+         C.byref(st))
+    return _stats_dict(st)
+
+
 def rtm_shot_host(solver: WaveEquationSolver, vel_ref, src, wavelet, nt: int, rec, data_host,
                   snap_kind: int = _lib.ST_SNAP_BF16, want=("image", "illumination", "reflectivity")):
     """Host-buffer RTM (every copy included). data_host: FP32 numpy [nt, nrec]

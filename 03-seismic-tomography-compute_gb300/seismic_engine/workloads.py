@@ -187,3 +187,61 @@ def small_case(n=(24, 20, 28), nt: int = 80, seed: int = 7, sponge_width: int = 
     w = ricker(25.0, dt, nt)
     return Workload("small", nx, ny, nz, 10.0, dt, nt, v,
                     [ShotSpec((nx // 2, ny // 2, 4), w, rec)], sponge_width=sponge_width)
+
+
+# ------------------------------------------------------------ traveltime tomography
+
+@dataclass
+class RayTomography:
+    """Straight-ray traveltime tomography on an n^3 cell grid: ray endpoints
+    (cell units), the true model x_true, the damping lam, and the seeds of
+    the data noise."""
+    name: str
+    n: int
+    ends: np.ndarray      # [n_rays, 6] FP64: x0 y0 z0 x1 y1 z1
+    x_true: np.ndarray    # n^3 FP64, x slowest
+    lam: float
+    noise_seed: int
+    noise_level: float = 0.01
+
+
+def ray_endpoints(n_rays: int, n: int = 100, seed: int = 4) -> np.ndarray:
+    """Sources uniform on the surface z = 0; receivers in one of four vertical
+    boreholes at cells (0.1n, 0.1n), (0.1n, 0.9n), (0.9n, 0.1n), (0.9n, 0.9n)
+    (cell centres), depth uniform in [0, n). Each ray goes to the borehole
+    diagonally opposite its source quadrant, which lengthens the paths to
+    about 1.8 n cells crossed per ray."""
+    rng = np.random.default_rng(seed)
+    xs = rng.uniform(0.0, n, n_rays)
+    ys = rng.uniform(0.0, n, n_rays)
+    zr = rng.uniform(0.0, n, n_rays)
+    near, far = int(0.1 * n) + 0.5, int(0.9 * n) + 0.5
+    bx = np.where(xs < 0.5 * n, far, near)
+    by = np.where(ys < 0.5 * n, far, near)
+    return np.stack([xs, ys, np.zeros(n_rays), bx, by, zr], axis=1)
+
+
+def smooth_model(n: int, sigma: float, seed: int) -> np.ndarray:
+    """Seeded white noise smoothed with a Gaussian (sigma cells), unit std."""
+    from scipy.ndimage import gaussian_filter
+    x = gaussian_filter(np.random.default_rng(seed).standard_normal((n, n, n)), sigma, mode="nearest")
+    return (x / x.std()).reshape(-1)
+
+
+def tomography_100(n_rays: int = 2_000_000, seed: int = 4) -> RayTomography:
+    """100^3 cells (1M unknowns), 2M straight surface-to-borehole rays,
+    (A^T A + 1e-2 I) x = A^T b with b = A x_true + 1% noise (seed 44)."""
+    n = 100
+    return RayTomography("tomo-100^3-2M-rays", n, ray_endpoints(n_rays, n, seed), smooth_model(n, 5.0, seed + 36),
+                         1e-2, 44)
+
+
+def tomography_small(n: int = 20, n_rays: int = 3000, seed: int = 7) -> RayTomography:
+    return RayTomography(f"tomo-{n}^3", n, ray_endpoints(n_rays, n, seed), smooth_model(n, 2.0, seed + 36), 1e-2,
+                         seed + 40)
+
+
+def noisy_data(A_x: np.ndarray, level: float, seed: int) -> np.ndarray:
+    """b = A x_true + level * std(A x_true) * N(0, 1)."""
+    noise = np.random.default_rng(seed).standard_normal(A_x.size)
+    return A_x + level * float(np.std(A_x)) * noise

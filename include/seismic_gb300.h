@@ -44,8 +44,9 @@ enum st_status {
 /* Which field of WaveEquationSolver::field() (wave_equation.h:16-22). */
 enum st_field_id { ST_FIELD_CURRENT = 0, ST_FIELD_PREVIOUS = 1, ST_FIELD_NEXT = 2, ST_FIELD_VELOCITY = 3 };
 
-/* Storage of forward snapshots for RTM / gradients. */
-enum st_snap_kind { ST_SNAP_NONE = 0, ST_SNAP_BF16 = 1, ST_SNAP_FP16 = 2, ST_SNAP_FP32 = 3, ST_SNAP_CHECKPOINT = 4 };
+/* Storage of forward snapshots for RTM / gradients (every step, or per
+ * segment in the checkpointed entry points). */
+enum st_snap_kind { ST_SNAP_NONE = 0, ST_SNAP_BF16 = 1, ST_SNAP_FP16 = 2, ST_SNAP_FP32 = 3 };
 
 /* seismic::GridParams (core/grid.h:9-20). halo_width must be 1 (7-point stencil). */
 typedef struct st_grid_params {
@@ -248,6 +249,36 @@ int st_shot_gradient(st_solver* s, const st_shot* shot, const float* adj_src, in
 int st_fwi_gradient(st_solver* s, const st_shot* shot, const float* d_obs, int snap_kind, float* grad_v,
                     double* misfit, float* residual);
 
+/* ------------------------------------------- checkpointed adjoint passes */
+/* The RTM and gradient passes above store one snapshot per time step
+ * (nt * nx*ny*nz values). These variants keep exact FP32 forward states
+ * (current + previous field) at segment boundaries of segment_steps steps,
+ * in at most max_slots slots (>= 1) chosen by a binomial (revolve) schedule,
+ * recompute one segment at a time into a segment_steps-snapshot buffer of
+ * snap_kind, and run that segment's adjoint steps from it. Results equal the
+ * store-every-step entry points with the same snap_kind. Device memory:
+ * (3 + 2 * min(max_slots, segments)) fields + segment_steps snapshots. With
+ * max_slots >= segments the cost is one extra forward sweep; fewer slots
+ * trade memory for more recomputation. No reference counterpart (the
+ * reference keeps its history in host memory, solver/wave_equation.cpp:463-480). */
+typedef struct st_checkpoint_stats {
+    int64_t forward_steps;  /* forward time steps run (first sweep + recomputes) */
+    int64_t adjoint_steps;
+    int64_t state_copies;   /* checkpoint stores and restores */
+    int segments;
+    int segment_steps;
+    int slots_used;
+    int64_t device_bytes;   /* scratch of the call */
+} st_checkpoint_stats;
+int st_rtm_shot_checkpointed(st_solver* s, const st_shot* shot, const float* data, int snap_kind,
+                             int segment_steps, int max_slots, float* image, float* illum, float* refl,
+                             st_checkpoint_stats* stats);
+int st_shot_gradient_checkpointed(st_solver* s, const st_shot* shot, const float* adj_src, int snap_kind,
+                                  int segment_steps, int max_slots, float* grad_v, st_checkpoint_stats* stats);
+int st_fwi_gradient_checkpointed(st_solver* s, const st_shot* shot, const float* d_obs, int snap_kind,
+                                 int segment_steps, int max_slots, float* grad_v, double* misfit, float* residual,
+                                 st_checkpoint_stats* stats);
+
 /* ------------------------------------------------ seismic::CSRMatrix face */
 /* Device CSR: int64 row pointers, int32 column indices, FP32 values. Host
  * entry points take the reference's int64 indices and FP64 values. */
@@ -273,6 +304,15 @@ int st_csr_build_from_triplets_device(st_csr* m, int64_t rows, int64_t cols, int
  * nx*ny*nz interior on the host. */
 int st_csr_build_fd_stencil_7point(st_csr* m, int64_t nx, int64_t ny, int64_t nz, const double* velocity, double dx,
                                    double dy, double dz, double dt, int pad);
+/* Straight-ray path-length matrix for traveltime tomography (no reference
+ * counterpart in C++; the reference's Python inversion samples the same
+ * straight rays at midpoints, seismic_tomography/inversion.py:329-433): row i
+ * = ray i from (x0,y0,z0) to (x1,y1,z1) (endpoints[6*i..6*i+5], in cell units,
+ * host or device memory), A[i, (ix*ny + iy)*nz + iz] = length of the ray inside
+ * that cell * cell_size, by exact voxel traversal; columns ascending, no
+ * padding. nnz (may be NULL) receives the entry count. */
+int st_csr_build_ray_matrix(st_csr* m, int64_t n_rays, const double* endpoints, int on_device, int64_t nx,
+                            int64_t ny, int64_t nz, double cell_size, int64_t* nnz);
 /* rows(), cols(), nnz() (csr_matrix.h:32-34): out = {rows, cols, nnz}. */
 int st_csr_shape(st_csr* m, int64_t out[3]);
 /* row_ptr(), col_ind(), values() (csr_matrix.h:36-38) copied to the host (any may be NULL). */

@@ -93,6 +93,9 @@ class Oracle:
         L.orc_normal_apply.argtypes = [C.c_void_p, C.c_double, _d, _d]
         L.orc_smooth_gradient.argtypes = [_d, C.c_int64, C.c_int64, C.c_int64, C.c_double, _d]
         L.orc_num_threads.restype = C.c_int
+        L.orc_ray_triplets.argtypes = [C.c_int64, _d, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int64, _i64, _i64,
+                                       _d]
+        L.orc_ray_triplets.restype = C.c_int64
         L.orc64_repair_field_nan.argtypes = [_d, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int, C.c_double]
         L.orc64_repair_field_nan.restype = C.c_int64
         L.orc64_clamp_field.argtypes = [_d, C.c_int64, C.c_double, C.c_double]
@@ -242,6 +245,18 @@ class Oracle:
         y = np.zeros(m.cols)
         self.lib.orc_normal_apply(m.h, lam, _p(x, _d), _p(y, _d))
         return y
+
+    def ray_matrix(self, ends, nx, ny, nz, h=1.0):
+        """Straight-ray path-length CSR (row_ptr, col, FP64 val) of rays
+        ends[i] = (x0, y0, z0, x1, y1, z1) in cell units."""
+        e = np.ascontiguousarray(ends, np.float64).reshape(-1, 6)
+        cap = max(1, e.shape[0] * (nx + ny + nz + 3))
+        r = np.zeros(cap, np.int64)
+        c = np.zeros(cap, np.int64)
+        v = np.zeros(cap, np.float64)
+        k = self.lib.orc_ray_triplets(e.shape[0], _p(e, _d), nx, ny, nz, h, cap, _p(r, _i64), _p(c, _i64), _p(v, _d))
+        assert k >= 0
+        return self.csr_build(e.shape[0], nx * ny * nz, r[:k], c[:k], v[:k])
 
     def smooth_gradient(self, g, nx, ny, nz, sigma):
         g = np.ascontiguousarray(g, np.float64).reshape(-1)

@@ -517,3 +517,62 @@ int64_t orc64_count_nan_inf(const double* d, int64_t count) {
     for (int64_t i = 0; i < count; ++i) n += !isfinite(d[i]);
     return n;
 }
+
+/* ------------------------------------------------------------ ray matrix */
+/* Straight-ray path lengths by exact voxel traversal (Amanatides & Woo 1987),
+ * restated from the algorithm, not from the reference: the reference's
+ * Python inversion (seismic_tomography/inversion.py:329-433) samples the same
+ * straight rays at n = max(floor(dist / (5 dx)), 2) midpoints instead. The ray
+ * p(t) = p0 + t (p1 - p0), t in [0, 1], is cut at the cell faces in order of
+ * t, ties to x, then y, then z; segment length = (t_exit - t) * |p1 - p0| * h.
+ * FP64, evaluated in source order (this file is built with
+ * -ffp-contract=off), so the GPU path can match it bit for bit. Emits
+ * (row, col, value) triplets; returns their count, or -1 when cap is too
+ * small. Parity of this restatement is against the traversal definition, not
+ * against reference output (the reference has no such builder). */
+static double orc_t_exit(int c, int step, double p0, double d) {
+    if (step == 0) return 1e300;
+    const double face = (double)(step > 0 ? c + 1 : c);
+    return (face - p0) / d;
+}
+
+int64_t orc_ray_triplets(int64_t nrays, const double* ends, int nx, int ny, int nz, double h, int64_t cap,
+                         int64_t* rows, int64_t* cols, double* vals) {
+    int64_t k = 0;
+    const int n[3] = {nx, ny, nz};
+    for (int64_t i = 0; i < nrays; ++i) {
+        const double* e = ends + 6 * i;
+        const double p0[3] = {e[0], e[1], e[2]};
+        const double d[3] = {e[3] - e[0], e[4] - e[1], e[5] - e[2]};
+        const double len = sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+        int c[3], step[3];
+        double tm[3];
+        for (int a = 0; a < 3; ++a) {
+            int f = (int)floor(p0[a]);
+            c[a] = f < 0 ? 0 : (f > n[a] - 1 ? n[a] - 1 : f);
+            step[a] = d[a] > 0.0 ? 1 : (d[a] < 0.0 ? -1 : 0);
+            tm[a] = orc_t_exit(c[a], step[a], p0[a], d[a]);
+        }
+        double t = 0.0;
+        const int max_iter = nx + ny + nz + 3;
+        for (int it = 0; it < max_iter; ++it) {
+            const int ax = (tm[0] <= tm[1] && tm[0] <= tm[2]) ? 0 : (tm[1] <= tm[2] ? 1 : 2);
+            const double tn = tm[ax];
+            const double te = tn < 1.0 ? tn : 1.0;
+            const double seg = ((te - t) * len) * h;
+            if (seg > 0.0) {
+                if (k >= cap) return -1;
+                rows[k] = i;
+                cols[k] = ((int64_t)c[0] * ny + c[1]) * nz + c[2];
+                vals[k] = seg;
+                ++k;
+            }
+            if (tn >= 1.0) break;
+            t = tn;
+            c[ax] += step[ax];
+            if (c[ax] < 0 || c[ax] >= n[ax]) break;
+            tm[ax] = orc_t_exit(c[ax], step[ax], p0[ax], d[ax]);
+        }
+    }
+    return k;
+}
