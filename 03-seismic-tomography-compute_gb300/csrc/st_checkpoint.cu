@@ -38,14 +38,6 @@ __global__ void absmax_kernel(const float* __restrict__ f, long long n, unsigned
     if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
 }
 
-__global__ void ckpt_rec_force_kernel(float* f, const float* c, Layout L, st_receiver_grid R, const float* row) {
-    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (q >= R.nx * R.ny) return;
-    const long long irx = q / R.ny, iry = q - irx * R.ny;
-    const long long i = L.at(R.x0 + irx * R.sx, R.y0 + iry * R.sy, R.z);
-    f[i] += c[i] * row[q];
-}
-
 // C(s + r, s), saturated.
 double binom_steps(int s, int r) {
     double v = 1.0;
@@ -225,10 +217,7 @@ int backward(CkptRun& c, int j) {
             ST_CUDA(cudaMemsetAsync(c.grad_c, 0, npts * sizeof(float), s->stream));
         }
         if (nrec > 0) {
-            ckpt_rec_force_kernel<<<(unsigned)((nrec + 255) / 256), 256, 0, s->stream>>>(
-                s->f[s->ic], s->c, L, R, c.force + (size_t)(nt - 1) * nrec);
-            count_launch();
-            ST_CUDA(cudaGetLastError());
+            ST_TRY(launch_rec_force(s, R, c.force + (size_t)(nt - 1) * nrec));
         }
         c.started = true;
     }

@@ -89,14 +89,6 @@ void set_receivers_args(StepArgs& a, const st_receiver_grid& R) {
     a.rny = (int)R.ny;
 }
 
-__global__ void rec_force_c_kernel(float* f, const float* c, Layout L, st_receiver_grid R, const float* row) {
-    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (q >= R.nx * R.ny) return;
-    const long long irx = q / R.ny, iry = q - irx * R.ny;
-    const long long i = L.at(R.x0 + irx * R.sx, R.y0 + iry * R.sy, R.z);
-    f[i] += c[i] * row[q];
-}
-
 double cfl_damp(st_solver* s) {
     // the coefficient array already carries damp^2; recover damp from it is
     // not possible per point, so recompute the reference rule on the host copy
@@ -127,10 +119,7 @@ int gradient_backward_impl(st_solver* s, const st_shot* shot, const float* adj, 
     ST_CUDA(cudaMemsetAsync(grad_c, 0, npts * sizeof(float), s->stream));
     if (nt <= 0) return ST_OK;
     if (nrec > 0) {
-        rec_force_c_kernel<<<(unsigned)((nrec + 255) / 256), 256, 0, s->stream>>>(s->f[s->ic], s->c, L, R,
-                                                                                 adj + (size_t)(nt - 1) * nrec);
-        count_launch();
-        ST_CUDA(cudaGetLastError());
+        ST_TRY(launch_rec_force(s, R, adj + (size_t)(nt - 1) * nrec));
     }
     for (int t = nt - 1; t >= 0; --t) {
         StepArgs a = base_args(s, nullptr);

@@ -26,13 +26,27 @@ struct StepArgs {
     unsigned* amax_next;     // |max| of the written field is atomically max-ed here
     const void* snap_in;     // forward snapshot paired with this step's centre field (imaging)
     const unsigned* amax_in;
-    float* image;            // image += f * (centre / c)   (compact interior)
+    float* image;            // image += f * (centre / c), centre / (c D) with the stable sponge
     float* illum;            // illum += f * f
     float* grad;             // gradient: grad += (centre / c) * L(snapshot)   (compact interior)
     int snap_t;              // gradient: time index of the snapshot in the store
     unsigned* flags;         // FLAG_GUARD / FLAG_TIMEOUT
     unsigned long long timeout_ns;
+    int stable_sponge;       // 1: out = D * (update + forcing) (damped new field), 0: the reference rule
 };
+
+// Sponge factor of interior point (ix, iy, iz): D(d) for the distance d to the
+// nearest face when d < sw, else 1 (apply_sponge_layer, wave_equation.cpp:262-297).
+__device__ __forceinline__ float sponge_D(const Layout& L, const float* dtab, int sw, long long ix, long long iy,
+                                          long long iz) {
+    long long d = ix;
+    d = min(d, L.nx - 1 - ix);
+    d = min(d, iy);
+    d = min(d, L.ny - 1 - iy);
+    d = min(d, iz);
+    d = min(d, L.nz - 1 - iz);
+    return (d >= 0 && d < sw) ? dtab[d] : 1.0f;
+}
 
 // Tensor maps of one device field for the two tile heights of the stencil
 // kernels ([0]: 16-row tiles, [1]: 32-row tiles): cur boxes {TZ+8, rows+2, 1}

@@ -24,23 +24,31 @@
 namespace stg {
 namespace {
 
-// f[receiver q] += (c at q) * row[q] over a receiver grid.
-__global__ void rec_force_kernel(float* f, const float* c, Layout L, st_receiver_grid R, const float* row) {
+// f[receiver q] += (c at q) * row[q] over a receiver grid (times the sponge
+// factor D at q with the stable sponge: mu = c D lambda).
+__global__ void rec_force_kernel(float* f, const float* c, Layout L, st_receiver_grid R, const float* row,
+                                 const float* dtab, int sw, int stable) {
     const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long n = R.nx * R.ny;
     if (q >= n) return;
     const long long irx = q / R.ny, iry = q - irx * R.ny;
-    const long long i = L.at(R.x0 + irx * R.sx, R.y0 + iry * R.sy, R.z);
-    f[i] += c[i] * row[q];
+    const long long ix = R.x0 + irx * R.sx, iy = R.y0 + iry * R.sy;
+    const long long i = L.at(ix, iy, R.z);
+    const float w = stable ? c[i] * sponge_D(L, dtab, sw, ix, iy, R.z) : c[i];
+    f[i] += w * row[q];
 }
 
 // trace[t] = lambda at the source before the forcing of step t-1:
-// (mu - c * d_{t-1}[q_src]) / c, where q_src < 0 when the source is not a receiver.
-__global__ void probe_kernel(const float* f, const float* c, long long idx, const float* force_row, long long q,
+// (mu - w * d_{t-1}[q_src]) / w with w = c (w = c D with the stable sponge),
+// where q_src < 0 when the source is not a receiver.
+__global__ void probe_kernel(const float* f, const float* c, Layout L, long long ix, long long iy, long long iz,
+                             const float* force_row, long long q, const float* dtab, int sw, int stable,
                              float* out) {
+    const long long idx = L.at(ix, iy, iz);
+    const float w = stable ? c[idx] * sponge_D(L, dtab, sw, ix, iy, iz) : c[idx];
     float v = f[idx];
-    if (force_row && q >= 0) v -= c[idx] * force_row[q];
-    *out = v / c[idx];
+    if (force_row && q >= 0) v -= w * force_row[q];
+    *out = v / w;
 }
 
 __global__ void f32_to_f64_kernel(const float* a, double* b, long long n) {
@@ -69,6 +77,16 @@ void set_receivers(StepArgs& a, const st_receiver_grid& R) {
 }
 
 }  // namespace
+
+int launch_rec_force(st_solver* s, const st_receiver_grid& R, const float* row) {
+    const long long nrec = R.nx * R.ny;
+    if (nrec <= 0) return ST_OK;
+    rec_force_kernel<<<(unsigned)((nrec + 255) / 256), 256, 0, s->stream>>>(s->f[s->ic], s->c, s->L, R, row, s->dtab,
+                                                                           s->sw, s->sponge_mode);
+    count_launch();
+    ST_CUDA(cudaGetLastError());
+    return ST_OK;
+}
 
 // Forward shot (shared by st_shot_forward and the RTM / gradient drivers).
 // seis may be null (no sampling); snap_kind != NONE needs snaps and amax.
@@ -136,10 +154,7 @@ int rtm_backward_impl(st_solver* s, const st_shot* shot, const float* data, int 
     }
     if (nt <= 0) return ST_OK;
     if (nrec > 0) {
-        rec_force_kernel<<<(unsigned)((nrec + 255) / 256), 256, 0, s->stream>>>(s->f[s->ic], s->c, L, R,
-                                                                               data + (size_t)(nt - 1) * nrec);
-    ::stg::count_launch();
-        ST_CUDA(cudaGetLastError());
+        ST_TRY(launch_rec_force(s, R, data + (size_t)(nt - 1) * nrec));
     }
     const long long src = dev_index(s, shot->src_ix, shot->src_iy, shot->src_iz);
     const long long q_src = receiver_at(R, shot->src_ix, shot->src_iy, shot->src_iz);
@@ -157,7 +172,8 @@ int rtm_backward_impl(st_solver* s, const st_shot* shot, const float* data, int 
         }
         ST_TRY(fused_step(s, a, SNAP_NONE, imaging ? snap_kind : SNAP_NONE, imaging ? 1 : 0, nullptr));
         if (src_trace) {
-            probe_kernel<<<1, 1, 0, s->stream>>>(s->f[s->ic], s->c, src, a.force_row, q_src, src_trace + t);
+            probe_kernel<<<1, 1, 0, s->stream>>>(s->f[s->ic], s->c, L, shot->src_ix, shot->src_iy, shot->src_iz,
+                                                 a.force_row, q_src, s->dtab, s->sw, s->sponge_mode, src_trace + t);
     ::stg::count_launch();
             ST_CUDA(cudaGetLastError());
         }

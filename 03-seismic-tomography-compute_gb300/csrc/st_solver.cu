@@ -203,6 +203,7 @@ StepArgs base_args(st_solver* s, float* out) {
     a.inj_x = -1;
     a.flags = s->flags;
     a.rsx = a.rsy = 1;
+    a.stable_sponge = s->sponge_mode == ST_SPONGE_STABLE;
     return a;
 }
 
@@ -553,7 +554,9 @@ int st_solver_get_field(st_solver* s, int which, double* out, int64_t count) {
     ST_CUDA(cudaSetDevice(s->device));
     ST_TRY(ensure_staging(s));
     const float* src = which == ST_FIELD_CURRENT ? s->f[s->ic] : (which == ST_FIELD_PREVIOUS ? s->f[s->ip] : s->f[s->in]);
-    ST_TRY(launch_dev_to_ref(src, s->staging, s->L, s->dtab, s->sw, which, s->stream));
+    // stored damping of the reference layout: previous D, next D^2 (D with the stable sponge)
+    const int pw = (which == ST_FIELD_NEXT && s->sponge_mode == ST_SPONGE_STABLE) ? 1 : which;
+    ST_TRY(launch_dev_to_ref(src, s->staging, s->L, s->dtab, s->sw, pw, s->stream));
     ST_CUDA(cudaMemcpyAsync(out, s->staging, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     ST_CUDA(cudaStreamSynchronize(s->stream));
     return ST_OK;
@@ -569,8 +572,22 @@ int st_solver_set_field(st_solver* s, int which, const double* in, int64_t count
     ST_TRY(ensure_staging(s));
     float* dst = which == ST_FIELD_CURRENT ? s->f[s->ic] : (which == ST_FIELD_PREVIOUS ? s->f[s->ip] : s->f[s->in]);
     ST_CUDA(cudaMemcpyAsync(s->staging, in, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-    ST_TRY(launch_ref_to_dev_undamp(s->staging, dst, s->L, s->dtab, s->sw, which, s->stream));
+    const int pw = (which == ST_FIELD_NEXT && s->sponge_mode == ST_SPONGE_STABLE) ? 1 : which;
+    ST_TRY(launch_ref_to_dev_undamp(s->staging, dst, s->L, s->dtab, s->sw, pw, s->stream));
     ST_CUDA(cudaStreamSynchronize(s->stream));
+    return ST_OK;
+}
+
+int st_solver_set_sponge_mode(st_solver* s, int mode) {
+    ST_CHECK(s, ST_ERR_ARG, "null solver");
+    ST_CHECK(mode == ST_SPONGE_REFERENCE || mode == ST_SPONGE_STABLE, ST_ERR_ARG, "bad sponge mode %d", mode);
+    s->sponge_mode = mode;
+    return ST_OK;
+}
+
+int st_solver_sponge_mode(st_solver* s, int* mode) {
+    ST_CHECK(s && mode, ST_ERR_ARG, "null argument");
+    *mode = s->sponge_mode;
     return ST_OK;
 }
 

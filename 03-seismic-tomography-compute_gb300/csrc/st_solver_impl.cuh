@@ -86,6 +86,7 @@ struct st_solver {
     size_t data_cap = 0;
     void* ckpt_buf = nullptr;       // checkpointed adjoint: working set, state slots, segment snapshots
     size_t ckpt_cap = 0;
+    int sponge_mode = ST_SPONGE_REFERENCE;  // ST_SPONGE_STABLE: damp the new field (Cerjan form)
     // phase boundaries of the last shot-level call, recorded on `stream`:
     // [0] start, [1] forward done, [2] backward done
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
@@ -112,6 +113,9 @@ inline void set_injection(StepArgs& a, int64_t ix, int64_t iy, int64_t iz, float
 }
 // Device scratch owned by the handle, grown on demand.
 int ensure_buffer(st_solver* s, void** buf, size_t* cap, size_t bytes);
+// Adjoint forcing of the receiver grid into the current field:
+// f += c * row (c * D * row with the stable sponge), st_rtm.cu.
+int launch_rec_force(st_solver* s, const st_receiver_grid& R, const float* row);
 // Checkpointed adjoint pass (st_checkpoint.cu). epi 1: image / illum get the
 // imaging condition; epi 2: grad_c the coefficient gradient. seis (may be
 // null) receives the forward seismograms before before_backward runs.

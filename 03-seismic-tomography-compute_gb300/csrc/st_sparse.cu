@@ -160,8 +160,21 @@ __global__ void __launch_bounds__(256) spmv_kernel(const long long* __restrict__
     double local = 0.0;
     for (long long row = gid; row < rows; row += stride) {
         const long long a = rp[row], b = rp[row + 1];
-        float sum = 0.0f;
-        for (long long p = a + lane; p < b; p += G) sum = fmaf(__ldg(val + p), __ldg(x + __ldg(col + p)), sum);
+        // four independent gathers in flight per lane on long rows
+        float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+        long long p = a + lane;
+        for (; p + 3 * G < b; p += 4 * G) {
+            const int c0 = __ldg(col + p), c1 = __ldg(col + p + G), c2 = __ldg(col + p + 2 * G),
+                      c3 = __ldg(col + p + 3 * G);
+            const float v0 = __ldg(val + p), v1 = __ldg(val + p + G), v2 = __ldg(val + p + 2 * G),
+                        v3 = __ldg(val + p + 3 * G);
+            s0 = fmaf(v0, __ldg(x + c0), s0);
+            s1 = fmaf(v1, __ldg(x + c1), s1);
+            s2 = fmaf(v2, __ldg(x + c2), s2);
+            s3 = fmaf(v3, __ldg(x + c3), s3);
+        }
+        for (; p < b; p += G) s0 = fmaf(__ldg(val + p), __ldg(x + __ldg(col + p)), s0);
+        float sum = (s0 + s1) + (s2 + s3);
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(FULL, sum, o, G);
         if (lane == 0) {

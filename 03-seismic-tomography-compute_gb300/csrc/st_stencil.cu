@@ -23,6 +23,15 @@
 //   - the adjoint-state gradient grad_c += (mu / c) * L S of a forward
 //     snapshot S staged through TMA with its halo.
 //
+// Stable sponge (opt-in, StepArgs::stable_sponge): the reference rule
+// u_{n+1} = 2u_n - D u_{n-1} + c L u_n grows exponentially for smooth modes in
+// a wide sponge (characteristic roots 1 +- sqrt(1 - D) when c L u is small;
+// the default 20-cell, 0.015 sponge diverges within a few hundred steps).
+// The Cerjan form damps the new field instead:
+//     out = D * (2u - D*prev + c L u)        (prev = the undamped u_{n-1})
+// whose roots have modulus D < 1. Its adjoint is again this operator for
+// mu = c * D * lambda, with forcing c * D * r entering before the damping.
+//
 // Data movement: each CTA owns a (16 or 32) x 64 (y,z) tile and marches along
 // x (the slowest axis), staging every x-plane of u (with a one-cell y/z halo),
 // prev and c in shared memory with TMA (cp.async.bulk.tensor, no multicast) in
@@ -243,14 +252,24 @@ __device__ __forceinline__ void process_row(const StepArgs& a, const RowCtx& R, 
                                 fired);
         res[k] = nv;
     }
-    if (rk >= 0 && irx >= 0 && R.iry >= 0) {
-        const int q = irx * a.rny + R.iry;
+    // Receivers: the adjoint forcing enters before the damping of the new
+    // field (stable sponge), the forward samples read the stored value. The
+    // two never meet in one step.
+    const bool rec_here = rk >= 0 && irx >= 0 && R.iry >= 0;
+    const int q = rec_here ? irx * a.rny + R.iry : 0;
+    if (rec_here && a.force_row) {
 #pragma unroll
         for (int k = 0; k < 4; ++k)
-            if (k == rk) {
-                if (a.seis_row) a.seis_row[q] = res[k];
-                if (a.force_row) res[k] = fmaf(cv[k], a.force_row[q], res[k]);
-            }
+            if (k == rk) res[k] = fmaf(cv[k], a.force_row[q], res[k]);
+    }
+    if (a.stable_sponge) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) res[k] *= D[k];
+    }
+    if (rec_here && a.seis_row) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k == rk) a.seis_row[q] = res[k];
     }
     if (R.inj && x == a.inj_x) {
 #pragma unroll
@@ -284,7 +303,7 @@ __device__ __forceinline__ void process_row(const StepArgs& a, const RowCtx& R, 
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 float f = fin[k];
-                float ad = u0[k] / cv[k];
+                float ad = u0[k] / (a.stable_sponge ? cv[k] * D[k] : cv[k]);
                 if (!isfinite(f)) f = 0.0f;
                 if (!isfinite(ad)) ad = 0.0f;
                 im[k] = fmaf(f, ad, im[k]);
@@ -296,7 +315,7 @@ __device__ __forceinline__ void process_row(const StepArgs& a, const RowCtx& R, 
             const float sc = __uint_as_float(*a.amax_in) / SNAP_QMAX;
             for (int k = 0; k < zvalid; ++k) {
                 float f = snap_load<SNAP_IN>(a.snap_in, cbase + k) * sc;
-                float ad = u0[k] / cv[k];
+                float ad = u0[k] / (a.stable_sponge ? cv[k] * D[k] : cv[k]);
                 if (!isfinite(f)) f = 0.0f;
                 if (!isfinite(ad)) ad = 0.0f;
                 a.image[cbase + k] += f * ad;

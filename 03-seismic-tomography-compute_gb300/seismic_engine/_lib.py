@@ -25,6 +25,7 @@ ST_ERR_UNSUPPORTED = -6
 
 ST_FIELD_CURRENT, ST_FIELD_PREVIOUS, ST_FIELD_NEXT, ST_FIELD_VELOCITY = 0, 1, 2, 3
 ST_SNAP_NONE, ST_SNAP_BF16, ST_SNAP_FP16, ST_SNAP_FP32 = 0, 1, 2, 3
+ST_SPONGE_REFERENCE, ST_SPONGE_STABLE = 0, 1
 
 
 class SeismicError(RuntimeError):
@@ -96,6 +97,8 @@ SIGNATURES = {
     "st_solver_reset_field": [_vp],
     "st_solver_get_field": [_vp, C.c_int, _d, C.c_int64],
     "st_solver_set_field": [_vp, C.c_int, _d, C.c_int64],
+    "st_solver_set_sponge_mode": [_vp, C.c_int],
+    "st_solver_sponge_mode": [_vp, C.POINTER(C.c_int)],
     "st_solver_compute_energy": [_vp, _d],
     "st_solver_verify_cfl": [_vp, C.POINTER(C.c_int)],
     "st_solver_set_amplitude_limit": [_vp, C.c_double],
@@ -131,6 +134,9 @@ SIGNATURES = {
                                       C.POINTER(CheckpointStatsC)],
     "st_fwi_gradient_checkpointed": [_vp, C.POINTER(ShotC), _vp, C.c_int, C.c_int, C.c_int, _vp, _d, _vp,
                                      C.POINTER(CheckpointStatsC)],
+    "st_conv3d_pack_weights": [_vp, _vp, C.c_int, _vp],
+    "st_conv3d_bf16": [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int64, C.c_int64, C.c_int64, C.c_int, _vp],
+    "st_conv3d_check": [_vp],
     # sparse
     "st_csr_create": [C.c_int64, C.c_int64, C.c_int64, C.c_int, C.POINTER(_vp)],
     "st_csr_destroy": [_vp],

@@ -67,6 +67,9 @@ class SolverConfig:
     sponge_damping: float = 0.015
     snapshot_interval: int = 100
     output_dir: str = "./output"
+    # "reference": the reference's sponge rule (diverges for wide sponges);
+    # "stable": the new field is damped (Cerjan form). Not a reference key.
+    sponge_mode: str = "reference"
 
     def c(self) -> _lib.SolverConfigC:
         return _lib.SolverConfigC(self.frequency, self.dt, self.nt, self.water_depth, self.seafloor_gradient,
@@ -124,6 +127,7 @@ class WaveEquationSolver:
         h = C.c_void_p()
         call("st_solver_create", C.byref(grid.c()), C.byref(config.c()), device, C.byref(h), allow_status=False)
         self._h = h
+        self.set_sponge_mode(getattr(config, "sponge_mode", "reference"))
         self.nx, self.ny, self.nz = grid.nx_global, grid.ny_global, grid.nz_global
         self.padded_size = (self.nx + 2) * (self.ny + 2) * (self.nz + 2)
 
@@ -141,6 +145,16 @@ class WaveEquationSolver:
     @property
     def handle(self):
         return self._h
+
+    def set_sponge_mode(self, mode):
+        """'reference' (default, the reference's rule) or 'stable' (Cerjan form)."""
+        m = {"reference": _lib.ST_SPONGE_REFERENCE, "stable": _lib.ST_SPONGE_STABLE}.get(mode, mode)
+        call("st_solver_set_sponge_mode", self._h, int(m))
+
+    def sponge_mode(self) -> str:
+        m = C.c_int()
+        call("st_solver_sponge_mode", self._h, C.byref(m))
+        return "stable" if m.value == _lib.ST_SPONGE_STABLE else "reference"
 
     def grid(self) -> GridParams:
         return self._grid

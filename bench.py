@@ -79,7 +79,7 @@ def config_dict(w, snap, n_gpus):
         "grid": [w.nx, w.ny, w.nz], "nt": w.nt, "dx_m": w.d, "dt_s": w.dt,
         "snapshots": f"{snap}+per-snapshot scale, store-all",
         "receivers": f"{w.shots[0].rec.nx}x{w.shots[0].rec.ny} on z={w.shots[0].rec.z}",
-        "sponge": [w.sponge_width, w.sponge_damping],
+        "sponge": [w.sponge_width, w.sponge_damping, w.sponge_mode],
         "l2": "inputs larger than L2: 4 FP32 fields of %.0f MB each + %.0f GB of snapshots" % (
             (w.nx + 2) * (w.ny + 2) * (w.nz + 8) * 4 / 1e6,
             w.nx * w.ny * w.nz * w.nt * (4 if snap == "fp32" else 2) / 1e9),
@@ -199,7 +199,7 @@ def cpu_rtm_sample(w, nt_sample):
     from oracle import Oracle
     from seismic_engine import workloads as wl
     o = Oracle()
-    g = o.grid(w.nx, w.ny, w.nz, w.d, w.d, w.d, w.dt, w.sponge_width, w.sponge_damping)
+    g = o.grid(w.nx, w.ny, w.nz, w.d, w.d, w.d, w.dt, w.sponge_width, w.sponge_damping, sponge_mode=w.sponge_mode)
     shot = w.shots[0]
     vel = wl.to_reference_layout(w.vel_migration)
     rec = shot.rec.coords()
@@ -266,7 +266,8 @@ def run_gpu(args):
     rec = shot.rec
     snap_kind = {"bf16": _lib.ST_SNAP_BF16, "fp16": _lib.ST_SNAP_FP16, "fp32": _lib.ST_SNAP_FP32}[args.snap]
     grid = se.GridParams(w.nx, w.ny, w.nz, w.d, w.d, w.d)
-    cfg = se.SolverConfig(dt=w.dt, nt=w.nt, sponge_width=w.sponge_width, sponge_damping=w.sponge_damping)
+    cfg = se.SolverConfig(dt=w.dt, nt=w.nt, sponge_width=w.sponge_width, sponge_damping=w.sponge_damping,
+                          sponge_mode=w.sponge_mode)
     s = se.WaveEquationSolver(grid, cfg, device=torch.cuda.current_device())
     vel_true = se.workloads.to_reference_layout(w.vel)
     vel_mig = se.workloads.to_reference_layout(w.vel_migration)

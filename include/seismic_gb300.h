@@ -139,6 +139,18 @@ int st_solver_reset_field(st_solver* s);
 /* field() / mutable_field() (wave_equation.h:72-73) in the reference layout. */
 int st_solver_get_field(st_solver* s, int which, double* out, int64_t count);
 int st_solver_set_field(st_solver* s, int which, const double* in, int64_t count);
+/* Sponge rule of every step taken by the handle. ST_SPONGE_REFERENCE (the
+ * default) is apply_sponge_layer as the reference calls it
+ * (wave_equation.cpp:56-76,262-297): current and previous damped after the
+ * update, u_{n+1} = 2u_n - D u_{n-1} + c L u_n, which grows without bound for
+ * smooth modes in wide sponges (the 20-cell, 0.015 default diverges within a
+ * few hundred steps). ST_SPONGE_STABLE damps the new field instead (Cerjan
+ * form), u_{n+1} = D (2u_n - D u_{n-1} + c L u_n), and is stable; the adjoint,
+ * imaging, gradient and checkpointed entry points follow the mode. No
+ * reference counterpart for the stable mode. */
+enum st_sponge_mode { ST_SPONGE_REFERENCE = 0, ST_SPONGE_STABLE = 1 };
+int st_solver_set_sponge_mode(st_solver* s, int mode);
+int st_solver_sponge_mode(st_solver* s, int* mode);
 /* Replaces compute_energy (wave_equation.cpp:482-490): FP64 sum of squares of finite current values. */
 int st_solver_compute_energy(st_solver* s, double* out);
 /* Replaces verify_cfl (wave_equation.cpp:445-451). */
@@ -278,6 +290,22 @@ int st_shot_gradient_checkpointed(st_solver* s, const st_shot* shot, const float
 int st_fwi_gradient_checkpointed(st_solver* s, const st_shot* shot, const float* d_obs, int snap_kind,
                                  int segment_steps, int max_slots, float* grad_v, double* misfit, float* residual,
                                  st_checkpoint_stats* stats);
+
+/* ------------------------------------- learned-preconditioner conv layer */
+/* 3x3x3 convolution of a 32-channel volume on the tensor cores (tcgen05,
+ * BF16 operands, FP32 accumulation); no reference counterpart (the learned
+ * CG preconditioner is new). Volumes of D x H x W voxels are padded and
+ * channels-last: [(D+2)(H+2)(W+2)][32] BF16, zero on the one-voxel border
+ * (out keeps that convention). out = relu?(conv(in) + bias + add), BF16 or,
+ * with out_fp32, FP32. packed_w: 55,296 bytes from st_conv3d_pack_weights.
+ * Asynchronous on `stream` (a cudaStream_t); W <= 156 (ST_ERR_UNSUPPORTED
+ * beyond: the shared-memory windows). st_conv3d_check
+ * synchronises the stream and reports a bounded-wait timeout of any earlier
+ * conv launch (ST_ERR_TIMEOUT), clearing it. */
+int st_conv3d_pack_weights(const float* w_oidhw, void* packed_w, int transpose, void* stream);
+int st_conv3d_bf16(const void* in, const void* packed_w, const float* bias, const void* add, void* out, int out_fp32,
+                   int64_t D, int64_t H, int64_t W, int relu, void* stream);
+int st_conv3d_check(void* stream);
 
 /* ------------------------------------------------ seismic::CSRMatrix face */
 /* Device CSR: int64 row pointers, int32 column indices, FP32 values. Host

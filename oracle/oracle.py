@@ -31,7 +31,7 @@ class OrcGrid(C.Structure):
     _fields_ = [("nx", C.c_int64), ("ny", C.c_int64), ("nz", C.c_int64),
                 ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double), ("dt", C.c_double),
                 ("sponge_width", C.c_int), ("sponge_damping", C.c_double),
-                ("amp_limit", C.c_double), ("cfl_safety", C.c_double)]
+                ("amp_limit", C.c_double), ("cfl_safety", C.c_double), ("sponge_mode", C.c_int)]
 
 
 def build_oracle(force: bool = False) -> str:
@@ -104,8 +104,12 @@ class Oracle:
 
     # ------------------------------------------------------------ propagator
     @staticmethod
-    def grid(nx, ny, nz, dx, dy, dz, dt, sponge_width=20, sponge_damping=0.015, amp_limit=1e10):
-        return OrcGrid(nx, ny, nz, dx, dy, dz, dt, sponge_width, sponge_damping, amp_limit, 0.49)
+    def grid(nx, ny, nz, dx, dy, dz, dt, sponge_width=20, sponge_damping=0.015, amp_limit=1e10,
+             sponge_mode="reference"):
+        """sponge_mode: "reference" (the reference's rule) or "stable" (Cerjan
+        form: the new field and the current are damped)."""
+        return OrcGrid(nx, ny, nz, dx, dy, dz, dt, sponge_width, sponge_damping, amp_limit, 0.49,
+                       1 if sponge_mode == "stable" else 0)
 
     def run(self, g: OrcGrid, vel, nsteps, src_xyz, src_w, rec_xyz, fp32=False, keep_states=False,
             init_cur=None, init_prev=None):

@@ -142,7 +142,8 @@ static int64_t FN(repair_nan)(REAL* d, int64_t count, int64_t nx, int64_t ny, in
 }
 
 /* Full reference step (step_forward == step_adjoint, wave_equation.cpp:56-98):
- * operator pass into *nxt, sponge on cur and prev, rotation
+ * operator pass into *nxt, sponge on cur and prev (cur and nxt with
+ * g->sponge_mode == 1, the stable form that is not in the reference), rotation
  * prev<-cur, cur<-nxt, nxt<-old prev, then the NaN health check with repair
  * (perform_health_check :407-424 -> FaultTolerance::attempt_recovery
  * fault_tolerance.cpp:198-257, 3 attempts). Returns the StepResult code. */
@@ -150,7 +151,8 @@ static int FN(step)(const orc_grid* g, const REAL* vel, REAL** cur, REAL** prev,
     const int64_t NXh = g->nx + 2, NYh = g->ny + 2, NZh = g->nz + 2, n = NXh * NYh * NZh;
     int fired = FN(fd7)(g, vel, *cur, *prev, *nxt);
     REAL* C = *cur;
-    REAL* Pv = *prev;
+    /* reference: damp current and previous; stable mode: the new field and current */
+    REAL* Pv = g->sponge_mode == 1 ? *nxt : *prev;
 #pragma omp parallel for schedule(static)
     for (int64_t ix = 0; ix < NXh; ++ix)
         for (int64_t iy = 0; iy < NYh; ++iy)

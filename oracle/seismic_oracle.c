@@ -33,6 +33,8 @@ typedef struct {
     double sponge_damping;
     double amp_limit;     /* WaveEquationSolver amplitude_limit_, default 1e10 */
     double cfl_safety;    /* FaultTolerance cfl_safety_factor_, default 0.49 */
+    int sponge_mode;      /* 0: the reference rule (damp current and previous after the update);
+                             1: stable Cerjan form (damp the new field and the current) - not in the reference */
 } orc_grid;
 
 #define REAL double
@@ -128,9 +130,18 @@ int orc64_adjoint(const orc_grid* g, const double* vel, int nt, int nrec, const 
                             double lap = (V[i + P] - 2.0 * V[i] + V[i - P]) * idx2 +
                                          (V[i + NZh] - 2.0 * V[i] + V[i - NZh]) * idy2 +
                                          (V[i + 1] - 2.0 * V[i] + V[i - 1]) * idz2;
-                            grad_c[k] += aC[i] * lap;
+                            grad_c[k] += (g->sponge_mode == 1 ? D[i] * aC[i] : aC[i]) * lap;
                         }
                     }
+        }
+        /* reference rule: (C, P) -> (2C - P + cLC, D C); transpose:
+         *   aC <- 2 aC' + L(c aC') + D aP',  aP <- -aC'.
+         * stable rule: (C, P) -> (D (2C - P + cLC), D C); with b = D aC':
+         *   aC <- 2 b + L(c b) + D aP',  aP <- -b.
+         * aP is kept premultiplied by D. */
+        if (g->sponge_mode == 1) {
+#pragma omp parallel for schedule(static)
+            for (int64_t i = 0; i < n; ++i) aC[i] *= D[i];
         }
 #pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < n; ++i) {

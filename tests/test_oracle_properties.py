@@ -7,14 +7,15 @@ import pytest
 from seismic_engine import workloads as wl
 
 
-def small(oracle, n=(10, 9, 11), nt=40, sw=3):
+def small(oracle, n=(10, 9, 11), nt=40, sw=3, mode="reference"):
     w = wl.small_case(n=n, nt=nt, seed=5, sponge_width=sw)
-    g = oracle.grid(w.nx, w.ny, w.nz, w.d, w.d, w.d, w.dt, w.sponge_width, w.sponge_damping)
+    g = oracle.grid(w.nx, w.ny, w.nz, w.d, w.d, w.d, w.dt, w.sponge_width, w.sponge_damping, sponge_mode=mode)
     return w, g
 
 
-def test_exact_adjoint_dot_product(oracle):
-    w, g = small(oracle)
+@pytest.mark.parametrize("mode", ["reference", "stable"])
+def test_exact_adjoint_dot_product(oracle, mode):
+    w, g = small(oracle, mode=mode)
     rng = np.random.default_rng(0)
     rec = w.shots[0].rec.coords()
     src = np.array([w.shots[0].src])
@@ -28,10 +29,11 @@ def test_exact_adjoint_dot_product(oracle):
     assert abs(lhs - rhs) <= 1e-11 * max(abs(lhs), 1e-300)
 
 
-def test_exact_adjoint_gradient_taylor(oracle):
+@pytest.mark.parametrize("mode", ["reference", "stable"])
+def test_exact_adjoint_gradient_taylor(oracle, mode):
     """J(c) = 1/2 ||F(c) - d||^2; the oracle's grad_c must give second-order
     Taylor remainders along a random smooth direction."""
-    w, g = small(oracle, n=(9, 8, 10), nt=30, sw=2)
+    w, g = small(oracle, n=(9, 8, 10), nt=30, sw=2, mode=mode)
     rng = np.random.default_rng(1)
     rec = w.shots[0].rec.coords()
     src = np.array([w.shots[0].src])
@@ -139,3 +141,22 @@ def test_fp32_floor_against_fp64(oracle):
     b = oracle.run(g, vel, w.nt, src, w.shots[0].wavelet[:, None], rec, fp32=True)
     rel = np.linalg.norm(b["seis"] - a["seis"]) / np.linalg.norm(a["seis"])
     assert rel < 1e-5
+
+
+def blob_run(oracle, mode, nt, n=40, sw=20):
+    v = np.full((n, n, n), 3000.0)
+    g = oracle.grid(n, n, n, 10.0, 10.0, 10.0, 0.001, sw, 0.015, sponge_mode=mode)
+    x = np.arange(n + 2) - (n + 1) / 2
+    blob = np.exp(-(x[:, None, None] ** 2 + x[None, :, None] ** 2 + x[None, None, :] ** 2) / 8.0).reshape(-1)
+    r = oracle.run(g, wl.to_reference_layout(v), nt, np.zeros((0, 3), np.int64), np.zeros((nt, 0)),
+                   np.zeros((0, 3), np.int64), init_cur=blob, init_prev=blob)
+    return float(np.abs(r["cur"]).max())
+
+
+def test_reference_sponge_diverges_and_stable_sponge_decays(oracle):
+    """The reference's sponge rule (damp current and previous after the update)
+    amplifies smooth modes in a wide sponge: with the default 20 cells and
+    0.015 a unit blob grows past 1e3 within 300 steps, no source involved. The
+    stable (Cerjan) form decays."""
+    assert blob_run(oracle, "reference", 300) > 1e3
+    assert blob_run(oracle, "stable", 300) < 0.1
