@@ -294,6 +294,13 @@ static int spmv_host(st_csr* m, int transpose, const double* x, int64_t nx, doub
 int st_csr_spmv(st_csr* m, const double* x, int64_t nx, double* y) { return spmv_host(m, 0, x, nx, y); }
 int st_csr_spmv_transpose(st_csr* m, const double* x, int64_t nx, double* y) { return spmv_host(m, 1, x, nx, y); }
 
+int st_csr_normal_jacobi(st_csr* m, double lam, float* dinv) {
+    ST_CHECK(m && dinv, ST_ERR_ARG, "null argument");
+    ST_CUDA(cudaSetDevice(m->device));
+    ST_TRY(ensure_transpose(m));
+    return launch_normal_jacobi(m->AT, lam, dinv, m->stream);
+}
+
 int st_csr_frobenius_norm(st_csr* m, double* out) {
     ST_CHECK(m && out, ST_ERR_ARG, "null argument");
     ST_CUDA(cudaSetDevice(m->device));

@@ -137,6 +137,12 @@ SIGNATURES = {
     "st_conv3d_pack_weights": [_vp, _vp, C.c_int, _vp],
     "st_conv3d_bf16": [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int64, C.c_int64, C.c_int64, C.c_int, _vp],
     "st_conv3d_check": [_vp],
+    "st_pc_in_conv": [_vp, _vp, _vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, _vp],
+    "st_pc_in_conv_wgrad": [_vp, _vp, _vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, _vp],
+    "st_pc_out_conv": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, _vp],
+    "st_pc_out_conv_bwd": [_vp, _vp, _vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, _vp],
+    "st_pc_relu_mask": [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, _vp],
+    "st_conv3d_wgrad": [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, _vp],
     # sparse
     "st_csr_create": [C.c_int64, C.c_int64, C.c_int64, C.c_int, C.POINTER(_vp)],
     "st_csr_destroy": [_vp],
@@ -153,6 +159,7 @@ SIGNATURES = {
     "st_csr_spmv_transpose": [_vp, _d, C.c_int64, _d],
     "st_csr_spmv_device": [_vp, C.c_int, _vp, _vp],
     "st_csr_frobenius_norm": [_vp, _d],
+    "st_csr_normal_jacobi": [_vp, C.c_double, _vp],
     "st_csr_scale": [_vp, C.c_double],
     "st_csr_add_diagonal": [_vp, C.c_double],
     "st_csr_clone": [_vp, C.POINTER(_vp)],

@@ -209,12 +209,28 @@ class RayTomography:
     noise_level: float = 0.01
 
 
-def ray_endpoints(n_rays: int, n: int = 100, seed: int = 4) -> np.ndarray:
+def _morton2(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """Interleaved bits of two non-negative integer arrays (Z-order key)."""
+    key = np.zeros(a.shape, np.uint64)
+    a = a.astype(np.uint64)
+    b = b.astype(np.uint64)
+    for bit in range(16):
+        key |= ((a >> np.uint64(bit)) & np.uint64(1)) << np.uint64(2 * bit + 1)
+        key |= ((b >> np.uint64(bit)) & np.uint64(1)) << np.uint64(2 * bit)
+    return key
+
+
+def ray_endpoints(n_rays: int, n: int = 100, seed: int = 4, spatial_order: bool = True) -> np.ndarray:
     """Sources uniform on the surface z = 0; receivers in one of four vertical
     boreholes at cells (0.1n, 0.1n), (0.1n, 0.9n), (0.9n, 0.1n), (0.9n, 0.9n)
     (cell centres), depth uniform in [0, n). Each ray goes to the borehole
     diagonally opposite its source quadrant, which lengthens the paths to
-    about 1.8 n cells crossed per ray."""
+    about 1.8 n cells crossed per ray.
+
+    spatial_order lists the rays by borehole, then source cell in Z order,
+    then receiver depth, so rays that share cells sit close together (a
+    better cache footprint for the SpMV gathers). The set of rays is the
+    same; the damped normal equations do not depend on their order."""
     rng = np.random.default_rng(seed)
     xs = rng.uniform(0.0, n, n_rays)
     ys = rng.uniform(0.0, n, n_rays)
@@ -222,7 +238,13 @@ def ray_endpoints(n_rays: int, n: int = 100, seed: int = 4) -> np.ndarray:
     near, far = int(0.1 * n) + 0.5, int(0.9 * n) + 0.5
     bx = np.where(xs < 0.5 * n, far, near)
     by = np.where(ys < 0.5 * n, far, near)
-    return np.stack([xs, ys, np.zeros(n_rays), bx, by, zr], axis=1)
+    ends = np.stack([xs, ys, np.zeros(n_rays), bx, by, zr], axis=1)
+    if spatial_order:
+        hole = (bx > 0.5 * n).astype(np.int64) * 2 + (by > 0.5 * n).astype(np.int64)
+        src = _morton2(np.floor(xs).astype(np.int64), np.floor(ys).astype(np.int64))
+        order = np.lexsort((zr, src, hole))
+        ends = ends[order]
+    return ends
 
 
 def smooth_model(n: int, sigma: float, seed: int) -> np.ndarray:

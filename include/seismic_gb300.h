@@ -295,8 +295,10 @@ int st_fwi_gradient_checkpointed(st_solver* s, const st_shot* shot, const float*
 /* 3x3x3 convolution of a 32-channel volume on the tensor cores (tcgen05,
  * BF16 operands, FP32 accumulation); no reference counterpart (the learned
  * CG preconditioner is new). Volumes of D x H x W voxels are padded and
- * channels-last: [(D+2)(H+2)(W+2)][32] BF16, zero on the one-voxel border
- * (out keeps that convention). out = relu?(conv(in) + bias + add), BF16 or,
+ * channels-last: [(D+2)(H+2)(W+2)][32] BF16, zero on the one-voxel border.
+ * The kernel writes every row of padded planes 1..D (zero on their border
+ * ring) and never planes 0 and D+1, which the caller zeroes once.
+ * out = relu?(conv(in) + bias + add), BF16 or,
  * with out_fp32, FP32. packed_w: 55,296 bytes from st_conv3d_pack_weights.
  * Asynchronous on `stream` (a cudaStream_t); W <= 156 (ST_ERR_UNSUPPORTED
  * beyond: the shared-memory windows). st_conv3d_check
@@ -306,6 +308,28 @@ int st_conv3d_pack_weights(const float* w_oidhw, void* packed_w, int transpose, 
 int st_conv3d_bf16(const void* in, const void* packed_w, const float* bias, const void* add, void* out, int out_fp32,
                    int64_t D, int64_t H, int64_t W, int relu, void* stream);
 int st_conv3d_check(void* stream);
+/* CUDA-core layers of the learned preconditioner z = dinv r + s_out N(r)
+ * (no reference counterpart). r, dinv, z, zhat: compact FP32 nx*ny*nz
+ * (x slowest); h, dh, g: padded channels-last BF16 32-channel volumes;
+ * scale, s_out: one device FP32 each. Weights FP32: w_in [32][2][27],
+ * w_out [32][27], conv [32][32][27] (out, in, tap = (kd*3 + kh)*3 + kw).
+ *  st_pc_in_conv       h = relu(C_in([scale r, scale dinv r]))
+ *  st_pc_in_conv_wgrad dw_in += dL/dw_in for the masked gradient g of h
+ *  st_pc_out_conv      zhat = C_out(h); z = dinv r + s_out zhat (z, zhat may be NULL)
+ *  st_pc_out_conv_bwd  dh = C_out^T(dzhat); dw_out += dL/dw_out
+ *  st_pc_relu_mask     g = dh * [h > 0]
+ *  st_conv3d_wgrad     dw += sum_v g[v] (x) x[v + tap] for a 32 -> 32 layer
+ * All asynchronous on `stream`; gradients accumulate (zero them first). */
+int st_pc_in_conv(const float* r, const float* dinv, const float* scale, const float* w_in, void* h, int64_t nx,
+                  int64_t ny, int64_t nz, void* stream);
+int st_pc_in_conv_wgrad(const float* r, const float* dinv, const float* scale, const void* g, float* dw_in,
+                        int64_t nx, int64_t ny, int64_t nz, void* stream);
+int st_pc_out_conv(const void* h, const float* w_out, const float* r, const float* dinv, const float* s_out,
+                   float* zhat, float* z, int64_t nx, int64_t ny, int64_t nz, void* stream);
+int st_pc_out_conv_bwd(const float* dzhat, const void* h, const float* w_out, void* dh, float* dw_out, int64_t nx,
+                       int64_t ny, int64_t nz, void* stream);
+int st_pc_relu_mask(const void* dh, const void* h, void* g, int64_t nx, int64_t ny, int64_t nz, void* stream);
+int st_conv3d_wgrad(const void* x, const void* g, float* dw, int64_t nx, int64_t ny, int64_t nz, void* stream);
 
 /* ------------------------------------------------ seismic::CSRMatrix face */
 /* Device CSR: int64 row pointers, int32 column indices, FP32 values. Host
@@ -388,6 +412,9 @@ int st_cg_device(st_csr* A, const float* b, float* x, int max_iter, double tol, 
 #define ST_CG_STATIC_MAX_N 1048576
 int st_cg_device_static(st_csr* A, const float* b, float* x, int max_iter, double tol, int jacobi, int* iters,
                         double* final_rel);
+/* dinv (device FP32, cols) = 1 / (column sums of A^2 + lam): the Jacobi
+ * preconditioner of A^T A + lam I (asynchronous on the matrix's stream). */
+int st_csr_normal_jacobi(st_csr* A, double lam, float* dinv);
 /* Tomography solve: (A^T A + lam I) x = A^T d for a rectangular A (no
  * reference counterpart), Jacobi diagonal = column sums of A^2 + lam when
  * jacobi != 0. rhs (may be NULL) receives A^T d; true_rel (may be NULL) the
