@@ -443,6 +443,38 @@ int st_normal_cg_device(st_csr* m, const float* d, double lam, int max_iter, dou
     return ST_OK;
 }
 
+int st_normal_fcg_device(st_csr* m, const float* d, double lam, int max_iter, double tol, st_pcnet* pc, float* x,
+                         int* iters, double* true_rel) {
+    ST_CHECK(m && d && x, ST_ERR_ARG, "null argument");
+    ST_CHECK(max_iter >= 0, ST_ERR_ARG, "negative iteration limit");
+    ST_CUDA(cudaSetDevice(m->device));
+    ST_TRY(ensure_transpose(m));
+    const long long n = m->A.cols, rows = m->A.rows;
+    ST_CHECK(!pc || pcnet_points(pc) == n, ST_ERR_ARG, "network grid has %lld points, the system %lld unknowns",
+             pc ? pcnet_points(pc) : 0ll, n);
+    Scratch sc;
+    float* b = sc.get<float>((size_t)n);
+    float* dinv = sc.get<float>((size_t)n);
+    float* r = sc.get<float>((size_t)n);
+    float* z = sc.get<float>((size_t)n);
+    float* p = sc.get<float>((size_t)n);
+    float* q = sc.get<float>((size_t)n);
+    float* ax = sc.get<float>((size_t)n);
+    float* t = sc.get<float>((size_t)rows);
+    FcgScalars* s = sc.get<FcgScalars>(1);
+    double* acc = sc.get<double>(2);
+    ST_ALLOC(b && dinv && r && z && p && q && ax && t && s && acc);
+    ST_TRY(launch_spmv(m->AT, d, b, nullptr, 0.0f, nullptr, nullptr, nullptr, m->stream));
+    ST_TRY(launch_normal_jacobi(m->AT, lam, dinv, m->stream));
+    int it = 0;
+    double rel = 0.0;
+    ST_TRY(run_fcg(m->A, m->AT, lam, b, x, dinv, pc, max_iter, tol, r, z, p, q, ax, t, s, acc, m->stream, &it, &rel));
+    ST_CUDA(cudaStreamSynchronize(m->stream));
+    if (iters) *iters = it;
+    if (true_rel) *true_rel = rel;
+    return ST_OK;
+}
+
 // SparseOps::dot_product (sparse_ops.cpp:172-187): FP64 inner product on the GPU.
 int st_dot(const double* a, const double* b, int64_t n, int device, double* out) {
     ST_CHECK((a && b) || n == 0, ST_ERR_ARG, "null argument");

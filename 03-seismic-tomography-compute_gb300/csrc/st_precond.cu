@@ -294,6 +294,58 @@ __global__ void __launch_bounds__(256) conv32_wgrad_kernel(const __nv_bfloat16* 
     for (int k = 0; k < 4; ++k) atomicAdd(&dw[((size_t)co * CH + ci0 + k) * NTAP + tap], acc[k]);
 }
 
+// acc[0] += sum r^2, acc[1] += sum dinv (multi-block, FP64 atomics).
+__global__ void pc_sums_kernel(const float* __restrict__ r, const float* __restrict__ dinv, long long n, double* acc) {
+    double a = 0.0, b = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        a += (double)r[i] * (double)r[i];
+        b += (double)dinv[i];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    __shared__ double ra[8], rb[8];
+    if ((threadIdx.x & 31) == 0) {
+        ra[threadIdx.x >> 5] = a;
+        rb[threadIdx.x >> 5] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        a = b = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            a += ra[w];
+            b += rb[w];
+        }
+        atomicAdd(acc, a);
+        atomicAdd(acc + 1, b);
+    }
+}
+
+// s[0] = 1 / rms(r), s[1] = rms(r) * mean(dinv)
+__global__ void pc_finalize_kernel(const double* acc, long long n, float* s) {
+    const double rms = sqrt(acc[0] / (double)n);
+    s[0] = rms > 0.0 ? (float)(1.0 / rms) : 0.0f;
+    s[1] = (float)(rms * (acc[1] / (double)n));
+}
+
+// a = s_in * sqrt(dinv) * r
+__global__ void pc_scale_in_kernel(const float* __restrict__ r, const float* __restrict__ dinv, const float* s,
+                                   long long n, float* __restrict__ a) {
+    const float si = s[0];
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        a[i] = si * sqrtf(dinv[i]) * r[i];
+}
+
+// z = dinv * r + (1 / s_in) * sqrt(dinv) * y
+__global__ void pc_combine_kernel(const float* __restrict__ y, const float* __restrict__ r,
+                                  const float* __restrict__ dinv, const float* s, long long n, float* __restrict__ z) {
+    const float si = s[0];
+    const float inv = si > 0.0f ? 1.0f / si : 0.0f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        z[i] = fmaf(inv * sqrtf(dinv[i]), y[i], dinv[i] * r[i]);
+}
+
 unsigned grid_for(long long n, int cap = 152 * 16) {
     return (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, cap));
 }
@@ -363,6 +415,54 @@ int st_pc_relu_mask(const void* dh, const void* h, void* g, int64_t nx, int64_t 
     return ST_OK;
 }
 
+int st_pc_scales(const float* r, const float* dinv, double* acc, float* scales, int64_t n, void* stream) {
+    ST_CHECK(r && dinv && acc && scales, ST_ERR_ARG, "null argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    ST_CUDA(cudaMemsetAsync(acc, 0, 2 * sizeof(double), st));
+    pc_sums_kernel<<<grid_for(n, 152 * 4), 256, 0, st>>>(r, dinv, n, acc);
+    count_launch();
+    pc_finalize_kernel<<<1, 1, 0, st>>>(acc, n, scales);
+    count_launch();
+    ST_CUDA(cudaGetLastError());
+    return ST_OK;
+}
+
+int st_pc_scale_in(const float* r, const float* dinv, const float* scales, float* a, int64_t n, void* stream) {
+    ST_CHECK(r && dinv && scales && a, ST_ERR_ARG, "null argument");
+    pc_scale_in_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(r, dinv, scales, n, a);
+    count_launch();
+    ST_CUDA(cudaGetLastError());
+    return ST_OK;
+}
+
+int st_pc_combine(const float* y, const float* r, const float* dinv, const float* scales, float* z, int64_t n,
+                  void* stream) {
+    ST_CHECK(y && r && dinv && scales && z, ST_ERR_ARG, "null argument");
+    pc_combine_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(y, r, dinv, scales, n, z);
+    count_launch();
+    ST_CUDA(cudaGetLastError());
+    return ST_OK;
+}
+
+int st_pc_tconv1(const float* a, const float* w, void* h, int64_t nx, int64_t ny, int64_t nz, void* stream) {
+    ST_CHECK(a && w && h, ST_ERR_ARG, "null argument");
+    const Vol v{(int)nx, (int)ny, (int)nz};
+    out_conv_dgrad_kernel<<<grid_for(v.n()), 256, 0, (cudaStream_t)stream>>>(a, w, v, static_cast<__nv_bfloat16*>(h));
+    count_launch();
+    ST_CUDA(cudaGetLastError());
+    return ST_OK;
+}
+
+int st_pc_conv1_wgrad(const float* dz, const void* h, float* dw, int64_t nx, int64_t ny, int64_t nz, void* stream) {
+    ST_CHECK(dz && h && dw, ST_ERR_ARG, "null argument");
+    const Vol v{(int)nx, (int)ny, (int)nz};
+    out_conv_wgrad_kernel<<<dim3(grid_for(v.n(), 64), NTAP), 256, 0, (cudaStream_t)stream>>>(
+        dz, static_cast<const __nv_bfloat16*>(h), v, dw);
+    count_launch();
+    ST_CUDA(cudaGetLastError());
+    return ST_OK;
+}
+
 int st_conv3d_wgrad(const void* x, const void* g, float* dw, int64_t nx, int64_t ny, int64_t nz, void* stream) {
     ST_CHECK(x && g && dw, ST_ERR_ARG, "null argument");
     const Vol v{(int)nx, (int)ny, (int)nz};
@@ -371,6 +471,129 @@ int st_conv3d_wgrad(const void* x, const void* g, float* dw, int64_t nx, int64_t
     count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- network handle
+// The trained preconditioner as one native object (weights packed once,
+// activations allocated once), applied by st_pcnet_apply inside the native
+// flexible CG. It is the symmetric positive (semi)definite form
+//     z = D r + S G^T G S r,   D = diag(dinv), S = sqrt(D),
+//     G = (I + conv_K) ... (I + conv_1) C^T,   C^T: 1 -> 32 channels,
+// so G^T = C (I + conv_1^T) ... (I + conv_K^T): the tensor-core kernel with
+// the transposed packing and the residual added. The input is scaled by
+// 1 / rms(r) and the output back, which keeps z linear in r.
+
+struct st_pcnet {
+    int device = 0;
+    int nx = 0, ny = 0, nz = 0, layers = 0;
+    float* w_c = nullptr;      // C: [32][27]
+    void* packed = nullptr;    // layers x 55,296 bytes (conv_k)
+    void* packed_t = nullptr;  // layers x 55,296 bytes (conv_k^T)
+    void* u = nullptr;         // two padded BF16 volumes (ping-pong)
+    float* a = nullptr;        // scaled input / output, n floats
+    double* acc = nullptr;
+    float* scales = nullptr;
+    size_t vol_bytes = 0;
+};
+
+namespace stg {
+long long pcnet_points(const st_pcnet* p) { return (long long)p->nx * p->ny * p->nz; }
+}  // namespace stg
+
+extern "C" {
+
+int st_pcnet_create(int64_t nx, int64_t ny, int64_t nz, int layers, int device, st_pcnet** out) {
+    ST_CHECK(out && nx > 0 && ny > 0 && nz > 0 && layers >= 0 && layers <= 64, ST_ERR_ARG, "bad network shape");
+    ST_CUDA(cudaSetDevice(device));
+    st_pcnet* p = new st_pcnet();
+    p->device = device;
+    p->nx = (int)nx;
+    p->ny = (int)ny;
+    p->nz = (int)nz;
+    p->layers = layers;
+    p->vol_bytes = (size_t)(nx + 2) * (size_t)(ny + 2) * (size_t)(nz + 2) * CH * 2;
+    const size_t wb = (size_t)std::max(layers, 1) * NTAP * CH * CH * 2;
+    const size_t n = (size_t)(nx * ny * nz);
+    const bool ok = cudaMalloc(&p->w_c, CH * NTAP * 4) == cudaSuccess && cudaMalloc(&p->packed, wb) == cudaSuccess &&
+                    cudaMalloc(&p->packed_t, wb) == cudaSuccess &&
+                    cudaMalloc(&p->u, 2 * p->vol_bytes) == cudaSuccess &&
+                    cudaMalloc(&p->a, n * sizeof(float)) == cudaSuccess &&
+                    cudaMalloc(&p->acc, 2 * sizeof(double)) == cudaSuccess &&
+                    cudaMalloc(&p->scales, 2 * sizeof(float)) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        cudaFree(p->w_c);
+        cudaFree(p->packed);
+        cudaFree(p->packed_t);
+        cudaFree(p->u);
+        cudaFree(p->a);
+        cudaFree(p->acc);
+        cudaFree(p->scales);
+        delete p;
+        set_error("device allocation for the preconditioner network failed");
+        return ST_ERR_ALLOC;
+    }
+    ST_CUDA(cudaMemset(p->u, 0, 2 * p->vol_bytes));
+    ST_CUDA(cudaMemset(p->w_c, 0, CH * NTAP * 4));
+    ST_CUDA(cudaMemset(p->packed, 0, wb));
+    ST_CUDA(cudaMemset(p->packed_t, 0, wb));
+    *out = p;
+    return ST_OK;
+}
+
+int st_pcnet_destroy(st_pcnet* p) {
+    if (!p) return ST_OK;
+    cudaSetDevice(p->device);
+    cudaDeviceSynchronize();
+    cudaFree(p->w_c);
+    cudaFree(p->packed);
+    cudaFree(p->packed_t);
+    cudaFree(p->u);
+    cudaFree(p->a);
+    cudaFree(p->acc);
+    cudaFree(p->scales);
+    delete p;
+    return ST_OK;
+}
+
+// w_c: device FP32 [32][27]; w_k: `layers` consecutive [32][32][27] FP32 blocks.
+int st_pcnet_set_weights(st_pcnet* p, const float* w_c, const float* w_k) {
+    ST_CHECK(p && w_c && (p->layers == 0 || w_k), ST_ERR_ARG, "null argument");
+    ST_CUDA(cudaSetDevice(p->device));
+    ST_CUDA(cudaMemcpy(p->w_c, w_c, CH * NTAP * 4, cudaMemcpyDeviceToDevice));
+    for (int k = 0; k < p->layers; ++k) {
+        const float* w = w_k + (size_t)k * CH * CH * NTAP;
+        const size_t off = (size_t)k * NTAP * CH * CH * 2;
+        ST_TRY(st_conv3d_pack_weights(w, static_cast<char*>(p->packed) + off, 0, nullptr));
+        ST_TRY(st_conv3d_pack_weights(w, static_cast<char*>(p->packed_t) + off, 1, nullptr));
+    }
+    ST_CUDA(cudaDeviceSynchronize());
+    return ST_OK;
+}
+
+int st_pcnet_apply(st_pcnet* p, const float* r, const float* dinv, float* z, void* stream) {
+    ST_CHECK(p && r && dinv && z, ST_ERR_ARG, "null argument");
+    const long long n = (long long)p->nx * p->ny * p->nz;
+    char* u0 = static_cast<char*>(p->u);
+    char* u1 = u0 + p->vol_bytes;
+    ST_TRY(st_pc_scales(r, dinv, p->acc, p->scales, n, stream));
+    ST_TRY(st_pc_scale_in(r, dinv, p->scales, p->a, n, stream));
+    ST_TRY(st_pc_tconv1(p->a, p->w_c, u0, p->nx, p->ny, p->nz, stream));
+    const size_t wsz = (size_t)NTAP * CH * CH * 2;
+    for (int k = 0; k < p->layers; ++k) {  // u <- (I + conv_k) u
+        ST_TRY(st_conv3d_bf16(u0, static_cast<char*>(p->packed) + k * wsz, nullptr, u0, u1, 0, p->nx, p->ny, p->nz, 0,
+                              stream));
+        std::swap(u0, u1);
+    }
+    for (int k = p->layers - 1; k >= 0; --k) {  // u <- (I + conv_k^T) u
+        ST_TRY(st_conv3d_bf16(u0, static_cast<char*>(p->packed_t) + k * wsz, nullptr, u0, u1, 0, p->nx, p->ny,
+                              p->nz, 0, stream));
+        std::swap(u0, u1);
+    }
+    ST_TRY(st_pc_out_conv(u0, p->w_c, nullptr, nullptr, nullptr, p->a, nullptr, p->nx, p->ny, p->nz, stream));
+    return st_pc_combine(p->a, r, dinv, p->scales, z, n, stream);
 }
 
 }  // extern "C"

@@ -112,4 +112,16 @@ int launch_fd_triplets(const double* vel, long long nx, long long ny, long long 
                        double idz2, double dt2, long long* tr, long long* tc, double* tv, cudaStream_t st);
 int run_cg(const CgProblem& P, CgWork& W, int max_iter, double tol, int check_every, CgResult* res, cudaStream_t st);
 
+// Flexible CG on (A^T A + lam I) x = b (st_fcg.cu); pc = the learned network
+// (null: Jacobi with dinv). Work vectors r, z, p, q, ax of A.cols floats, t of
+// A.rows floats, acc two doubles.
+struct FcgScalars {
+    double pq, pr, rr, zr, zq, jq;
+};
+int run_fcg(const DevCsr& A, const DevCsr& AT, double lam, const float* b, float* x, const float* dinv,
+            st_pcnet* pc, int max_iter, double tol, float* r, float* z, float* p, float* q, float* ax, float* t,
+            FcgScalars* sc, double* acc, cudaStream_t st, int* iters, double* true_rel);
+// Unknowns of a preconditioner network (st_precond.cu).
+long long pcnet_points(const st_pcnet* p);
+
 }  // namespace stg

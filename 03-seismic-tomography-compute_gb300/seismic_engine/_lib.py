@@ -143,6 +143,11 @@ SIGNATURES = {
     "st_pc_out_conv_bwd": [_vp, _vp, _vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, _vp],
     "st_pc_relu_mask": [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, _vp],
     "st_conv3d_wgrad": [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, _vp],
+    "st_pc_scales": [_vp, _vp, _vp, _vp, C.c_int64, _vp],
+    "st_pc_scale_in": [_vp, _vp, _vp, _vp, C.c_int64, _vp],
+    "st_pc_combine": [_vp, _vp, _vp, _vp, _vp, C.c_int64, _vp],
+    "st_pc_tconv1": [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, _vp],
+    "st_pc_conv1_wgrad": [_vp, _vp, _vp, C.c_int64, C.c_int64, C.c_int64, _vp],
     # sparse
     "st_csr_create": [C.c_int64, C.c_int64, C.c_int64, C.c_int, C.POINTER(_vp)],
     "st_csr_destroy": [_vp],
@@ -160,6 +165,11 @@ SIGNATURES = {
     "st_csr_spmv_device": [_vp, C.c_int, _vp, _vp],
     "st_csr_frobenius_norm": [_vp, _d],
     "st_csr_normal_jacobi": [_vp, C.c_double, _vp],
+    "st_pcnet_create": [C.c_int64, C.c_int64, C.c_int64, C.c_int, C.c_int, C.POINTER(_vp)],
+    "st_pcnet_destroy": [_vp],
+    "st_pcnet_set_weights": [_vp, _vp, _vp],
+    "st_pcnet_apply": [_vp, _vp, _vp, _vp, _vp],
+    "st_normal_fcg_device": [_vp, _vp, C.c_double, C.c_int, C.c_double, _vp, _vp, C.POINTER(C.c_int), _d],
     "st_csr_scale": [_vp, C.c_double],
     "st_csr_add_diagonal": [_vp, C.c_double],
     "st_csr_clone": [_vp, C.POINTER(_vp)],

@@ -330,6 +330,18 @@ int st_pc_out_conv_bwd(const float* dzhat, const void* h, const float* w_out, vo
                        int64_t ny, int64_t nz, void* stream);
 int st_pc_relu_mask(const void* dh, const void* h, void* g, int64_t nx, int64_t ny, int64_t nz, void* stream);
 int st_conv3d_wgrad(const void* x, const void* g, float* dw, int64_t nx, int64_t ny, int64_t nz, void* stream);
+/* Pieces of the symmetric form z = D r + S G^T G S r (st_pcnet below):
+ *  st_pc_scales      scales = {1 / rms(r), rms(r) mean(dinv)} (acc: 2 doubles of scratch)
+ *  st_pc_scale_in    a = scales[0] * sqrt(dinv) * r
+ *  st_pc_combine     z = dinv * r + sqrt(dinv) * y / scales[0]
+ *  st_pc_tconv1      h = C^T(a): 1 -> 32 channels, h[v][c] = sum_tap w[c][tap] a[v - tap]
+ *  st_pc_conv1_wgrad dw[c][tap] += sum_v dz[v] h[v + tap][c] */
+int st_pc_scales(const float* r, const float* dinv, double* acc, float* scales, int64_t n, void* stream);
+int st_pc_scale_in(const float* r, const float* dinv, const float* scales, float* a, int64_t n, void* stream);
+int st_pc_combine(const float* y, const float* r, const float* dinv, const float* scales, float* z, int64_t n,
+                  void* stream);
+int st_pc_tconv1(const float* a, const float* w, void* h, int64_t nx, int64_t ny, int64_t nz, void* stream);
+int st_pc_conv1_wgrad(const float* dz, const void* h, float* dw, int64_t nx, int64_t ny, int64_t nz, void* stream);
 
 /* ------------------------------------------------ seismic::CSRMatrix face */
 /* Device CSR: int64 row pointers, int32 column indices, FP32 values. Host
@@ -412,6 +424,22 @@ int st_cg_device(st_csr* A, const float* b, float* x, int max_iter, double tol, 
 #define ST_CG_STATIC_MAX_N 1048576
 int st_cg_device_static(st_csr* A, const float* b, float* x, int max_iter, double tol, int jacobi, int* iters,
                         double* final_rel);
+/* Learned preconditioner as a native handle (no reference counterpart):
+ * the symmetric positive (semi)definite z = D r + S G^T G S r, D = diag(dinv),
+ * S = sqrt(D), G = (I + conv_K)...(I + conv_1) C^T with `layers` tensor-core
+ * 32 -> 32 layers (G^T by the transposed packing). Weights are device FP32:
+ * w_c [32][27], w_k `layers` consecutive [32][32][27] blocks, trained by
+ * seismic_engine.precond. */
+typedef struct st_pcnet st_pcnet;
+int st_pcnet_create(int64_t nx, int64_t ny, int64_t nz, int layers, int device, st_pcnet** out);
+int st_pcnet_destroy(st_pcnet* p);
+int st_pcnet_set_weights(st_pcnet* p, const float* w_c, const float* w_k);
+int st_pcnet_apply(st_pcnet* p, const float* r, const float* dinv, float* z, void* stream);
+/* Flexible CG on (A^T A + lam I) x = A^T d (device FP32 d, x) preconditioned
+ * by pc, or by Jacobi when pc is NULL; stops when the true relative residual
+ * (FP64 norms) is <= tol. No reference counterpart. */
+int st_normal_fcg_device(st_csr* A, const float* d, double lam, int max_iter, double tol, st_pcnet* pc, float* x,
+                         int* iters, double* true_rel);
 /* dinv (device FP32, cols) = 1 / (column sums of A^2 + lam): the Jacobi
  * preconditioner of A^T A + lam I (asynchronous on the matrix's stream). */
 int st_csr_normal_jacobi(st_csr* A, double lam, float* dinv);

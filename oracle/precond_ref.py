@@ -1,15 +1,15 @@
 """CPU oracle of the learned CG preconditioner network (TEST INFRASTRUCTURE
 ONLY: the product never imports this file).
 
-Restates in numpy FP64 the network the GPU layers compute
+Restates in numpy FP64 the preconditioner the GPU layers compute
 (seismic_engine/precond.py, csrc/st_precond.cu, csrc/st_conv.cu):
-    h0 = relu(C_in([s r, s dinv r])),  h_k = relu(conv_k(h_{k-1}) + h_{k-1}),
-    zhat = C_out(h_K),  z = dinv r + s_out zhat,
+    z = D r + S G^T G S r,  G = (I + conv_K)...(I + conv_1) C^T,
+D = diag(dinv), S = sqrt(D), input scaled by 1 / rms(r) and output back;
 3x3x3 convolutions with zero padding, tap = (kd*3 + kh)*3 + kw, weights
-[out][in][27]. With bf16=True the BF16 storage of the GPU path is emulated
-(activations, their gradients and the tensor-core layers' weights rounded to
-BF16, round-to-nearest-even), leaving FP32-vs-FP64 accumulation as the only
-difference. The network is new in this project (the reference has no
+[out][in][27]. With bf16_storage the BF16 storage of the GPU path is
+emulated (activations, their gradients and the tensor-core layers' weights
+rounded to BF16, round-to-nearest-even), leaving FP32-vs-FP64 accumulation
+as the only difference. The network is new in this project (the reference has no
 learned preconditioner), so parity here is against this restatement.
 """
 from __future__ import annotations
@@ -65,35 +65,43 @@ def wgrad(x, g):
 
 
 class Net:
-    def __init__(self, w_in, w_k, w_out, bf16_storage=True):
-        self.w_in = np.asarray(w_in, np.float64)
-        self.w_out = np.asarray(w_out, np.float64)
+    """z = D r + S G^T G S r, G = (I + conv_K)...(I + conv_1) C^T (see the
+    module docstring of seismic_engine/precond.py)."""
+
+    def __init__(self, w_c, w_k, bf16_storage=True):
         self.q = bf16 if bf16_storage else (lambda a: np.asarray(a, np.float64))
+        self.w_c = np.asarray(w_c, np.float64)[None]  # (1, 32, 27)
         self.w_k = [self.q(np.asarray(w, np.float64)) for w in w_k]
 
     def forward(self, r, dinv, shape):
-        D, H, W = shape
-        r = np.asarray(r, np.float64).reshape(D, H, W)
-        dinv = np.asarray(dinv, np.float64).reshape(D, H, W)
-        s = 1.0 / np.sqrt(np.mean(np.float32(r) ** 2))
-        x = np.stack([s * r, s * dinv * r])
-        h = [self.q(np.maximum(conv(x, self.w_in), 0.0))]
+        q = self.q
+        r = np.asarray(r, np.float64).reshape(shape)
+        dinv = np.asarray(dinv, np.float64).reshape(shape)
+        s = 1.0 / np.sqrt(np.mean(np.float32(r).astype(np.float64) ** 2))
+        sq = np.sqrt(dinv)
+        a = (s * sq * r)[None]
+        u = [q(conv_t(a, self.w_c))]
         for w in self.w_k:
-            h.append(self.q(np.maximum(conv(h[-1], w) + h[-1], 0.0)))
-        zhat = conv(h[-1], self.w_out[None])[0]
-        self.cache = (x, h)
-        return zhat.reshape(-1)
-
-    def backward(self, dzhat, shape):
-        x, h = self.cache
-        dz = np.asarray(dzhat, np.float64).reshape((1,) + tuple(shape))
-        d_out = wgrad(h[-1], dz)[0]
-        dh = self.q(conv_t(dz, self.w_out[None]))
-        d_k = [None] * len(self.w_k)
+            u.append(q(u[-1] + conv(u[-1], w)))
+        v = [None] * len(self.w_k) + [u[-1]]
         for k in range(len(self.w_k), 0, -1):
-            g = self.q(dh * (h[k] > 0))
-            d_k[k - 1] = wgrad(h[k - 1], g)
-            dh = self.q(conv_t(g, self.w_k[k - 1]) + g)
-        g0 = self.q(dh * (h[0] > 0))
-        d_in = wgrad(x, g0)
-        return d_in, d_k, d_out
+            v[k - 1] = q(v[k] + conv_t(v[k], self.w_k[k - 1]))
+        y = conv(v[0], self.w_c)[0]
+        self.cache = (a, u, v, sq, s)
+        return (dinv * r + sq * y / s).reshape(-1)
+
+    def backward(self, dz, shape):
+        q = self.q
+        a, u, v, sq, s = self.cache
+        dy = (sq * np.asarray(dz, np.float64).reshape(shape) / s)[None]
+        d_c = wgrad(v[0], dy)[0]
+        d = q(conv_t(dy, self.w_c))
+        d_k = [np.zeros_like(w) for w in self.w_k]
+        for k in range(1, len(self.w_k) + 1):
+            d_k[k - 1] += wgrad(d, v[k])
+            d = q(d + conv(d, self.w_k[k - 1]))
+        for k in range(len(self.w_k), 0, -1):
+            d_k[k - 1] += wgrad(u[k - 1], d)
+            d = q(d + conv_t(d, self.w_k[k - 1]))
+        d_c = d_c + wgrad(d, a)[0]
+        return d_c, d_k
