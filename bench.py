@@ -52,7 +52,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU sample time")
+    ap.add_argument("--kernel", choices=["conv", "spmv"], default=None,
+                    help="time one kernel alone (profiling runs) instead of the workload")
     ap.add_argument("--no-tomo", action="store_true", help="skip the tomography CG measurement")
+    ap.add_argument("--tomo-n", type=int, default=100, help="cell grid edge of the --kernel spmv matrix")
+    ap.add_argument("--tomo-rays", type=int, default=2_000_000, help="rays of the --kernel spmv matrix")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner solve")
     return ap.parse_args()
 
@@ -456,8 +460,72 @@ def run_gpu(args):
     return 0
 
 
+def run_kernel(args):
+    """Single-kernel timing for profiling: 'conv' = the tensor-core 3x3x3
+    32 -> 32 convolution on a 100^3 volume; 'spmv' = A x and A^T y of the
+    100^3 / 2M-ray tomography matrix. Prints one JSON line."""
+    import ctypes as C
+    import torch
+    import seismic_engine as se
+    from seismic_engine import _lib
+    L = _lib.load()
+    st = torch.cuda.current_stream()
+    res = {"kernel": args.kernel, "steps": args.steps, "warmup": args.warmup}
+    if args.kernel == "conv":
+        n = 100
+        g = torch.Generator(device="cuda").manual_seed(0)
+        x = torch.zeros((n + 2, n + 2, n + 2, 32), dtype=torch.bfloat16, device="cuda")
+        x[1:-1, 1:-1, 1:-1] = torch.randn((n, n, n, 32), device="cuda", generator=g).to(torch.bfloat16)
+        y = torch.zeros_like(x)
+        w = torch.randn((32, 32, 3, 3, 3), device="cuda", generator=g) / 30
+        wp = torch.empty(27 * 32 * 32, dtype=torch.bfloat16, device="cuda")
+        L.st_conv3d_pack_weights(C.c_void_p(w.data_ptr()), C.c_void_p(wp.data_ptr()), 0, C.c_void_p(st.cuda_stream))
+
+        def one():
+            rc = L.st_conv3d_bf16(C.c_void_p(x.data_ptr()), C.c_void_p(wp.data_ptr()), None, C.c_void_p(x.data_ptr()),
+                                  C.c_void_p(y.data_ptr()), 0, n, n, n, 0, C.c_void_p(st.cuda_stream))
+            assert rc == 0
+        flops = 2.0 * n ** 3 * 32 * 32 * 27
+        res.update({"workload": f"3x3x3 conv, 32 -> 32 channels, BF16 operands, {n}^3 voxels", "flops": flops})
+    else:
+        nt_, nr_ = args.tomo_n, args.tomo_rays
+        A = se.CSRMatrix()
+        nnz = A.build_ray_matrix(torch.from_numpy(se.workloads.ray_endpoints(nr_, nt_, 4)).cuda(), nt_, nt_, nt_)
+        xv = torch.randn(A.cols(), device="cuda")
+        yv = torch.zeros(A.rows(), device="cuda")
+        zv = torch.zeros(A.cols(), device="cuda")
+
+        def one():
+            A.spmv_device(xv, yv)
+            A.spmv_device(yv, zv, transpose=True)
+        res.update({"workload": f"A x and A^T y, {A.rows()} x {A.cols()}, nnz {nnz}",
+                    "alg_bytes": 2 * nnz * 8 + (A.rows() + A.cols()) * 16})
+        st = torch.cuda.ExternalStream(A.stream_ptr())  # the SpMV kernels run on the matrix's stream
+    for _ in range(args.warmup):
+        one()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(args.steps):
+        one()
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    res["ms"] = ms
+    if "flops" in res:
+        res["tflops"] = res["flops"] / ms / 1e9
+    if "alg_bytes" in res:
+        res["gbs"] = res["alg_bytes"] / ms / 1e6
+    if args.kernel == "conv":
+        assert L.st_conv3d_check(C.c_void_p(st.cuda_stream)) == 0
+    print(json.dumps(res), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.kernel:
+        return run_kernel(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)
