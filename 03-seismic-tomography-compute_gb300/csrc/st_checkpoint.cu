@@ -83,6 +83,8 @@ struct CkptRun {
     float* illum = nullptr;
     float* grad_c = nullptr;
     CUtensorMap msnap;
+    ImageMaps imaps;
+    bool staged = false;
     std::function<int()> before_backward;
     bool started = false;
     st_checkpoint_stats stats{};
@@ -237,9 +239,10 @@ int backward(CkptRun& c, int j) {
         a.amax_in = c.amax_seg + (t - t0);
         if (c.epi == 1) {
             a.snap_in = c.segbuf + (size_t)(t - t0) * per;
+            a.snap_t = t - t0;
             a.image = c.image;
             a.illum = c.illum;
-            ST_TRY(fused_step(s, a, SNAP_NONE, c.kind, 1, nullptr));
+            ST_TRY(fused_step(s, a, SNAP_NONE, c.kind, 1, nullptr, c.staged ? &c.imaps : nullptr));
         } else {
             a.snap_t = t - t0;
             a.grad = c.grad_c;
@@ -329,6 +332,8 @@ int checkpointed_adjoint(st_solver* s, const st_shot* shot, int snap_kind, int s
     c.amax_seg = reinterpret_cast<unsigned*>(c.segbuf + sbytes);
     for (int k = 0; k < 3; ++k) ST_TRY(build_field_maps(&c.gm[k], c.g[k], L));
     if (epi == 2) ST_TRY(build_snap_map_grad(&c.msnap, c.segbuf, snap_kind, L, c.seg));
+    c.staged = epi == 1 && image_maps_supported(snap_kind, L);
+    if (c.staged) ST_TRY(build_image_maps(&c.imaps, c.segbuf, snap_kind, c.seg, image, illum, L));
     c.slot_of.assign((size_t)c.nseg, -1);
     for (int k = c.nslots - 1; k >= 0; --k) c.free_slots.push_back(k);
 

@@ -64,10 +64,23 @@ int build_field_maps(FieldMaps* m, const float* base, const Layout& L);
 // least min_waves waves of resident CTAs when the grid allows it.
 int fd_step_grid_chunks(const Layout& L, int tyv, int minb, int min_waves);
 
+// Maps of the staged imaging variant: the snapshot store (box {64, 16} at
+// (z, y, x, t)) and the compact image / illumination volumes (box {64, 16}).
+struct ImageMaps {
+    CUtensorMap snap, image, illum;
+};
+bool image_maps_supported(int kind, const Layout& L);
+int build_image_maps(ImageMaps* m, const void* snaps, int kind, long long nt, const float* image,
+                     const float* illum, const Layout& L);
+int make_compact_map(CUtensorMap* map, const float* base, const Layout& L, int bz, int by);
+
 // Launch one fused step. snap_out / snap_in are SnapKind values; epi: 0 = none,
-// 1 = imaging, 2 = gradient (needs msnap, the snapshot store's map).
+// 1 = imaging (operands staged by TMA when imaps is given, StepArgs::snap_t
+// then indexes the store; loaded at use from snap_in otherwise), 2 = gradient
+// (needs msnap, the snapshot store's map).
 int launch_fd_step(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
-                   StepArgs a, int snap_out, int snap_in, int epi, const CUtensorMap* msnap, cudaStream_t st);
+                   StepArgs a, int snap_out, int snap_in, int epi, const CUtensorMap* msnap, cudaStream_t st,
+                   const ImageMaps* imaps = nullptr);
 // 4-D map over a snapshot store for the gradient step's halo tile.
 int build_snap_map_grad(CUtensorMap* m, const void* base, int kind, const Layout& L, long long nt);
 

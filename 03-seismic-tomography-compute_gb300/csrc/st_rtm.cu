@@ -147,6 +147,10 @@ int rtm_backward_impl(st_solver* s, const st_shot* shot, const float* data, int 
     const size_t npts = (size_t)(L.nx * L.ny * L.nz);
     const size_t per = npts * (size_t)snap_bytes(snap_kind);
     const bool imaging = snaps != nullptr;
+    // the imaging operands ride the TMA ring when the store's rows allow it
+    ImageMaps imaps;
+    const bool staged = imaging && image_maps_supported(snap_kind, L);
+    if (staged) ST_TRY(build_image_maps(&imaps, snaps, snap_kind, std::max(nt, 1), image, illum, L));
     ST_TRY(zero_fields(s));
     if (imaging) {
         ST_CUDA(cudaMemsetAsync(image, 0, npts * sizeof(float), s->stream));
@@ -166,11 +170,13 @@ int rtm_backward_impl(st_solver* s, const st_shot* shot, const float* data, int 
         }
         if (imaging) {
             a.snap_in = static_cast<const char*>(snaps) + (size_t)t * per;
+            a.snap_t = t;
             a.amax_in = amax + t;
             a.image = image;
             a.illum = illum;
         }
-        ST_TRY(fused_step(s, a, SNAP_NONE, imaging ? snap_kind : SNAP_NONE, imaging ? 1 : 0, nullptr));
+        ST_TRY(fused_step(s, a, SNAP_NONE, imaging ? snap_kind : SNAP_NONE, imaging ? 1 : 0, nullptr,
+                          staged ? &imaps : nullptr));
         if (src_trace) {
             probe_kernel<<<1, 1, 0, s->stream>>>(s->f[s->ic], s->c, L, shot->src_ix, shot->src_iy, shot->src_iz,
                                                  a.force_row, q_src, s->dtab, s->sw, s->sponge_mode, src_trace + t);

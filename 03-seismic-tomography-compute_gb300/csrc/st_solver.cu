@@ -209,10 +209,11 @@ StepArgs base_args(st_solver* s, float* out) {
 
 // One fused step out = f[in] from cur = f[ic], prev = f[ip]; then rotates the
 // roles so cur = out, prev = old cur, third = old prev.
-int fused_step(st_solver* s, StepArgs a, int snap_out, int snap_in, int epi, const CUtensorMap* msnap) {
+int fused_step(st_solver* s, StepArgs a, int snap_out, int snap_in, int epi, const CUtensorMap* msnap,
+               const ImageMaps* imaps) {
     a.out = s->f[s->in];
     ST_TRY(launch_fd_step(s->L, s->maps[s->ic], s->maps[s->ip], s->map_c, a, snap_out, snap_in, epi, msnap,
-                          s->stream));
+                          s->stream, imaps));
     const int old_c = s->ic, old_p = s->ip, old_n = s->in;
     s->ic = old_n;
     s->ip = old_c;

@@ -101,7 +101,8 @@ int refresh_coeff(st_solver* s);
 int read_flags(st_solver* s, unsigned* out);
 StepArgs base_args(st_solver* s, float* out);
 // epi: 0 none, 1 imaging, 2 gradient (msnap = the snapshot store's map)
-int fused_step(st_solver* s, StepArgs a, int snap_out, int snap_in, int epi, const CUtensorMap* msnap);
+int fused_step(st_solver* s, StepArgs a, int snap_out, int snap_in, int epi, const CUtensorMap* msnap,
+               const ImageMaps* imaps = nullptr);
 int zero_fields(st_solver* s);
 long long dev_index(const st_solver* s, int64_t ix, int64_t iy, int64_t iz);
 bool finite_sample(const double* w, int64_t len, int64_t t, float* out);

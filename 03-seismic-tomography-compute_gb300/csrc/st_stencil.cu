@@ -60,7 +60,10 @@ constexpr int EXTRA_BYTES = 128 + DTAB_MAX * 4;
 constexpr int SM_SMEM = 232448;               // shared memory per SM (227 KB usable per CTA)
 constexpr unsigned FULL = 0xffffffffu;
 
-enum Epilogue : int { EPI_NONE = 0, EPI_IMAGE = 1, EPI_GRAD = 2 };
+// EPI_IMAGE_T: imaging with its operands (snapshot, image, illumination tiles)
+// staged through the TMA ring instead of loaded at use.
+enum Epilogue : int { EPI_NONE = 0, EPI_IMAGE = 1, EPI_GRAD = 2, EPI_IMAGE_T = 3 };
+constexpr bool is_image(int e) { return e == EPI_IMAGE || e == EPI_IMAGE_T; }
 
 // Per-variant tiling. Forward variants give each thread 2 adjacent rows
 // (32-row tiles, 2 CTAs per SM): fewer instructions per point. The imaging
@@ -68,6 +71,8 @@ enum Epilogue : int { EPI_NONE = 0, EPI_IMAGE = 1, EPI_GRAD = 2 };
 // directly, give each thread 1 row (16-row tiles) so more warps per SM hide
 // those accesses. The gradient variant also stages the forward snapshot tile
 // with its halo (box starting 16 bytes left of the tile), in a 3-deep ring.
+// The staged imaging variant adds the snapshot, image and illumination tiles
+// of each plane to the stage (3-deep ring).
 template <int EPI, int SNAP_IN>
 struct Geo {
     static constexpr int RPT = EPI == EPI_NONE ? 2 : 1;  // rows per thread
@@ -76,14 +81,16 @@ struct Geo {
     static constexpr int CUR_BYTES = CUR_W * CUR_H * 4;
     static constexpr int CUR_BYTES_PAD = ((CUR_BYTES + 127) / 128) * 128;
     static constexpr int CTR_BYTES = TZ * TYV * 4;
-    static constexpr int STAGES = EPI == EPI_GRAD ? 3 : 4;
-    static constexpr int SES = EPI == EPI_GRAD ? snap_bytes(SNAP_IN) : 0;
-    static constexpr int SW = EPI == EPI_GRAD ? (SES == 2 ? TZ + 16 : TZ + 8) : 0;
+    static constexpr int STAGES = (EPI == EPI_GRAD || EPI == EPI_IMAGE_T) ? 3 : 4;
+    static constexpr int SES = (EPI == EPI_GRAD || EPI == EPI_IMAGE_T) ? snap_bytes(SNAP_IN) : 0;
+    static constexpr int SW = EPI == EPI_GRAD ? (SES == 2 ? TZ + 16 : TZ + 8) : (EPI == EPI_IMAGE_T ? TZ : 0);
     static constexpr int SOFF = EPI == EPI_GRAD ? (SES == 2 ? 8 : 4) : 0;
-    static constexpr int SNAP_TILE = SW * CUR_H * SES;
+    static constexpr int SNAP_H = EPI == EPI_GRAD ? CUR_H : TYV;
+    static constexpr int SNAP_TILE = SW * SNAP_H * SES;
     static constexpr int SNAP_TILE_PAD = ((SNAP_TILE + 127) / 128) * 128;
-    static constexpr int STAGE_BYTES = CUR_BYTES_PAD + 2 * CTR_BYTES + SNAP_TILE_PAD;
-    static constexpr int STAGE_TX = CUR_BYTES + 2 * CTR_BYTES + SNAP_TILE;
+    static constexpr int ACC_BYTES = EPI == EPI_IMAGE_T ? 2 * CTR_BYTES : 0;  // image + illumination tiles
+    static constexpr int STAGE_BYTES = CUR_BYTES_PAD + 2 * CTR_BYTES + SNAP_TILE_PAD + ACC_BYTES;
+    static constexpr int STAGE_TX = CUR_BYTES + 2 * CTR_BYTES + SNAP_TILE + ACC_BYTES;
     static constexpr int SMEM = STAGES * STAGE_BYTES + EXTRA_BYTES;
     static constexpr int FIT = SM_SMEM / (SMEM + 1024);
     static constexpr int MINB = FIT < 4 ? FIT : 4;       // resident CTAs per SM
@@ -295,7 +302,7 @@ __device__ __forceinline__ void process_row(const StepArgs& a, const RowCtx& R, 
         for (int k = 0; k < 4; ++k)
             if (k < zvalid) amax = fmaxf(amax, fabsf(res[k]));
     }
-    if constexpr (EPI == EPI_IMAGE) {
+    if constexpr (is_image(EPI)) {
         if (vec_acc) {
             float im[4], il[4];
             f4_to(acc0, im);
@@ -340,6 +347,7 @@ template <int SNAP_OUT, int SNAP_IN, int EPI>
 __global__ void __launch_bounds__(NTHREADS, (Geo<EPI, SNAP_IN>::MINB))
     fd_step_kernel(const __grid_constant__ CUtensorMap map_cur, const __grid_constant__ CUtensorMap map_prev,
                    const __grid_constant__ CUtensorMap map_c, const __grid_constant__ CUtensorMap map_snap,
+                   const __grid_constant__ CUtensorMap map_img, const __grid_constant__ CUtensorMap map_ill,
                    const StepArgs a) {
     using G = Geo<EPI, SNAP_IN>;
     constexpr int STAGES = G::STAGES;
@@ -412,6 +420,11 @@ __global__ void __launch_bounds__(NTHREADS, (Geo<EPI, SNAP_IN>::MINB))
         return reinterpret_cast<const unsigned char*>(smem + s * G::STAGE_BYTES + G::CUR_BYTES_PAD +
                                                       2 * G::CTR_BYTES);
     };
+    auto img_tile = [&](int s) {
+        return reinterpret_cast<float*>(smem + s * G::STAGE_BYTES + G::CUR_BYTES_PAD + 2 * G::CTR_BYTES +
+                                        G::SNAP_TILE_PAD);
+    };
+    auto ill_tile = [&](int s) { return img_tile(s) + TZ * TYV; };
 
     if (tid == 0) {
         for (int s = 0; s < STAGES; ++s) mbar_init(&bar[s], 1);
@@ -430,6 +443,12 @@ __global__ void __launch_bounds__(NTHREADS, (Geo<EPI, SNAP_IN>::MINB))
         if constexpr (EPI == EPI_GRAD)
             tma_load_4d(const_cast<unsigned char*>(snap_tile(s)), &map_snap, &bar[s], z0 - G::SOFF, y0 - 1, xd - 1,
                         a.snap_t);
+        if constexpr (EPI == EPI_IMAGE_T) {
+            // compact interior tiles of interior plane xd - 1 (zero outside the domain)
+            tma_load_4d(const_cast<unsigned char*>(snap_tile(s)), &map_snap, &bar[s], z0, y0, xd - 1, a.snap_t);
+            tma_load_3d(img_tile(s), &map_img, &bar[s], z0, y0, xd - 1);
+            tma_load_3d(ill_tile(s), &map_ill, &bar[s], z0, y0, xd - 1);
+        }
     };
     int issued = 0;
     if (tid == 0) {
@@ -457,7 +476,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo<EPI, SNAP_IN>::MINB))
     // its single accumulator.
     constexpr bool kPrefetch = EPI == EPI_GRAD;
     auto prefetch = [&](int x) {
-        if constexpr (EPI != EPI_NONE) {
+        if constexpr (EPI == EPI_IMAGE || EPI == EPI_GRAD) {
             if (!vec_acc || x >= xb) return;
             const long long ca = ((long long)x * a.ny + RA.iy) * a.nz + iz0;
             const long long cb = ca + a.nz;
@@ -534,6 +553,14 @@ __global__ void __launch_bounds__(NTHREADS, (Geo<EPI, SNAP_IN>::MINB))
             const long long cbA = ((long long)x * a.ny + RA.iy) * a.nz + iz0;
             float finA[4] = {0, 0, 0, 0}, finB[4] = {0, 0, 0, 0};
             if constexpr (!kPrefetch) prefetch(x);  // operands of this plane, at use
+            if constexpr (EPI == EPI_IMAGE_T) {
+                // operands staged with the plane's tiles
+                snap_smem4<SNAP_IN>(snap_tile(sp), ctrA, finA);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) finA[k] *= snap_scale;
+                a0A = *reinterpret_cast<const float4*>(img_tile(sp) + ctrA);
+                a1A = *reinterpret_cast<const float4*>(ill_tile(sp) + ctrA);
+            }
             if constexpr (EPI == EPI_IMAGE) {
                 snap_unpack4<SNAP_IN>(snA, finA);
                 if constexpr (RPT == 2) snap_unpack4<SNAP_IN>(snB, finB);
@@ -618,7 +645,8 @@ __global__ void __launch_bounds__(NTHREADS, (Geo<EPI, SNAP_IN>::MINB))
 
 template <int SO, int SI, int EPI>
 int launch_variant(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
-                   const CUtensorMap& msnap, StepArgs a, cudaStream_t st) {
+                   const CUtensorMap& msnap, StepArgs a, cudaStream_t st, const CUtensorMap* mimg = nullptr,
+                   const CUtensorMap* mill = nullptr) {
     using G = Geo<EPI, SI>;
     constexpr int SMEM = G::SMEM;
     constexpr int ti = G::RPT == 2 ? 1 : 0;  // which tile height the maps were built for
@@ -639,7 +667,10 @@ int launch_variant(const Layout& L, const FieldMaps& mcur, const FieldMaps& mpre
     a.x_chunk = (int)((L.nx + chunks - 1) / chunks);
     const int nch = (int)((L.nx + a.x_chunk - 1) / a.x_chunk);
     dim3 grid((unsigned)((L.nz + TZ - 1) / TZ), (unsigned)((L.ny + G::TYV - 1) / G::TYV), (unsigned)nch);
-    fd_step_kernel<SO, SI, EPI><<<grid, NTHREADS, SMEM, st>>>(mcur.cur[ti], mprev.ctr[ti], mc.ctr[ti], msnap, a);
+    const CUtensorMap& mi = mimg ? *mimg : msnap;  // unused unless EPI == EPI_IMAGE_T
+    const CUtensorMap& ml = mill ? *mill : msnap;
+    fd_step_kernel<SO, SI, EPI><<<grid, NTHREADS, SMEM, st>>>(mcur.cur[ti], mprev.ctr[ti], mc.ctr[ti], msnap, mi, ml,
+                                                             a);
     ::stg::count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
@@ -857,7 +888,8 @@ int fd_step_grid_chunks(const Layout& L, int tyv, int minb, int min_waves) {
 }
 
 int launch_fd_step(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
-                   StepArgs a, int snap_out, int snap_in, int epi, const CUtensorMap* msnap, cudaStream_t st) {
+                   StepArgs a, int snap_out, int snap_in, int epi, const CUtensorMap* msnap, cudaStream_t st,
+                   const ImageMaps* imaps) {
     a.nx = (int)L.nx;
     a.ny = (int)L.ny;
     a.nz = (int)L.nz;
@@ -865,6 +897,22 @@ int launch_fd_step(const Layout& L, const FieldMaps& mcur, const FieldMaps& mpre
     a.plane = L.plane;
     if (a.timeout_ns == 0) a.timeout_ns = 2000000000ull;
     const CUtensorMap& ms = msnap ? *msnap : mc.ctr[0];  // unused unless epi == gradient
+    if (epi == EPI_IMAGE && imaps) {
+        // operands staged by TMA: snapshot store map (box {64, 16}), image and illumination maps
+        ST_CHECK(snap_out == SNAP_NONE, ST_ERR_ARG, "imaging step cannot also store snapshots");
+        switch (snap_in) {
+            case SNAP_BF16:
+                return launch_variant<SNAP_NONE, SNAP_BF16, EPI_IMAGE_T>(L, mcur, mprev, mc, imaps->snap, a, st,
+                                                                         &imaps->image, &imaps->illum);
+            case SNAP_FP16:
+                return launch_variant<SNAP_NONE, SNAP_FP16, EPI_IMAGE_T>(L, mcur, mprev, mc, imaps->snap, a, st,
+                                                                         &imaps->image, &imaps->illum);
+            case SNAP_FP32:
+                return launch_variant<SNAP_NONE, SNAP_FP32, EPI_IMAGE_T>(L, mcur, mprev, mc, imaps->snap, a, st,
+                                                                         &imaps->image, &imaps->illum);
+            default: ST_CHECK(false, ST_ERR_ARG, "imaging step needs a snapshot kind");
+        }
+    }
     if (epi == EPI_IMAGE) {
         ST_CHECK(snap_out == SNAP_NONE, ST_ERR_ARG, "imaging step cannot also store snapshots");
         switch (snap_in) {
@@ -890,6 +938,38 @@ int launch_fd_step(const Layout& L, const FieldMaps& mcur, const FieldMaps& mpre
         case SNAP_FP32: return launch_variant<SNAP_FP32, SNAP_NONE, EPI_NONE>(L, mcur, mprev, mc, ms, a, st);
         default: ST_CHECK(false, ST_ERR_ARG, "bad snapshot kind %d", snap_out);
     }
+}
+
+int build_image_maps(ImageMaps* m, const void* snaps, int kind, long long nt, const float* image,
+                     const float* illum, const Layout& L) {
+    ST_CHECK(image_maps_supported(kind, L), ST_ERR_UNSUPPORTED, "staged imaging needs nz * %d bytes divisible by 16",
+             snap_bytes(kind));
+    ST_TRY(make_snap_map(&m->snap, snaps, kind, L, nt, TZ, 16));
+    ST_TRY(make_compact_map(&m->image, image, L, TZ, 16));
+    ST_TRY(make_compact_map(&m->illum, illum, L, TZ, 16));
+    return ST_OK;
+}
+
+bool image_maps_supported(int kind, const Layout& L) {
+    const int es = snap_bytes(kind);
+    return es > 0 && (L.nz * es) % 16 == 0 && (L.nz % 4) == 0;
+}
+
+// 3-D map over a compact interior FP32 volume [nx][ny][nz], box {bz, by, 1}.
+int make_compact_map(CUtensorMap* map, const float* base, const Layout& L, int bz, int by) {
+    EncodeTiledFn enc = nullptr;
+    ST_TRY(get_encode_tiled(&enc));
+    ST_CHECK((reinterpret_cast<uintptr_t>(base) & 15) == 0, ST_ERR_ARG, "volume base not 16-byte aligned");
+    ST_CHECK((L.nz * 4) % 16 == 0, ST_ERR_ARG, "compact volume rows must be multiples of 16 bytes");
+    cuuint64_t dims[3] = {(cuuint64_t)L.nz, (cuuint64_t)L.ny, (cuuint64_t)L.nx};
+    cuuint64_t strides[2] = {(cuuint64_t)L.nz * 4, (cuuint64_t)(L.ny * L.nz) * 4};
+    cuuint32_t box[3] = {(cuuint32_t)bz, (cuuint32_t)by, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    ST_CHECK(r == CUDA_SUCCESS, ST_ERR_CUDA, "cuTensorMapEncodeTiled (compact volume) failed (%d)", (int)r);
+    return ST_OK;
 }
 
 int build_snap_map_grad(CUtensorMap* m, const void* base, int kind, const Layout& L, long long nt) {

@@ -93,9 +93,12 @@ def rtm_case(se, oracle, n=(28, 24, 32), nt=90):
     return w, shot, g, mig_ref, d_obs.astype(np.float32)
 
 
-def test_rtm_image_matches_oracle(se, oracle):
+@pytest.mark.parametrize("n", [(28, 24, 32), (27, 23, 30)])
+def test_rtm_image_matches_oracle(se, oracle, n):
+    """nz = 32: imaging operands staged through the TMA ring; nz = 30 (rows
+    not a multiple of 16 bytes for 16-bit snapshots): loaded at use."""
     import torch
-    w, shot, g, mig_ref, d_obs = rtm_case(se, oracle)
+    w, shot, g, mig_ref, d_obs = rtm_case(se, oracle, n=n)
     fwd = oracle.run(g, mig_ref, w.nt, np.array([shot.src]), shot.wavelet[:, None], shot.rec.coords(),
                      keep_states=True)
     ref = oracle.adjoint(g, mig_ref, w.nt, shot.rec.coords(), d_obs.astype(np.float64), states=fwd["states"],
