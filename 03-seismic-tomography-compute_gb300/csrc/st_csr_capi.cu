@@ -397,7 +397,7 @@ int st_cg(st_csr* m, const double* b, int64_t nb, int max_iter, double tol, int 
 // Damped normal equations (A^T A + lam I) x = A^T d of a rectangular A.
 int st_normal_cg_device(st_csr* m, const float* d, double lam, int max_iter, double tol, int jacobi, float* x,
                         float* rhs, int* iters, double* final_rel, double* true_rel) {
-    ST_CHECK(m && d && x, ST_ERR_ARG, "null argument");
+    ST_CHECK(m && x && (d || rhs), ST_ERR_ARG, "null argument");
     ST_CUDA(cudaSetDevice(m->device));
     ST_TRY(ensure_transpose(m));
     const long long n = m->A.cols, rows = m->A.rows;
@@ -412,7 +412,7 @@ int st_normal_cg_device(st_csr* m, const float* d, double lam, int max_iter, dou
     float* b = rhs ? rhs : sc.get<float>((size_t)n);
     float* dinv = jacobi ? sc.get<float>((size_t)n) : nullptr;
     ST_ALLOC(W.r && W.z && W.p && W.q && W.t && W.sc && b && (!jacobi || dinv));
-    ST_TRY(launch_spmv(m->AT, d, b, nullptr, 0.0f, nullptr, nullptr, nullptr, m->stream));
+    if (d) ST_TRY(launch_spmv(m->AT, d, b, nullptr, 0.0f, nullptr, nullptr, nullptr, m->stream));
     if (jacobi) ST_TRY(launch_normal_jacobi(m->AT, lam, dinv, m->stream));
     CgProblem P;
     P.A = &m->A;

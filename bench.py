@@ -52,6 +52,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU sample time")
+    ap.add_argument("--workload", choices=["rtm", "large"], default="rtm",
+                    help="large: one 512^3, 8-shot adjoint tomography iteration (not the headline line)")
+    ap.add_argument("--segment", type=int, default=200, help="checkpoint segment length of --workload large")
+    ap.add_argument("--compare", action="store_true",
+                    help="--workload large: also time FP32 segment snapshots and unpreconditioned CG")
     ap.add_argument("--kernel", choices=["conv", "spmv"], default=None,
                     help="time one kernel alone (profiling runs) instead of the workload")
     ap.add_argument("--no-tomo", action="store_true", help="skip the tomography CG measurement")
@@ -522,10 +527,95 @@ def run_kernel(args):
     return 0
 
 
+def laplacian_csr(n, mu=1.0):
+    """sqrt(mu) L for the 7-point Laplacian L on an n^3 grid (Dirichlet), built
+    by the FD-stencil builder with v dt / d = 1 (off-diagonals 1, diagonal
+    2 - 6) and a diagonal shift of -2."""
+    import seismic_engine as se
+    A = se.CSRMatrix()
+    A.build_fd_stencil_7point(n, n, n, np.full(n ** 3, 1.0), 1.0, 1.0, 1.0, 1.0)
+    A.add_diagonal(-2.0)
+    if mu != 1.0:
+        A.scale(float(np.sqrt(mu)))
+    return A
+
+
+def run_large(args):
+    """One adjoint tomography iteration on the 512^3 workload: 8 shots one
+    after another, each forward + checkpointed adjoint gradient (BF16 segment
+    snapshots), the summed velocity gradient restricted to a 256^3 inversion
+    grid (2x2x2 means) and a Jacobi-PCG model update (I + mu L^T L) x = g,
+    L the 7-point Laplacian (mu = 1). Prints one JSON line."""
+    import torch
+    import seismic_engine as se
+    import seismic_engine.fwi as fwi
+    nt = args.nt if args.nt != 2000 else 4000
+    w = se.workloads.large_512(nt=nt)
+    n = w.nx
+    cfg = se.SolverConfig(dt=w.dt, nt=nt, sponge_width=w.sponge_width, sponge_damping=w.sponge_damping,
+                          sponge_mode=w.sponge_mode)
+    s = se.WaveEquationSolver(se.GridParams(n, n, n, w.d, w.d, w.d), cfg)
+    v_true = torch.from_numpy(w.vel.astype(np.float32)).cuda()
+    v0 = torch.from_numpy(se.workloads.smooth(w.vel, 6.0).astype(np.float32)).cuda()
+    fwi.set_velocity_device(s, v_true)
+    d_obs = []
+    for sh in w.shots:  # observed data (input preparation, untimed)
+        d = torch.zeros((nt, sh.rec.count), device="cuda")
+        se.shot_forward(s, sh.src, sh.wavelet, nt, sh.rec, seis=d)
+        d_obs.append(d)
+    torch.cuda.synchronize()
+    fwi.set_velocity_device(s, v0)
+    L = laplacian_csr(n // 2)
+    slots = -(-nt // args.segment)
+
+    def iteration(kind, jacobi):
+        g = torch.zeros(w.points, device="cuda")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        misfit = 0.0
+        for sh, d in zip(w.shots, d_obs):
+            misfit += fwi.fwi_gradient(s, sh.src, sh.wavelet, nt, sh.rec, d, g, snap_kind=kind,
+                                       checkpoint=(args.segment, slots))
+        torch.cuda.synchronize()
+        t_grad = time.perf_counter() - t0
+        gr = torch.nn.functional.avg_pool3d(g.reshape(1, 1, n, n, n), 2).reshape(-1).contiguous()
+        x = torch.zeros_like(gr)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        it, rel, true_rel = se.normal_cg_device(L, None, 1.0, x, 5000, 1e-6, jacobi, rhs=gr.clone())
+        torch.cuda.synchronize()
+        t_cg = time.perf_counter() - t1
+        return {"seconds": t_grad + t_cg, "gradient_s": t_grad, "cg_s": t_cg, "cg_iterations": it,
+                "cg_true_rel": true_rel, "misfit": misfit}
+
+    res = iteration(_snap("bf16"), True)
+    # forward sweep + recompute + adjoint steps of every shot
+    pts = float(w.points) * nt * 3 * len(w.shots)
+    line = {"metric": "adjoint tomography iteration", "value": res["seconds"], "unit": "s",
+            "higher_is_better": False, "n_gpus": 1, "dtype": "f32",
+            "config": {"workload": f"{w.name} x {nt} steps, {len(w.shots)} shots, 256x256 receivers, "
+                                   f"checkpointed adjoint (segments of {args.segment}, BF16 snapshots), "
+                                   f"PCG (I + L^T L) update on a {n // 2}^3 grid"},
+           "gpts_per_s": pts / res["gradient_s"] / 1e9, "bf16_checkpointed_pcg": res}
+    if args.compare:
+        line["fp32_checkpointed"] = iteration(_snap("fp32"), True)
+        line["plain_cg"] = iteration(_snap("bf16"), False)
+    print(json.dumps(line), flush=True)
+    s.close()
+    return 0
+
+
+def _snap(name):
+    from seismic_engine import _lib
+    return {"bf16": _lib.ST_SNAP_BF16, "fp16": _lib.ST_SNAP_FP16, "fp32": _lib.ST_SNAP_FP32}[name]
+
+
 def main():
     args = parse()
     if args.kernel:
         return run_kernel(args)
+    if args.workload == "large":
+        return run_large(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

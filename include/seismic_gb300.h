@@ -445,8 +445,10 @@ int st_normal_fcg_device(st_csr* A, const float* d, double lam, int max_iter, do
 int st_csr_normal_jacobi(st_csr* A, double lam, float* dinv);
 /* Tomography solve: (A^T A + lam I) x = A^T d for a rectangular A (no
  * reference counterpart), Jacobi diagonal = column sums of A^2 + lam when
- * jacobi != 0. rhs (may be NULL) receives A^T d; true_rel (may be NULL) the
- * FP64 relative true residual ||A^T d - (A^T A + lam I) x|| / ||A^T d||. */
+ * jacobi != 0. rhs (may be NULL) receives A^T d; with d == NULL, rhs is the
+ * given right-hand side instead (e.g. a gradient for the regularised update
+ * (I + mu L^T L) x = g with A = sqrt(mu) L, lam = 1). true_rel (may be NULL)
+ * receives the FP64 relative true residual ||rhs - (A^T A + lam I) x|| / ||rhs||. */
 int st_normal_cg_device(st_csr* A, const float* d, double lam, int max_iter, double tol, int jacobi, float* x,
                         float* rhs, int* iters, double* final_rel, double* true_rel);
 /* Replaces dot_product (sparse_ops.cpp:172-187): FP64 inner product. */

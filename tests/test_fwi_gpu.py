@@ -118,3 +118,35 @@ def test_autograd_function_matches_entry_point(se):
         m += se.fwi.fwi_gradient(s, sh.src, sh.wavelet, w.nt, sh.rec, d_obs[i].contiguous(), g, snap_kind=3)
     assert abs(float(loss.detach()) - m) <= 1e-6 * m
     assert rel(vv.grad.reshape(-1).cpu().numpy(), g.cpu().numpy()) < 1e-5
+
+
+def test_exact_gradient_vs_reference_pointwise_formula(se):
+    """The reference's adjoint-state gradient (seismic_tomography/gradient.py:
+    24-40) is the pointwise g = -u * lambda * 2 v dt^2; summed over time that is
+    -2 v dt^2 times the zero-lag image of the forward and adjoint fields. The
+    exact discrete gradient correlates lambda with L u instead of u (L u ~ -k^2
+    u for band-limited waves), so the two agree in direction but not exactly:
+    their cosine similarity is stated and required to be clearly positive."""
+    import torch
+    w = se.workloads.small_case(n=(32, 28, 40), nt=160, seed=24, sponge_width=6)
+    s = se.WaveEquationSolver(se.GridParams(w.nx, w.ny, w.nz, w.d, w.d, w.d),
+                              se.SolverConfig(dt=w.dt, nt=w.nt, sponge_width=w.sponge_width,
+                                              sponge_damping=w.sponge_damping, sponge_mode="stable"))
+    sh = w.shots[0]
+    v0 = torch.from_numpy(se.workloads.smooth(w.vel, 2.0).astype(np.float32)).cuda()
+    se.fwi.set_velocity_device(s, torch.from_numpy(w.vel.astype(np.float32)).cuda())
+    d_obs = torch.zeros((w.nt, sh.rec.count), device="cuda")
+    se.shot_forward(s, sh.src, sh.wavelet, w.nt, sh.rec, seis=d_obs)
+    se.fwi.set_velocity_device(s, v0)
+    g = torch.zeros(w.points, device="cuda")
+    res = torch.zeros_like(d_obs)
+    se.fwi.fwi_gradient(s, sh.src, sh.wavelet, w.nt, sh.rec, d_obs, g, snap_kind=3, residual=res)
+    image = torch.zeros(w.points, device="cuda")
+    illum = torch.zeros(w.points, device="cuda")
+    assert se.rtm_shot(s, sh.src, sh.wavelet, w.nt, sh.rec, res, image, illum, snap_kind=3) == 0
+    torch.cuda.synchronize()
+    g_ref = -image * 2.0 * v0.reshape(-1) * w.dt * w.dt
+    cos = float(torch.dot(g.double(), g_ref.double()) / (torch.linalg.norm(g.double()) *
+                                                          torch.linalg.norm(g_ref.double())))
+    print(f"cosine(exact gradient, reference pointwise formula) = {cos:.3f}")
+    assert cos > 0.5

@@ -199,3 +199,26 @@ def test_smooth_gradient_vs_oracle(se, oracle):
         ref = oracle.smooth_gradient(g, nx, ny, nz, sigma)
         np.testing.assert_allclose(out, ref, rtol=1e-12, atol=1e-13)
     assert not se.SparseOps.smooth_gradient(np.ones(10), nx, ny, nz, 1.0).any()
+
+
+def test_regularised_update_with_given_rhs(se):
+    """(I + L^T L) x = g for the 7-point Laplacian L (built by the FD-stencil
+    builder with unit coefficients and a diagonal shift) with the right-hand
+    side given directly: against a dense FP64 solve."""
+    import torch
+    n = 10
+    L = se.CSRMatrix()
+    L.build_fd_stencil_7point(n, n, n, np.full(n ** 3, 1.0), 1.0, 1.0, 1.0, 1.0)
+    L.add_diagonal(-2.0)
+    rp, col, val = L.row_ptr(), L.col_ind(), L.values()
+    Ld = np.zeros((n ** 3, n ** 3))
+    for i in range(n ** 3):
+        Ld[i, col[rp[i]:rp[i + 1]]] = val[rp[i]:rp[i + 1]]
+    assert np.allclose(np.diag(Ld), -6.0) and np.allclose(Ld, Ld.T)
+    g = np.random.default_rng(13).standard_normal(n ** 3)
+    xs = np.linalg.solve(np.eye(n ** 3) + Ld.T @ Ld, g)
+    x = torch.zeros(n ** 3, device="cuda")
+    rhs = torch.from_numpy(g.astype(np.float32)).cuda()
+    it, rel, true_rel = se.normal_cg_device(L, None, 1.0, x, 2000, 1e-7, True, rhs=rhs)
+    assert true_rel < 1e-6
+    assert np.linalg.norm(x.cpu().numpy() - xs) <= 1e-5 * np.linalg.norm(xs)
