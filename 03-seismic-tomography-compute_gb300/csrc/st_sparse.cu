@@ -16,6 +16,8 @@
 
 #include "st_sparse.cuh"
 
+#include <cstdlib>
+
 namespace stg {
 namespace {
 
@@ -535,6 +537,18 @@ int build_transpose(const DevCsr& A, DevCsr* T, cudaStream_t st) {
 int launch_spmv(const DevCsr& A, const float* x, float* y, const float* add, float add_scale, const float* pdot,
                 double* dot_acc, const int* done, cudaStream_t st) {
     const double avg = A.rows > 0 ? (double)A.nnz / (double)A.rows : 0.0;
+    // tuning override: SEISMIC_GB300_SPMV_G=<2|4|8|16|32> threads per row
+    static const int forced = [] {
+        const char* e = std::getenv("SEISMIC_GB300_SPMV_G");
+        return e ? std::atoi(e) : 0;
+    }();
+    switch (forced) {
+        case 32: return launch_spmv_g<32>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
+        case 16: return launch_spmv_g<16>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
+        case 8: return launch_spmv_g<8>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
+        case 4: return launch_spmv_g<4>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
+        default: break;
+    }
     if (avg >= 48) return launch_spmv_g<32>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
     if (avg >= 24) return launch_spmv_g<16>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
     if (avg >= 10) return launch_spmv_g<8>(A, x, y, add, add_scale, pdot, dot_acc, done, st);

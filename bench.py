@@ -506,6 +506,17 @@ def run_kernel(args):
         res.update({"workload": f"A x and A^T y, {A.rows()} x {A.cols()}, nnz {nnz}",
                     "alg_bytes": 2 * nnz * 8 + (A.rows() + A.cols()) * 16})
         st = torch.cuda.ExternalStream(A.stream_ptr())  # the SpMV kernels run on the matrix's stream
+        one()
+        torch.cuda.synchronize()
+        for name, fn in (("A_ms", lambda: A.spmv_device(xv, yv)),
+                         ("AT_ms", lambda: A.spmv_device(yv, zv, transpose=True))):
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f0.record(st)
+            for _ in range(max(args.steps, 1)):
+                fn()
+            f1.record(st)
+            torch.cuda.synchronize()
+            res[name] = f0.elapsed_time(f1) / max(args.steps, 1)
     for _ in range(args.warmup):
         one()
     torch.cuda.synchronize()
