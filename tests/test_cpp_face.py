@@ -1,0 +1,62 @@
+"""The header-only C++ face (include/seismic_gb300.hpp): compiles and links
+against the library on CPU; on the GPU its figures equal those of the same
+calls through the Python face (same library), and its CG solves."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(REPO, "03-seismic-tomography-compute_gb300")
+OUT = os.path.join(REPO, "tests", "_build")
+
+
+def build_demo():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("st_build", os.path.join(PKG, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    lib = mod.build()
+    os.makedirs(OUT, exist_ok=True)
+    exe = os.path.join(OUT, "face_demo")
+    libdir = os.path.dirname(lib)
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", os.path.join(REPO, "include"),
+           os.path.join(REPO, "tests", "cpp", "face_demo.cpp"), "-L", libdir, "-lseismic_gb300",
+           f"-Wl,-rpath,{libdir}", "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return exe
+
+
+def test_cpp_face_compiles_and_links():
+    assert os.path.exists(build_demo())
+
+
+@pytest.mark.gpu
+def test_cpp_face_matches_python_face():
+    import seismic_engine as se
+    exe = build_demo()
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    vals = {}
+    for line in r.stdout.splitlines():
+        k, *v = line.split()
+        vals[k] = [float(t) for t in v]
+    s = se.WaveEquationSolver(se.GridParams(20, 18, 22, 10.0, 10.0, 10.0),
+                              se.SolverConfig(dt=0.001, sponge_width=4, sponge_damping=0.015))
+    s.initialize_velocity(2500.0)
+    for t in range(30):
+        s.inject_source(10, 9, 5, [np.sin(0.3 * t)])
+        s.step_forward(t)
+    e = s.compute_energy()
+    assert vals["energy"][0] == pytest.approx(e, rel=1e-12)
+    assert vals["energy"][1] == pytest.approx(e, rel=1e-6)
+    assert vals["cfl"][0] == 1 and vals["mpi"][0] == 2.0
+    f = s.field()
+    eng = se.RTMEngine(20, 18, 22, 10.0, 10.0, 10.0, 1)
+    eng.apply_image_condition(f.current, f.previous, 20, 24, 0)
+    eng.finalize_image()
+    assert vals["image"][0] == pytest.approx(float(eng.result().image.sum()), rel=1e-12)
+    assert vals["cg_rel"][0] < 1e-5
+    assert vals["nnz"][0] > 0 and vals["nnz"][1] == 512
