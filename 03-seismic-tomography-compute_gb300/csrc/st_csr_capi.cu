@@ -217,6 +217,23 @@ int st_csr_build_ray_matrix(st_csr* m, int64_t n_rays, const double* endpoints, 
     return ST_OK;
 }
 
+int st_csr_build_sampled_ray_matrix(st_csr* m, st_ray_picks* p, int64_t* nnz) {
+    ST_CHECK(m && p, ST_ERR_ARG, "null argument");
+    ST_CUDA(cudaSetDevice(m->device));
+    DevCsr out;
+    long long total = 0;
+    int rc = build_sampled_ray_csr(p, &out, &total, m->stream);
+    if (rc < 0) {
+        out.release();
+        return rc;
+    }
+    m->A.release();
+    drop_transpose(m);
+    m->A = out;
+    if (nnz) *nnz = total;
+    return ST_OK;
+}
+
 int st_csr_shape(st_csr* m, int64_t out[3]) {
     ST_CHECK(m && out, ST_ERR_ARG, "null argument");
     out[0] = m->A.rows;

@@ -97,6 +97,9 @@ int build_transpose(const DevCsr& A, DevCsr* T, cudaStream_t st);
 // endpoints in cell units; total_nnz (may be null) receives the entry count.
 int build_ray_csr(long long nrays, const double* d_ends, int nx, int ny, int nz, double h, DevCsr* out,
                   long long* total_nnz, cudaStream_t st);
+// Sampled-ray matrix of a pick set (st_sampled_rays.cu): rows = picks,
+// columns = cells, duplicates (samples of one pick in one cell) summed.
+int build_sampled_ray_csr(const st_ray_picks* p, DevCsr* out, long long* nnz, cudaStream_t st);
 int launch_spmv(const DevCsr& A, const float* x, float* y, const float* add, float add_scale, const float* pdot,
                 double* dot_acc, const int* done, cudaStream_t st);
 int launch_f64_to_f32(const double* a, float* b, long long n, cudaStream_t st);

@@ -18,6 +18,7 @@ from .config import (  # noqa: F401
     InversionConfig, ModelConfig, TomographyConfig, load_config,
 )
 from .rtm import RTMConfig, RTMEngine, RTMImageCondition, SliceAxis, SliceSpec  # noqa: F401
+from .rays import SampledRays  # noqa: F401
 from . import workloads  # noqa: F401
 
 __version__ = "1.2.0+gb300"

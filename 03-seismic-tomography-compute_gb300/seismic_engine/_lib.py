@@ -74,6 +74,12 @@ class ShotC(C.Structure):
                 ("rec", ReceiverGridC)]
 
 
+class RayModelC(C.Structure):
+    _fields_ = [("nx", C.c_int64), ("ny", C.c_int64), ("nz", C.c_int64),
+                ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+                ("origin_x", C.c_double), ("origin_y", C.c_double), ("origin_z", C.c_double)]
+
+
 _d = C.POINTER(C.c_double)
 _f = C.POINTER(C.c_float)
 _i64 = C.POINTER(C.c_int64)
@@ -156,6 +162,13 @@ SIGNATURES = {
     "st_csr_build_fd_stencil_7point": [_vp, C.c_int64, C.c_int64, C.c_int64, _d, C.c_double, C.c_double,
                                        C.c_double, C.c_double, C.c_int],
     "st_csr_build_ray_matrix": [_vp, C.c_int64, _vp, C.c_int, C.c_int64, C.c_int64, C.c_int64, C.c_double, _i64],
+    "st_csr_build_sampled_ray_matrix": [_vp, _vp, _i64],
+    "st_ray_picks_create": [C.c_int, C.POINTER(RayModelC), C.c_int64, _vp, _vp, _vp, _vp, _vp, C.POINTER(_vp)],
+    "st_ray_picks_destroy": [_vp],
+    "st_ray_picks_info": [_vp, _i64],
+    "st_ray_picks_stream": [_vp, C.POINTER(_vp)],
+    "st_ray_picks_forward_model": [_vp, _vp, C.c_int, _vp],
+    "st_ray_picks_compute_gradient": [_vp, _vp, _vp, C.c_int, _vp],
     "st_csr_shape": [_vp, _i64],
     "st_csr_get": [_vp, _i64, _i64, _d],
     "st_csr_device_arrays": [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)],

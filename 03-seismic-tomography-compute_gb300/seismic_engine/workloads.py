@@ -271,3 +271,48 @@ def noisy_data(A_x: np.ndarray, level: float, seed: int) -> np.ndarray:
     """b = A x_true + level * std(A x_true) * N(0, 1)."""
     noise = np.random.default_rng(seed).standard_normal(A_x.size)
     return A_x + level * float(np.std(A_x)) * noise
+
+
+# ------------------------------------------- midpoint-sampled traveltime picks
+
+@dataclass
+class PickSet:
+    """Picks of the reference's Python inversion driver (one per source-station
+    pair): model = (nx, ny, nz, dx, dy, dz, origin_x, origin_y, origin_z),
+    world coordinates in metres, velocities vp (nx, ny, nz) FP64 in m/s."""
+    name: str
+    model: tuple
+    src_xyz: np.ndarray   # [n_picks, 3]
+    sta_xyz: np.ndarray   # [n_picks, 3]
+    weight: np.ndarray    # [n_picks]
+    vp: np.ndarray        # (nx, ny, nz)
+
+
+def gradient_model(nx: int, ny: int, nz: int, dz: float, water_depth: float = 4000.0) -> np.ndarray:
+    """VelocityModel.initialize_gradient_model's vp (model.py:46-64): water
+    (1500 m/s) above water_depth, below it 3000 (1 + 0.3 depth / 5000) capped
+    at 8500."""
+    z = np.arange(nz) * dz
+    col = np.where(z < water_depth, 1500.0, np.minimum(3000.0 * (1.0 + 0.3 * (z - water_depth) / 5000.0), 8500.0))
+    return np.broadcast_to(col, (nx, ny, nz)).copy()
+
+
+def obs_picks(n: int = 100, d: float = 200.0, n_sources: int = 2000, n_stations: int = 1000,
+              seed: int = 9) -> PickSet:
+    """n^3 cells of d metres; sources (earthquakes) uniform in the volume below
+    the seafloor, ocean-bottom stations uniform on the seafloor at 4000 m; one
+    pick per source-station pair (n_sources * n_stations picks, in source-major
+    order), weights uniform in [0.5, 1.5]; vp = the gradient model plus a
+    smooth 5% perturbation."""
+    rng = np.random.default_rng(seed)
+    ext = n * d
+    src = np.stack([rng.uniform(0, ext, n_sources), rng.uniform(0, ext, n_sources),
+                    rng.uniform(4000.0, ext, n_sources)], axis=1)
+    sta = np.stack([rng.uniform(0, ext, n_stations), rng.uniform(0, ext, n_stations),
+                    np.full(n_stations, 4000.0)], axis=1)
+    src_xyz = np.repeat(src, n_stations, axis=0)
+    sta_xyz = np.tile(sta, (n_sources, 1))
+    weight = rng.uniform(0.5, 1.5, n_sources * n_stations)
+    vp = gradient_model(n, n, n, d) * (1.0 + 0.05 * smooth_model(n, 4.0, seed + 1).reshape(n, n, n))
+    return PickSet(f"picks-{n}^3-{n_sources}x{n_stations}", (n, n, n, d, d, d, 0.0, 0.0, 0.0), src_xyz, sta_xyz,
+                   weight, vp)

@@ -57,12 +57,13 @@ def parse():
     ap.add_argument("--segment", type=int, default=200, help="checkpoint segment length of --workload large")
     ap.add_argument("--compare", action="store_true",
                     help="--workload large: also time FP32 segment snapshots and unpreconditioned CG")
-    ap.add_argument("--kernel", choices=["conv", "spmv"], default=None,
+    ap.add_argument("--kernel", choices=["conv", "spmv", "rays"], default=None,
                     help="time one kernel alone (profiling runs) instead of the workload")
     ap.add_argument("--no-tomo", action="store_true", help="skip the tomography CG measurement")
     ap.add_argument("--tomo-n", type=int, default=100, help="cell grid edge of the --kernel spmv matrix")
     ap.add_argument("--tomo-rays", type=int, default=2_000_000, help="rays of the --kernel spmv matrix")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner solve")
+    ap.add_argument("--no-rays", action="store_true", help="skip the sampled-ray forward/gradient measurement")
     return ap.parse_args()
 
 
@@ -342,6 +343,69 @@ def run_tomography(args):
     return out
 
 
+def run_sampled_rays(args):
+    """The reference's Python inversion driver's traveltime forward model and
+    gradient (midpoint-sampled straight rays, inversion.py:329-433) on 100^3
+    cells of 200 m with 2000 sources x 1000 ocean-bottom stations (2M picks):
+    pick-set build, device forward and gradient (CUDA events on the pick
+    set's stream), the same through the host API (numpy in and out), and the
+    oracle's single-thread C restatement on a bounded sample of the picks."""
+    import torch
+    import seismic_engine as se
+    ps = se.workloads.obs_picks()
+    t0 = time.perf_counter()
+    rays = se.SampledRays(ps.model, ps.src_xyz, ps.sta_xyz, ps.weight)
+    build_ms = 1e3 * (time.perf_counter() - t0)
+    vp = torch.from_numpy(ps.vp.reshape(-1)).cuda()
+    rng = np.random.default_rng(3)
+    res = torch.from_numpy(rng.standard_normal(rays.n_picks) * 0.05).cuda()
+    times = torch.empty(rays.n_picks, dtype=torch.float64, device="cuda")
+    grad = torch.empty(rays.n_cells, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.ExternalStream(rays.stream_ptr())
+    out = {"workload": f"{ps.name}: {rays.n_picks} picks, {rays.n_samples} midpoint samples on "
+                       f"{ps.model[0]}^3 cells of {ps.model[3]:.0f} m (FP64, bit-exact vs the reference's formulas)",
+           "n_picks": rays.n_picks, "n_samples": rays.n_samples, "build_ms": build_ms}
+    for name, fn in (("forward", lambda: rays.forward_model(vp, out=times)),
+                     ("gradient", lambda: rays.compute_gradient(vp, res, out=grad))):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(10):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 10
+        out[name] = {"ms": ms, "gsamples_per_s": rays.n_samples / ms / 1e6}
+    vp_h = ps.vp.reshape(-1).copy()
+    res_h = res.cpu().numpy()
+    rays.forward_model(vp_h)
+    t0 = time.perf_counter()
+    t_h = rays.forward_model(vp_h)
+    g_h = rays.compute_gradient(vp_h, res_h)
+    out["host_api_ms"] = {"forward_plus_gradient": 1e3 * (time.perf_counter() - t0),
+                          "h2d_bytes": int(2 * vp_h.nbytes + res_h.nbytes), "d2h_bytes": int(t_h.nbytes + g_h.nbytes)}
+    out["host_matches_device"] = bool(np.array_equal(t_h, times.cpu().numpy()) and
+                                      np.array_equal(g_h, grad.cpu().numpy()))
+    if not args.no_cpu_baseline:
+        from oracle import Oracle
+        orc = Oracle()
+        k = 100_000
+        n = np.array(ps.model[:3])
+        d = np.array(ps.model[3:6])
+        o = np.array(ps.model[6:9])
+        t0 = time.perf_counter()
+        orc.sampled_traveltimes(n, d, o, ps.src_xyz[:k], ps.sta_xyz[:k], None, ps.vp)
+        orc.sampled_gradient(n, d, o, ps.src_xyz[:k], ps.sta_xyz[:k], None, ps.weight[:k], ps.vp, res_h[:k])
+        cpu_s = (time.perf_counter() - t0) * rays.n_picks / k
+        gpu_s = (out["forward"]["ms"] + out["gradient"]["ms"]) / 1e3
+        out["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": f"first {k} picks, scaled to all",
+                               "forward_plus_gradient_s": cpu_s, "gpu_speedup": cpu_s / gpu_s}
+    rays.close()
+    return out
+
+
 # ---------------------------------------------------------------- GPU leg
 def run_gpu(args):
     import torch
@@ -457,6 +521,9 @@ def run_gpu(args):
         del image, illum, refl, data
         torch.cuda.empty_cache()
         line["tomography"] = run_tomography(args)
+    if rank == 0 and world == 1 and not args.no_rays:
+        torch.cuda.empty_cache()
+        line["sampled_rays"] = run_sampled_rays(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -468,7 +535,8 @@ def run_gpu(args):
 def run_kernel(args):
     """Single-kernel timing for profiling: 'conv' = the tensor-core 3x3x3
     32 -> 32 convolution on a 100^3 volume; 'spmv' = A x and A^T y of the
-    100^3 / 2M-ray tomography matrix. Prints one JSON line."""
+    100^3 / 2M-ray tomography matrix; 'rays' = the sampled-ray forward model
+    and gradient of 2M picks. Prints one JSON line."""
     import ctypes as C
     import torch
     import seismic_engine as se
@@ -492,6 +560,30 @@ def run_kernel(args):
             assert rc == 0
         flops = 2.0 * n ** 3 * 32 * 32 * 27
         res.update({"workload": f"3x3x3 conv, 32 -> 32 channels, BF16 operands, {n}^3 voxels", "flops": flops})
+    elif args.kernel == "rays":
+        ps = se.workloads.obs_picks()
+        rays = se.SampledRays(ps.model, ps.src_xyz, ps.sta_xyz, ps.weight)
+        vp = torch.from_numpy(ps.vp.reshape(-1)).cuda()
+        rs = torch.from_numpy(np.random.default_rng(3).standard_normal(rays.n_picks) * 0.05).cuda()
+        tt = torch.empty(rays.n_picks, dtype=torch.float64, device="cuda")
+        gg = torch.empty(rays.n_cells, dtype=torch.float64, device="cuda")
+
+        def one():
+            rays.forward_model(vp, out=tt)
+            rays.compute_gradient(vp, rs, out=gg)
+        res.update({"workload": f"sampled-ray forward + gradient, {rays.n_picks} picks, {rays.n_samples} samples"})
+        st = torch.cuda.ExternalStream(rays.stream_ptr())
+        one()
+        torch.cuda.synchronize()
+        for name, fn in (("forward_ms", lambda: rays.forward_model(vp, out=tt)),
+                         ("gradient_ms", lambda: rays.compute_gradient(vp, rs, out=gg))):
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f0.record(st)
+            for _ in range(max(args.steps, 1)):
+                fn()
+            f1.record(st)
+            torch.cuda.synchronize()
+            res[name] = f0.elapsed_time(f1) / max(args.steps, 1)
     else:
         nt_, nr_ = args.tomo_n, args.tomo_rays
         A = se.CSRMatrix()

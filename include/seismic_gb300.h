@@ -377,6 +377,61 @@ int st_csr_build_fd_stencil_7point(st_csr* m, int64_t nx, int64_t ny, int64_t nz
  * padding. nnz (may be NULL) receives the entry count. */
 int st_csr_build_ray_matrix(st_csr* m, int64_t n_rays, const double* endpoints, int on_device, int64_t nx,
                             int64_t ny, int64_t nz, double cell_size, int64_t* nnz);
+/* ------------------------------------------ sampled straight-ray picks */
+/* The traveltime forward model and gradient of the reference's Python
+ * inversion driver, AdjointStateInversion._forward_model and
+ * _compute_gradient (seismic_tomography/inversion.py:329-433), on the GPU.
+ * Each pick's source and station are snapped to cells (int((p - origin) / d)
+ * clamped to the grid, :344-350); the ray between the two cells is sampled
+ * at n = max(int(dist / (5 dx)), 2) midpoints, cell = int(c_src + frac *
+ * (c_sta - c_src)) per axis with frac = (k + 0.5) / n (:352-364), each of
+ * length ds = dist / n. The sample list is built once per pick set; the
+ * forward model and the gradient then run for any velocity model.
+ * Velocities vp are the model's (nx, ny, nz) array in C order (cell (ix, iy,
+ * iz) at (ix * ny + iy) * nz + iz, model.py:27,89), FP64. */
+typedef struct st_ray_model {
+    int64_t nx, ny, nz;                 /* VelocityModel.nx/ny/nz (model.py:13-18) */
+    double dx, dy, dz;                  /* cell spacing */
+    double origin_x, origin_y, origin_z; /* VelocityModel.origin_* */
+} st_ray_model;
+typedef struct st_ray_picks st_ray_picks;
+/* n_picks picks in the order of OBSDataCoordinator.picks (obs_data.py:38-40):
+ * src_xyz / sta_xyz = [n_picks][3] world coordinates of each pick's source
+ * and station, weight = pick.weight, valid[i] = 0 for a pick whose source or
+ * station id is unknown (time 0, no gradient, :333-335; NULL = all valid).
+ * dist (may be NULL) = the source-station distances to use: the reference
+ * squares Python floats with x ** 2 (libm pow), which can round one unit in
+ * the last place away from the x * x computed here, so passing its
+ * distances makes every result the reference's bit for bit. All host
+ * arrays, copied. Non-finite coordinates (where the reference's int() would
+ * raise) and rays of more than 2^24 samples are refused with ST_ERR_ARG. */
+int st_ray_picks_create(int device, const st_ray_model* model, int64_t n_picks, const double* src_xyz,
+                        const double* sta_xyz, const double* dist, const double* weight, const uint8_t* valid,
+                        st_ray_picks** out);
+int st_ray_picks_destroy(st_ray_picks* p);
+/* out = {n_picks, n_samples (total midpoint samples), n_cells}. */
+int st_ray_picks_info(st_ray_picks* p, int64_t out[3]);
+int st_ray_picks_stream(st_ray_picks* p, void** out);
+/* _forward_model (inversion.py:329-381): times[i] = sum over the samples in
+ * order of ds / v, an invalid velocity (non-finite or <= 0) read as 1500, a
+ * non-finite term skipped, a non-finite or negative sum replaced by
+ * dist / 6000. FP64, bit-exact against the reference given its distances.
+ * on_device = 0: host arrays, returns when done; 1: device arrays, enqueued
+ * on the handle's stream. */
+int st_ray_picks_forward_model(st_ray_picks* p, const double* vp, int on_device, double* times);
+/* _compute_gradient (inversion.py:383-433): gradient (n_cells, overwritten)
+ * = sum over picks with a finite residual and their samples at a valid
+ * velocity of (residual * (-ds / v^2)) * weight, each cell's terms added in
+ * the reference's pick, then sample order (bit-exact as above). */
+int st_ray_picks_compute_gradient(st_ray_picks* p, const double* vp, const double* residuals, int on_device,
+                                  double* gradient);
+/* The sampled-ray matrix of the picks as a CSR (rows = picks, columns =
+ * cells, A[i, c] = ds_i * the number of samples of pick i in cell c, FP32),
+ * so that A (1 / vp) gives the forward model wherever every velocity is
+ * valid, and -(A^T (w r)) / vp^2 the gradient: the system the reference's
+ * inversion linearises, for the CG solvers. nnz may be NULL. */
+int st_csr_build_sampled_ray_matrix(st_csr* m, st_ray_picks* p, int64_t* nnz);
+
 /* rows(), cols(), nnz() (csr_matrix.h:32-34): out = {rows, cols, nnz}. */
 int st_csr_shape(st_csr* m, int64_t out[3]);
 /* row_ptr(), col_ind(), values() (csr_matrix.h:36-38) copied to the host (any may be NULL). */

@@ -96,6 +96,9 @@ class Oracle:
         L.orc_ray_triplets.argtypes = [C.c_int64, _d, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int64, _i64, _i64,
                                        _d]
         L.orc_ray_triplets.restype = C.c_int64
+        _u8 = C.POINTER(C.c_uint8)
+        L.orc_sampled_traveltimes.argtypes = [_i64, _d, _d, C.c_int64, _d, _d, _d, _u8, _d, _d]
+        L.orc_sampled_gradient.argtypes = [_i64, _d, _d, C.c_int64, _d, _d, _d, _u8, _d, _d, _d, _d]
         L.orc64_repair_field_nan.argtypes = [_d, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int, C.c_double]
         L.orc64_repair_field_nan.restype = C.c_int64
         L.orc64_clamp_field.argtypes = [_d, C.c_int64, C.c_double, C.c_double]
@@ -261,6 +264,43 @@ class Oracle:
         k = self.lib.orc_ray_triplets(e.shape[0], _p(e, _d), nx, ny, nz, h, cap, _p(r, _i64), _p(c, _i64), _p(v, _d))
         assert k >= 0
         return self.csr_build(e.shape[0], nx * ny * nz, r[:k], c[:k], v[:k])
+
+    @staticmethod
+    def _picks(n, d, origin, src_xyz, sta_xyz, valid, dist=None):
+        n = np.ascontiguousarray(n, np.int64)
+        d = np.ascontiguousarray(d, np.float64)
+        o = np.ascontiguousarray(origin, np.float64)
+        s = np.ascontiguousarray(src_xyz, np.float64).reshape(-1, 3)
+        r = np.ascontiguousarray(sta_xyz, np.float64).reshape(-1, 3)
+        v = np.ones(s.shape[0], np.uint8) if valid is None else np.ascontiguousarray(valid, np.uint8)
+        dp = None if dist is None else _p(np.ascontiguousarray(dist, np.float64), _d)
+        return n, d, o, s, r, v, dp
+
+    def sampled_traveltimes(self, n, d, origin, src_xyz, sta_xyz, valid, vp, dist=None):
+        """Midpoint-sampled straight-ray traveltimes of the reference's Python
+        inversion (inversion.py:329-381); vp (nx, ny, nz) FP64; dist = the
+        per-pick source-station distances to use (None: computed)."""
+        dist = None if dist is None else np.ascontiguousarray(dist, np.float64)
+        n, d, o, s, r, v, dp = self._picks(n, d, origin, src_xyz, sta_xyz, valid, dist)
+        vp = np.ascontiguousarray(vp, np.float64).reshape(-1)
+        t = np.zeros(s.shape[0])
+        u8 = C.POINTER(C.c_uint8)
+        self.lib.orc_sampled_traveltimes(_p(n, _i64), _p(d, _d), _p(o, _d), s.shape[0], _p(s, _d), _p(r, _d),
+                                         dp, _p(v, u8), _p(vp, _d), _p(t, _d))
+        return t
+
+    def sampled_gradient(self, n, d, origin, src_xyz, sta_xyz, valid, weight, vp, residuals, dist=None):
+        """Its gradient (inversion.py:383-433), FP64 over the nx*ny*nz cells."""
+        dist = None if dist is None else np.ascontiguousarray(dist, np.float64)
+        n, d, o, s, r, v, dp = self._picks(n, d, origin, src_xyz, sta_xyz, valid, dist)
+        vp = np.ascontiguousarray(vp, np.float64).reshape(-1)
+        w = np.ascontiguousarray(weight, np.float64)
+        res = np.ascontiguousarray(residuals, np.float64)
+        g = np.zeros(int(np.prod(n)))
+        u8 = C.POINTER(C.c_uint8)
+        self.lib.orc_sampled_gradient(_p(n, _i64), _p(d, _d), _p(o, _d), s.shape[0], _p(s, _d), _p(r, _d),
+                                      dp, _p(v, u8), _p(w, _d), _p(vp, _d), _p(res, _d), _p(g, _d))
+        return g
 
     def smooth_gradient(self, g, nx, ny, nz, sigma):
         g = np.ascontiguousarray(g, np.float64).reshape(-1)

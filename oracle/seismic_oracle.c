@@ -587,3 +587,100 @@ int64_t orc_ray_triplets(int64_t nrays, const double* ends, int nx, int ny, int 
     }
     return k;
 }
+
+/* ------------------------------------------------------- sampled rays */
+/* Straight-ray traveltimes and their gradient as the reference's Python
+ * inversion driver computes them (seismic_tomography/inversion.py:329-433):
+ * the source and the station are snapped to cells (int((p - origin) / d),
+ * clamped to the grid; :344-350); the ray is sampled at
+ * n = max(int(dist / (5 dx)), 2) midpoints frac = (k + 0.5) / n, cell
+ * c = int(c_src + frac * (c_sta - c_src)) per axis (:355-364), each sample
+ * of length ds = dist / n. Forward (:329-381): t = sum ds / v in sample
+ * order, an invalid velocity (non-finite or <= 0) read as 1500, a
+ * non-finite term skipped, a non-finite or negative total replaced by
+ * dist / 6000. Gradient (:383-433): g[cell] += (r * (-ds / (v * v))) * w in
+ * pick, then sample order, picks with a non-finite residual and samples at
+ * an invalid velocity skipped. Picks with valid[i] == 0 (unknown source or
+ * station) get time 0 and no gradient. vp is (nx, ny, nz) C order, cell
+ * (ix, iy, iz) -> (ix * ny + iy) * nz + iz. FP64 in source order (no
+ * contractions). The reference's distance squares Python floats with
+ * x ** 2 (libm pow), which can round one unit in the last place away from
+ * the correctly rounded x * x used here; given the reference's distances
+ * (dist != NULL) the results are the reference's bit for bit. */
+static int64_t orc_snap(double p, double o, double d, int64_t n) {
+    const double q = (p - o) / d;
+    if (q < 1.0) return 0;
+    if (q >= (double)(n - 1)) return n - 1;
+    return (int64_t)q;
+}
+
+typedef struct {
+    int64_t c0[3], c1[3];
+    int64_t n_steps;
+    double dist, ds;
+} orc_pick_geo;
+
+static orc_pick_geo orc_pick(const int64_t n[3], const double d[3], const double o[3], const double* s,
+                             const double* r, const double* dist) {
+    orc_pick_geo g;
+    const double ex = s[0] - r[0], ey = s[1] - r[1], ez = s[2] - r[2];
+    g.dist = dist ? *dist : sqrt((ex * ex + ey * ey) + ez * ez);
+    for (int a = 0; a < 3; ++a) {
+        g.c0[a] = orc_snap(s[a], o[a], d[a], n[a]);
+        g.c1[a] = orc_snap(r[a], o[a], d[a], n[a]);
+    }
+    const double q = g.dist / (d[0] * 5.0);
+    g.n_steps = q < 3.0 ? 2 : (int64_t)q;
+    g.ds = g.dist / (double)g.n_steps;
+    return g;
+}
+
+static int64_t orc_sample_cell(const orc_pick_geo* g, const int64_t n[3], int64_t k) {
+    const double frac = ((double)k + 0.5) / (double)g->n_steps;
+    int64_t c[3];
+    for (int a = 0; a < 3; ++a) {
+        int64_t v = (int64_t)((double)g->c0[a] + frac * (double)(g->c1[a] - g->c0[a]));
+        c[a] = v < 0 ? 0 : (v > n[a] - 1 ? n[a] - 1 : v);
+    }
+    return (c[0] * n[1] + c[1]) * n[2] + c[2];
+}
+
+void orc_sampled_traveltimes(const int64_t n[3], const double d[3], const double o[3], int64_t n_picks,
+                             const double* src, const double* sta, const double* dist, const uint8_t* valid,
+                             const double* vp, double* times) {
+    for (int64_t i = 0; i < n_picks; ++i) {
+        times[i] = 0.0;
+        if (valid && !valid[i]) continue;
+        const orc_pick_geo g = orc_pick(n, d, o, src + 3 * i, sta + 3 * i, dist ? dist + i : NULL);
+        double t = 0.0;
+        for (int64_t k = 0; k < g.n_steps; ++k) {
+            double v = vp[orc_sample_cell(&g, n, k)];
+            if (!isfinite(v) || v <= 0.0) v = 1500.0;
+            const double term = g.ds / v;
+            if (!isfinite(term)) continue;
+            t += term;
+        }
+        if (!isfinite(t) || t < 0.0) t = g.dist / 6000.0;
+        times[i] = t;
+    }
+}
+
+void orc_sampled_gradient(const int64_t n[3], const double d[3], const double o[3], int64_t n_picks,
+                          const double* src, const double* sta, const double* dist, const uint8_t* valid,
+                          const double* weight,
+                          const double* vp, const double* resid, double* grad) {
+    memset(grad, 0, sizeof(double) * (size_t)(n[0] * n[1] * n[2]));
+    for (int64_t i = 0; i < n_picks; ++i) {
+        if (valid && !valid[i]) continue;
+        if (!isfinite(resid[i])) continue;
+        const orc_pick_geo g = orc_pick(n, d, o, src + 3 * i, sta + 3 * i, dist ? dist + i : NULL);
+        for (int64_t k = 0; k < g.n_steps; ++k) {
+            const int64_t c = orc_sample_cell(&g, n, k);
+            const double v = vp[c];
+            if (!isfinite(v) || v <= 0.0) continue;
+            const double f = -g.ds / (v * v);
+            if (!isfinite(f)) continue;
+            grad[c] += (resid[i] * f) * weight[i];
+        }
+    }
+}

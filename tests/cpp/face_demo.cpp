@@ -25,7 +25,7 @@ int main(int argc, char** argv) {
     const seismic::WaveField& f = solver.field();
     double e = 0.0;
     for (double v : f.current) e += v * v;
-    std::printf("energy %.9e %.9e\n", solver.compute_energy(), e);
+    std::printf("energy %.17g %.17g\n", solver.compute_energy(), e);
     std::printf("cfl %d\n", solver.verify_cfl() ? 1 : 0);
     std::printf("mpi %g\n", mpi.allreduce_sum(2.0));
 
@@ -34,7 +34,7 @@ int main(int argc, char** argv) {
     rtm.finalize_image();
     double img = 0.0;
     for (double v : rtm.result().image) img += v;
-    std::printf("image %.9e\n", img);
+    std::printf("image %.17g\n", img);
 
     seismic::CSRMatrix A;
     std::vector<double> vel(8 * 8 * 8, 2000.0);
@@ -48,7 +48,7 @@ int main(int argc, char** argv) {
         bb += b[i] * b[i];
     }
     std::printf("cg_rel %.3e\n", std::sqrt(r / bb));
-    std::printf("nnz %lld rows %lld\n", (long long)A.nnz(), (long long)A.rows());
-    std::printf("dot %.9e\n", seismic::SparseOps::dot_product(b, x));
+    std::printf("nnz %lld %lld\n", (long long)A.nnz(), (long long)A.rows());
+    std::printf("dot %.17g\n", seismic::SparseOps::dot_product(b, x));
     return 0;
 }
