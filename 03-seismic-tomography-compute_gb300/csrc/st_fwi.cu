@@ -22,7 +22,8 @@
 
 namespace stg {
 
-int shot_forward_impl(st_solver* s, const st_shot* shot, float* seis, int snap_kind, void* snaps, unsigned* amax);
+int shot_forward_impl(st_solver* s, const st_shot* shot, float* seis, int snap_kind, void* snaps, unsigned* amax,
+                      bool slices = false);
 
 namespace {
 

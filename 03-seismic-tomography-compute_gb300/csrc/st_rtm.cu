@@ -15,6 +15,7 @@
 // path keeps its imaging math and its RTMImageCondition outputs and supplies
 // the missing adjoint.
 #include "st_solver_impl.cuh"
+#include "st_slices.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -90,7 +91,8 @@ int launch_rec_force(st_solver* s, const st_receiver_grid& R, const float* row) 
 
 // Forward shot (shared by st_shot_forward and the RTM / gradient drivers).
 // seis may be null (no sampling); snap_kind != NONE needs snaps and amax.
-int shot_forward_impl(st_solver* s, const st_shot* shot, float* seis, int snap_kind, void* snaps, unsigned* amax) {
+int shot_forward_impl(st_solver* s, const st_shot* shot, float* seis, int snap_kind, void* snaps, unsigned* amax,
+                      bool slices = false) {
     const Layout& L = s->L;
     ST_CHECK(shot->src_ix >= 0 && shot->src_ix < L.nx && shot->src_iy >= 0 && shot->src_iy < L.ny &&
                  shot->src_iz >= 0 && shot->src_iz < L.nz,
@@ -123,6 +125,10 @@ int shot_forward_impl(st_solver* s, const st_shot* shot, float* seis, int snap_k
             a.amax_next = amax + t + 1;
         }
         ST_TRY(fused_step(s, a, snap_kind, SNAP_NONE, 0, nullptr));
+        if (slices && s->slices && t % s->slice_interval == 0) {
+            const SliceSrc S{s->f[s->ic], nullptr, nullptr, ST_FIELD_DEVICE_FP32, ST_IMAGE_FP32, L};
+            ST_TRY(slice_stream_capture(s->slices, S, t, s->stream));
+        }
     }
     return ST_OK;
 }
@@ -177,6 +183,12 @@ int rtm_backward_impl(st_solver* s, const st_shot* shot, const float* data, int 
         }
         ST_TRY(fused_step(s, a, SNAP_NONE, imaging ? snap_kind : SNAP_NONE, imaging ? 1 : 0, nullptr,
                           staged ? &imaps : nullptr));
+        if (imaging && s->slices && t % s->slice_interval == 0) {
+            SliceSrc S{a.snap_in, s->f[s->ic], image, ST_FIELD_DEVICE_FP32, ST_IMAGE_FP32, L};
+            S.fwd_snap = snap_kind;
+            S.fwd_amax = amax + t;
+            ST_TRY(slice_stream_capture(s->slices, S, t, s->stream));
+        }
         if (src_trace) {
             probe_kernel<<<1, 1, 0, s->stream>>>(s->f[s->ic], s->c, L, shot->src_ix, shot->src_iy, shot->src_iz,
                                                  a.force_row, q_src, s->dtab, s->sw, s->sponge_mode, src_trace + t);
@@ -199,7 +211,7 @@ int st_shot_forward(st_solver* s, const st_shot* shot, float* seis, int snap_kin
     ST_CHECK(snap_kind == ST_SNAP_NONE || (snaps && snap_amax), ST_ERR_ARG, "snapshot buffers missing");
     ST_CHECK(shot->rec.nx * shot->rec.ny == 0 || seis, ST_ERR_ARG, "receivers given but no seismogram buffer");
     ST_CUDA(cudaSetDevice(s->device));
-    ST_TRY(shot_forward_impl(s, shot, seis, snap_kind, snaps, snap_amax));
+    ST_TRY(shot_forward_impl(s, shot, seis, snap_kind, snaps, snap_amax, true));
     unsigned fl = 0;
     ST_TRY(read_flags(s, &fl));
     return (fl & FLAG_GUARD) ? ST_NAN_DETECTED_AND_REPAIRED : ST_OK;

@@ -8,6 +8,7 @@
 // coefficient c = v^2 dt^2 (times the reference's CFL damping factor^2), the
 // sponge table, and an FP64 host copy of the velocity in the reference layout.
 #include "st_solver_impl.cuh"
+#include "st_slices.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -583,6 +584,23 @@ int st_solver_set_sponge_mode(st_solver* s, int mode) {
     ST_CHECK(s, ST_ERR_ARG, "null solver");
     ST_CHECK(mode == ST_SPONGE_REFERENCE || mode == ST_SPONGE_STABLE, ST_ERR_ARG, "bad sponge mode %d", mode);
     s->sponge_mode = mode;
+    return ST_OK;
+}
+
+int st_solver_set_slice_stream(st_solver* s, st_slice_stream* ss, int interval) {
+    ST_CHECK(s, ST_ERR_ARG, "null solver");
+    if (ss && interval > 0) {
+        int64_t nx, ny, nz;
+        slice_stream_extents(ss, &nx, &ny, &nz);
+        ST_CHECK(nx == s->L.nx && ny == s->L.ny && nz == s->L.nz, ST_ERR_ARG,
+                 "slice stream grid %lldx%lldx%lld does not match the solver's", (long long)nx, (long long)ny,
+                 (long long)nz);
+        s->slices = ss;
+        s->slice_interval = interval;
+    } else {
+        s->slices = nullptr;
+        s->slice_interval = 0;
+    }
     return ST_OK;
 }
 

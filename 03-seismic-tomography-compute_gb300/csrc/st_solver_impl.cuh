@@ -87,6 +87,8 @@ struct st_solver {
     void* ckpt_buf = nullptr;       // checkpointed adjoint: working set, state slots, segment snapshots
     size_t ckpt_cap = 0;
     int sponge_mode = ST_SPONGE_REFERENCE;  // ST_SPONGE_STABLE: damp the new field (Cerjan form)
+    st_slice_stream* slices = nullptr;  // RTM slice stream (configure_rtm), borrowed
+    int slice_interval = 0;             // capture every slice_interval steps
     // phase boundaries of the last shot-level call, recorded on `stream`:
     // [0] start, [1] forward done, [2] backward done
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};

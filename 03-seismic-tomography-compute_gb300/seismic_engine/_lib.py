@@ -74,6 +74,10 @@ class ShotC(C.Structure):
                 ("rec", ReceiverGridC)]
 
 
+class SliceSpecC(C.Structure):
+    _fields_ = [("axis", C.c_int32), ("index", C.c_int64), ("stride", C.c_int64)]
+
+
 class RayModelC(C.Structure):
     _fields_ = [("nx", C.c_int64), ("ny", C.c_int64), ("nz", C.c_int64),
                 ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
@@ -170,6 +174,22 @@ SIGNATURES = {
     "st_ray_picks_forward_model": [_vp, _vp, C.c_int, _vp],
     "st_ray_picks_compute_gradient": [_vp, _vp, _vp, C.c_int, _vp],
     "st_csr_shape": [_vp, _i64],
+    "st_mmap_writer_open": [C.c_char_p, C.c_int64, C.POINTER(_vp)],
+    "st_mmap_writer_write_frame": [_vp, _vp, C.c_int64],
+    "st_mmap_writer_info": [_vp, _i64],
+    "st_mmap_writer_close": [_vp],
+    "st_mmap_read_frame": [C.c_char_p, C.c_int64, _vp, C.c_int64, _i64],
+    "st_mmap_count_frames": [C.c_char_p, _i64],
+    "st_slice_frame_bytes": [C.c_int64, C.c_int64, C.c_int64, C.POINTER(SliceSpecC)],
+    "st_capture_slice_frames": [C.c_int64, C.c_int64, C.c_int64, C.POINTER(SliceSpecC), C.c_int, _vp, _vp, C.c_int,
+                                _vp, C.c_int, C.c_int64, C.c_double, _vp, C.c_int64, _i64, _vp],
+    "st_slice_stream_create": [C.c_char_p, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.POINTER(SliceSpecC), C.c_int,
+                               C.c_int, C.c_int, C.POINTER(_vp)],
+    "st_slice_stream_capture": [_vp, _vp, _vp, C.c_int, _vp, C.c_int, C.c_int64, _vp],
+    "st_slice_stream_flush": [_vp],
+    "st_slice_stream_stats": [_vp, _i64],
+    "st_slice_stream_destroy": [_vp],
+    "st_solver_set_slice_stream": [_vp, _vp, C.c_int],
     "st_csr_get": [_vp, _i64, _i64, _d],
     "st_csr_device_arrays": [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)],
     "st_csr_stream": [_vp, C.POINTER(_vp)],
@@ -198,7 +218,7 @@ SIGNATURES = {
     "st_field_clamp": [_d, C.c_int64, C.c_double, C.c_double, C.c_int],
     "st_field_repair_nan": [_d, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int, C.c_double, C.c_int],
 }
-_RESTYPES = {"st_last_error": C.c_char_p}
+_RESTYPES = {"st_last_error": C.c_char_p, "st_slice_frame_bytes": C.c_int64}
 
 _lock = threading.Lock()
 _lib = None

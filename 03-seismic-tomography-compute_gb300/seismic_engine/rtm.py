@@ -27,8 +27,8 @@ class SliceAxis(enum.IntEnum):
 
 @dataclass
 class SliceSpec:
-    """seismic::SliceSpec (rtm_engine.h:19-23). Slice capture feeds the
-    reference's visualisation stream and is not part of this library."""
+    """seismic::SliceSpec (rtm_engine.h:19-23); index < 0 = the middle plane.
+    Slice capture and the mmap ring are in seismic_engine.slices."""
     axis: SliceAxis = SliceAxis.Z
     index: int = -1
     stride: int = 1

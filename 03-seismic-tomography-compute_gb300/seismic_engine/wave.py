@@ -133,6 +133,7 @@ class WaveEquationSolver:
 
     def close(self):
         if getattr(self, "_h", None):
+            self.shutdown_rtm_resources()
             _lib.load().st_solver_destroy(self._h)
             self._h = None
 
@@ -260,6 +261,36 @@ class WaveEquationSolver:
         call("st_solver_fault_stats", self._h, C.byref(s))
         return FaultStats(s.total_nan_count, s.total_inf_count, s.cells_repaired, s.timesteps_recovered,
                           s.global_abort_count)
+
+    # ---- RTM slice streaming (wave_equation.cpp:510-575)
+    def configure_rtm(self, cfg):
+        """WaveEquationSolver::configure_rtm: with enable_rtm and
+        enable_mmap_writer, a GPU slice stream on cfg.mmap_filename (ring of
+        cfg.mmap_max_bytes) captures cfg.slice_specs (default: the middle Z, Y
+        and X planes) every cfg.snapshot_interval steps of shot_forward and of
+        the imaging pass of rtm_shot (forward snapshot, adjoint field, image)."""
+        from .slices import SliceStream
+        self.shutdown_rtm_resources()
+        self._rtm_cfg = cfg
+        if cfg.enable_rtm and cfg.enable_mmap_writer and cfg.mmap_filename:
+            ss = SliceStream(cfg.mmap_filename, self.nx, self.ny, self.nz, specs=cfg.slice_specs,
+                             max_bytes=cfg.mmap_max_bytes, capacity=cfg.ring_buffer_capacity)
+            call("st_solver_set_slice_stream", self._h, ss.handle, max(int(cfg.snapshot_interval), 1))
+            self._slices = ss
+
+    def slice_stream(self):
+        """The attached SliceStream (the reference's snapshot_buffer() /
+        mmap_writer() pair), or None."""
+        return getattr(self, "_slices", None)
+
+    def shutdown_rtm_resources(self):
+        """Detaches and closes the slice stream (wave_equation.cpp:562-575),
+        after every captured frame is in the file."""
+        ss = getattr(self, "_slices", None)
+        if ss is not None:
+            call("st_solver_set_slice_stream", self._h, None, 0)
+            ss.close()
+            self._slices = None
 
     # ---- GB300 additions
     def device_field_ptr(self, which: int) -> int:

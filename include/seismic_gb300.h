@@ -243,6 +243,93 @@ int st_rtm_engine_finalize_image(st_rtm_engine* e);
 int st_rtm_engine_reset_image(st_rtm_engine* e);
 int st_rtm_engine_result(st_rtm_engine* e, double* image, double* illumination, double* reflectivity);
 
+/* ---------------------------------------- RTM slice frames and the mmap ring */
+/* The on-disk slice stream of the reference's RTM visualisation path:
+ * RTMEngine::extract_slices / capture_single_slice (rtm/rtm_engine.cpp:
+ * 59-168), LockFreeSnapshotBuffer::serialize_slice + compute_checksum
+ * (rtm/snapshot_buffer.cpp:102-153,207-229) and MmapSnapshotWriter
+ * (rtm/mmap_writer.h:26-124, mmap_writer.cpp). File: a 120-byte header of 15
+ * int64 (magic 0x52544D534E4150, header_size 120, file_size_bytes,
+ * frame_count, write_offset, ring_start, ring_capacity, 8 reserved), then
+ * records [int64 size][frame]; a frame that does not fit before
+ * file_size_bytes restarts the ring at offset 120 (ring_start + 1; the frame
+ * count keeps growing). Frame: a 124-byte packed SliceFrameHeader in a
+ * 128-byte slot (bytes 124..127 are 0 here; the reference copies them from
+ * past its struct), then the forward, adjoint and image-condition slices as
+ * FP64, non-finite values written as 0; checksum over the payload:
+ * s = rotl13(s ^ w) over little-endian 32-bit words; sequence_id 0. */
+enum st_slice_axis { ST_SLICE_X = 0, ST_SLICE_Y = 1, ST_SLICE_Z = 2, ST_SLICE_VOLUME = 3 };
+/* SliceSpec (rtm_engine.h:19-23); index < 0 = the middle plane (n / 2). */
+typedef struct st_slice_spec {
+    int32_t axis;
+    int64_t index;
+    int64_t stride;
+} st_slice_spec;
+/* Field kinds of the capture sources. */
+enum st_field_kind {
+    ST_FIELD_DEVICE_FP32 = 0,   /* the device layout (st_field_layout), FP32 */
+    ST_FIELD_REFERENCE_FP64 = 1 /* the reference layout, FP64, on the device */
+};
+enum st_image_kind { ST_IMAGE_FP32 = 0, ST_IMAGE_FP64 = 1 }; /* nx*ny*nz interior, device */
+
+typedef struct st_mmap_writer st_mmap_writer;
+/* MmapSnapshotWriter::open (mmap_writer.cpp:36-127): creates / truncates the
+ * file to max_bytes and maps it. max_bytes must exceed the 120-byte header. */
+int st_mmap_writer_open(const char* path, int64_t max_bytes, st_mmap_writer** out);
+/* write_frame (mmap_writer.cpp:152-176): appends [size][frame]; 0 on
+ * success. A frame larger than the ring itself is refused (ST_ERR_ARG; the
+ * reference would write past its mapping). */
+int st_mmap_writer_write_frame(st_mmap_writer* w, const uint8_t* frame, int64_t size);
+/* out = {frame_count, write_offset, capacity_bytes, frames_written,
+ *        frames_dropped, total_bytes_written, mmap_cycles} (Stats,
+ *        mmap_writer.h:63-70). */
+int st_mmap_writer_info(st_mmap_writer* w, int64_t out[7]);
+/* close (msync, unmap) and free the handle. */
+int st_mmap_writer_close(st_mmap_writer* w);
+/* read_frame / count_frames (mmap_writer.cpp:241-331): frame `index` counted
+ * from the ring start (out may be NULL to ask the size; cap = out's size);
+ * count = the header's frame_count. */
+int st_mmap_read_frame(const char* path, int64_t index, uint8_t* out, int64_t cap, int64_t* size);
+int st_mmap_count_frames(const char* path, int64_t* count);
+
+/* Bytes of the frame of one spec on an nx*ny*nz interior (0 for VOLUME). */
+int64_t st_slice_frame_bytes(int64_t nx, int64_t ny, int64_t nz, const st_slice_spec* spec);
+/* Serializes the frames of n_specs specs from device fields fwd / adj (kind
+ * field_kind) and the image-condition array ic (kind ic_kind; NULL = zeros)
+ * into `frames` (device memory, the frames back to back in spec order,
+ * VOLUME specs skipped), on `stream`. timestamp = capture_timestamp.
+ * bytes (may be NULL) receives the total. */
+int st_capture_slice_frames(int64_t nx, int64_t ny, int64_t nz, const st_slice_spec* specs, int n_specs,
+                            const void* fwd, const void* adj, int field_kind, const void* ic, int ic_kind,
+                            int64_t timestep, double timestamp, uint8_t* frames, int64_t cap, int64_t* bytes,
+                            void* stream);
+
+/* A slice stream: the capture above into `capacity` pinned host slots, each
+ * copied back asynchronously and appended to an mmap ring by a writer
+ * thread (the roles of LockFreeSnapshotBuffer and the writer's drain
+ * thread, mmap_writer.cpp:199-225). A capture that finds its slot busy is
+ * dropped and counted, as try_enqueue drops (snapshot_buffer.cpp:28-56). */
+typedef struct st_slice_stream st_slice_stream;
+int st_slice_stream_create(const char* path, int64_t max_bytes, int64_t nx, int64_t ny, int64_t nz,
+                           const st_slice_spec* specs, int n_specs, int capacity, int device, st_slice_stream** out);
+/* Captures every spec's frame at this time step (asynchronous on `stream`;
+ * the sources may be overwritten once the stream has passed this point). */
+int st_slice_stream_capture(st_slice_stream* ss, const void* fwd, const void* adj, int field_kind, const void* ic,
+                            int ic_kind, int64_t timestep, void* stream);
+/* Waits until every captured frame is in the file. */
+int st_slice_stream_flush(st_slice_stream* ss);
+/* out = {captured, dropped, written, bytes_written}. */
+int st_slice_stream_stats(st_slice_stream* ss, int64_t out[4]);
+/* Flushes, stops the writer thread and closes the file. */
+int st_slice_stream_destroy(st_slice_stream* ss);
+/* Attaches a slice stream to a solver (the streaming half of
+ * WaveEquationSolver::configure_rtm, solver/wave_equation.cpp:520-560; the
+ * stream is borrowed and must outlive the attachment): every `interval`
+ * steps st_shot_forward captures (current field, zeros, zeros) and the
+ * imaging pass of st_rtm_shot captures (the stored forward snapshot V_t,
+ * the adjoint field, the image so far). ss = NULL or interval <= 0 detaches. */
+int st_solver_set_slice_stream(st_solver* s, st_slice_stream* ss, int interval);
+
 /* ------------------------------------------------------ FWI gradients */
 /* Sets the model from a device FP32 interior velocity (nx*ny*nz, x slowest);
  * the host copy (reference layout, edge-replicated halo) is refreshed too. */

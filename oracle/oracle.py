@@ -97,6 +97,11 @@ class Oracle:
                                        _d]
         L.orc_ray_triplets.restype = C.c_int64
         _u8 = C.POINTER(C.c_uint8)
+        L.orc_slice_checksum.argtypes = [_u8, C.c_size_t]
+        L.orc_slice_checksum.restype = C.c_uint32
+        L.orc_slice_frame.argtypes = [C.c_int, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int, _d, _d, _d,
+                                      C.c_int64, C.c_double, _u8, C.c_int64]
+        L.orc_slice_frame.restype = C.c_int64
         L.orc_sampled_traveltimes.argtypes = [_i64, _d, _d, C.c_int64, _d, _d, _d, _u8, _d, _d]
         L.orc_sampled_gradient.argtypes = [_i64, _d, _d, C.c_int64, _d, _d, _d, _u8, _d, _d, _d, _d]
         L.orc64_repair_field_nan.argtypes = [_d, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int, C.c_double]
@@ -302,6 +307,24 @@ class Oracle:
                                       dp, _p(v, u8), _p(w, _d), _p(vp, _d), _p(res, _d), _p(g, _d))
         return g
 
+    def slice_checksum(self, payload: bytes) -> int:
+        """LockFreeSnapshotBuffer::compute_checksum (snapshot_buffer.cpp:207-229)."""
+        buf = np.frombuffer(bytes(payload), np.uint8).copy()
+        return int(self.lib.orc_slice_checksum(buf.ctypes.data_as(C.POINTER(C.c_uint8)), buf.size))
+
+    def slice_frame(self, axis, index, nx, ny, nz, fwd, adj, ic, timestep, timestamp=0.0) -> bytes:
+        """One serialized slice frame (capture_single_slice + serialize_slice)
+        from reference-layout FP64 fields fwd / adj and the interior ic."""
+        f = np.ascontiguousarray(fwd, np.float64).reshape(-1)
+        a = np.ascontiguousarray(adj, np.float64).reshape(-1)
+        c = np.ascontiguousarray(ic, np.float64).reshape(-1)
+        cap = 128 + 3 * 8 * max(nx, ny) * max(ny, nz)
+        out = np.zeros(cap, np.uint8)
+        n = self.lib.orc_slice_frame(axis, index, nx, ny, nz, 1, _p(f, _d), _p(a, _d), _p(c, _d), timestep,
+                                     float(timestamp), out.ctypes.data_as(C.POINTER(C.c_uint8)), cap)
+        assert n > 0
+        return out[:n].tobytes()
+
     def smooth_gradient(self, g, nx, ny, nz, sigma):
         g = np.ascontiguousarray(g, np.float64).reshape(-1)
         out = np.zeros(nx * ny * nz)
@@ -351,6 +374,55 @@ class Reference:
         L.ref_count_nan_inf.restype = C.c_int64
         L.ref_clamp_field.argtypes = [_d, C.c_int64, C.c_double, C.c_double]
         L.ref_load_config.argtypes = [C.c_char_p, _d]
+        _u8 = C.POINTER(C.c_uint8)
+        L.ref_extract_slices.argtypes = [C.c_int64] * 3 + [C.c_int, _i32, _i64, _d, _d, _d, C.c_int64, C.c_int64,
+                                                           _d, _i64]
+        L.ref_mmap_write.argtypes = [C.c_char_p, C.c_int64, C.c_int, _u8, _i64, _i64]
+        L.ref_mmap_read_frame.argtypes = [C.c_char_p, C.c_int64, _u8, C.c_int64]
+        L.ref_mmap_read_frame.restype = C.c_int64
+        L.ref_mmap_count_frames.argtypes = [C.c_char_p]
+        L.ref_mmap_count_frames.restype = C.c_int64
+
+    def extract_slices(self, nx, ny, nz, specs, fwd, adj, ic, timestep=0):
+        """RTMEngine::extract_slices with a collecting callback: a list of
+        (axis, index, forward, adjoint, ic) with (dim0, dim1) arrays."""
+        axes = np.array([a for a, _ in specs], np.int32)
+        idx = np.array([i for _, i in specs], np.int64)
+        f = np.ascontiguousarray(fwd, np.float64).reshape(-1)
+        a = np.ascontiguousarray(adj, np.float64).reshape(-1)
+        c = np.ascontiguousarray(ic, np.float64).reshape(-1)
+        cap = 3 * len(specs) * max(nx, ny) * max(ny, nz)
+        vals = np.zeros(cap)
+        meta = np.zeros(4 * len(specs), np.int64)
+        k = self.lib.ref_extract_slices(nx, ny, nz, len(specs), _p(axes, _i32), _p(idx, _i64), _p(f, _d), _p(a, _d),
+                                        _p(c, _d), timestep, cap, _p(vals, _d), _p(meta, _i64))
+        assert k >= 0
+        out, o = [], 0
+        for j in range(k):
+            ax, ix, d0, d1 = (int(v) for v in meta[4 * j:4 * j + 4])
+            n = d0 * d1
+            out.append((ax, ix, vals[o:o + n].reshape(d0, d1), vals[o + n:o + 2 * n].reshape(d0, d1),
+                        vals[o + 2 * n:o + 3 * n].reshape(d0, d1)))
+            o += 3 * n
+        return out
+
+    def mmap_write(self, path, max_bytes, frames):
+        """MmapSnapshotWriter open / write_frame per frame / close; returns
+        (accepted, [frames_written, frames_dropped, total_bytes, mmap_cycles])."""
+        data = np.frombuffer(b"".join(frames), np.uint8).copy() if frames else np.zeros(1, np.uint8)
+        sizes = np.array([len(f) for f in frames] or [0], np.int64)
+        stats = np.zeros(4, np.int64)
+        ok = self.lib.ref_mmap_write(os.fsencode(path), max_bytes, len(frames),
+                                     data.ctypes.data_as(C.POINTER(C.c_uint8)), _p(sizes, _i64), _p(stats, _i64))
+        return ok, [int(v) for v in stats]
+
+    def mmap_read_frame(self, path, index, cap=1 << 26):
+        buf = np.zeros(cap, np.uint8)
+        n = self.lib.ref_mmap_read_frame(os.fsencode(path), index, buf.ctypes.data_as(C.POINTER(C.c_uint8)), cap)
+        return None if n < 0 else buf[:n].tobytes()
+
+    def mmap_count_frames(self, path):
+        return int(self.lib.ref_mmap_count_frames(os.fsencode(path)))
 
     def run_steps(self, nx, ny, nz, dx, dy, dz, dt, sw, damp, vel, nsteps, src_xyz, src_w, rec_xyz, adjoint=False):
         npad = (nx + 2) * (ny + 2) * (nz + 2)

@@ -209,3 +209,74 @@ int ref_load_config(const char* path, double* out) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- slices
+#include "rtm/mmap_writer.h"
+
+extern "C" {
+
+// RTMEngine::extract_slices (rtm/rtm_engine.cpp:59-81) with a callback that
+// collects every CapturedSlice: meta[4 * k ..] = axis, index, dim0, dim1;
+// vals = forward, adjoint and ic slices of each capture, concatenated.
+// Returns the number of slices, or -1 when cap is too small.
+int ref_extract_slices(int64_t nx, int64_t ny, int64_t nz, int n_specs, const int* axes, const int64_t* index,
+                       const double* fwd, const double* adj, const double* ic, int64_t timestep, int64_t cap,
+                       double* vals, int64_t* meta) {
+    seismic::RTMEngine eng(nx, ny, nz, 10.0, 10.0, 10.0, 1);
+    std::vector<seismic::SliceSpec> specs;
+    for (int k = 0; k < n_specs; ++k) specs.push_back({static_cast<seismic::SliceAxis>(axes[k]), index[k], 1});
+    eng.set_slice_specs(specs);
+    std::vector<seismic::RTMEngine::CapturedSlice> got;
+    eng.set_slice_callback([&got](const seismic::RTMEngine::CapturedSlice& s) { got.push_back(s); });
+    eng.extract_slices(fwd, adj, ic, ny + 2, nz + 2, timestep);
+    int64_t o = 0;
+    for (size_t k = 0; k < got.size(); ++k) {
+        const auto& s = got[k];
+        meta[4 * k] = static_cast<int64_t>(s.axis);
+        meta[4 * k + 1] = s.index;
+        meta[4 * k + 2] = s.dim0;
+        meta[4 * k + 3] = s.dim1;
+        const int64_t n = s.dim0 * s.dim1;
+        if (o + 3 * n > cap) return -1;
+        std::memcpy(vals + o, s.forward_slice.data(), n * sizeof(double));
+        std::memcpy(vals + o + n, s.adjoint_slice.data(), n * sizeof(double));
+        std::memcpy(vals + o + 2 * n, s.ic_slice.data(), n * sizeof(double));
+        o += 3 * n;
+    }
+    return static_cast<int>(got.size());
+}
+
+// MmapSnapshotWriter (rtm/mmap_writer.cpp:36-183): open(path, max_bytes),
+// write_frame for each of the n frames (data concatenated, sizes[k] bytes),
+// close. stats = frames_written, frames_dropped, total_bytes_written,
+// mmap_cycles; returns the number of frames write_frame accepted.
+int ref_mmap_write(const char* path, int64_t max_bytes, int n, const uint8_t* data, const int64_t* sizes,
+                   int64_t* stats) {
+    seismic::MmapSnapshotWriter w;
+    if (!w.open(path, max_bytes)) return -1;
+    int ok = 0;
+    int64_t o = 0;
+    for (int k = 0; k < n; ++k) {
+        ok += w.write_frame(data + o, sizes[k]) ? 1 : 0;
+        o += sizes[k];
+    }
+    const auto s = w.stats();
+    stats[0] = s.frames_written;
+    stats[1] = s.frames_dropped_buffer_full;
+    stats[2] = s.total_bytes_written;
+    stats[3] = s.mmap_cycles;
+    w.close();
+    return ok;
+}
+
+// MmapSnapshotWriter::read_frame / count_frames (rtm/mmap_writer.cpp:241-331).
+int64_t ref_mmap_read_frame(const char* path, int64_t index, uint8_t* out, int64_t cap) {
+    std::vector<uint8_t> buf;
+    if (!seismic::MmapSnapshotWriter::read_frame(path, index, buf)) return -1;
+    if (static_cast<int64_t>(buf.size()) > cap) return -2;
+    std::memcpy(out, buf.data(), buf.size());
+    return static_cast<int64_t>(buf.size());
+}
+int64_t ref_mmap_count_frames(const char* path) { return seismic::MmapSnapshotWriter::count_frames(path); }
+
+}  // extern "C"

@@ -684,3 +684,94 @@ void orc_sampled_gradient(const int64_t n[3], const double d[3], const double o[
         }
     }
 }
+
+/* ------------------------------------------------------- slice frames */
+/* RTMEngine::capture_single_slice (rtm/rtm_engine.cpp:83-168): the slice of
+ * the halo-padded forward and adjoint fields (pitches nyp = ny + 2hw,
+ * nzp = nz + 2hw) at interior index `index` along `axis` (0 = X: dim0 = ny,
+ * dim1 = nz; 1 = Y: nx, nz; 2 = Z: nx, ny), non-finite values read as 0; the
+ * image-condition slice is the first dim0 * dim1 values of `ic` (the
+ * reference indexes ic with the slice's own 2-D index). Then
+ * LockFreeSnapshotBuffer::serialize_slice (rtm/snapshot_buffer.cpp:102-153):
+ * a 124-byte packed SliceFrameHeader in a 128-byte slot (the reference
+ * copies 128 bytes from the 124-byte struct; bytes 124..127 are written 0
+ * here), then the three FP64 slices; checksum (:207-229) over the payload:
+ * s = rotl13(s ^ w) over little-endian 32-bit words, the trailing bytes
+ * XORed in unrotated; sequence_id 0. Returns the frame size, or -1 when cap
+ * is too small or the axis is not X, Y or Z. Parity of the serializer is
+ * against this restatement of the source (the reference's
+ * snapshot_buffer.cpp does not compile); the slice values are pinned to the
+ * reference's RTMEngine::extract_slices. */
+uint32_t orc_slice_checksum(const uint8_t* data, size_t size) {
+    uint32_t sum = 0;
+    const size_t n32 = size / 4, rest = size % 4;
+    for (size_t i = 0; i < n32; ++i) {
+        uint32_t w;
+        memcpy(&w, data + 4 * i, 4);
+        sum ^= w;
+        sum = (sum << 13) | (sum >> 19);
+    }
+    if (rest) {
+        uint32_t r = 0;
+        for (size_t i = 0; i < rest; ++i) r |= (uint32_t)data[4 * n32 + i] << (8 * i);
+        sum ^= r;
+    }
+    return sum;
+}
+
+static void put64(uint8_t* p, int64_t v) { memcpy(p, &v, 8); }
+
+int64_t orc_slice_frame(int axis, int64_t index, int64_t nx, int64_t ny, int64_t nz, int hw, const double* fwd,
+                        const double* adj, const double* ic, int64_t timestep, double timestamp, uint8_t* out,
+                        int64_t cap) {
+    int64_t d0, d1;
+    if (axis == 0) { d0 = ny; d1 = nz; }
+    else if (axis == 1) { d0 = nx; d1 = nz; }
+    else if (axis == 2) { d0 = nx; d1 = ny; }
+    else return -1;
+    const int64_t n = d0 * d1, bytes = n * 8, size = 128 + 3 * bytes;
+    if (size > cap) return -1;
+    const int64_t nyp = ny + 2 * hw, nzp = nz + 2 * hw;
+    double* f = (double*)malloc((size_t)bytes);
+    double* a = (double*)malloc((size_t)bytes);
+    double* c = (double*)malloc((size_t)bytes);
+    for (int64_t i = 0; i < d0; ++i)
+        for (int64_t j = 0; j < d1; ++j) {
+            int64_t ix, iy, iz;
+            if (axis == 0) { ix = index; iy = i; iz = j; }
+            else if (axis == 1) { ix = i; iy = index; iz = j; }
+            else { ix = i; iy = j; iz = index; }
+            const int64_t src = (ix + hw) * nyp * nzp + (iy + hw) * nzp + (iz + hw);
+            const int64_t dst = i * d1 + j;
+            f[dst] = isfinite(fwd[src]) ? fwd[src] : 0.0;
+            a[dst] = isfinite(adj[src]) ? adj[src] : 0.0;
+            c[dst] = isfinite(ic[dst]) ? ic[dst] : 0.0;
+        }
+    memset(out, 0, 128);
+    const uint64_t magic = 0x534C494345303031ULL;
+    const int32_t ax = axis;
+    memcpy(out + 0, &magic, 8);
+    put64(out + 8, timestep);
+    memcpy(out + 16, &ax, 4);
+    put64(out + 20, index);
+    put64(out + 28, d0);
+    put64(out + 36, d1);
+    put64(out + 44, size);
+    put64(out + 52, 128);
+    put64(out + 60, 128 + bytes);
+    put64(out + 68, 128 + 2 * bytes);
+    put64(out + 76, bytes);
+    put64(out + 84, bytes);
+    put64(out + 92, bytes);
+    memcpy(out + 100, &timestamp, 8);
+    put64(out + 108, 0);
+    memcpy(out + 128, f, (size_t)bytes);
+    memcpy(out + 128 + bytes, a, (size_t)bytes);
+    memcpy(out + 128 + 2 * bytes, c, (size_t)bytes);
+    const uint32_t cs = orc_slice_checksum(out + 128, (size_t)(3 * bytes));
+    memcpy(out + 116, &cs, 4);
+    free(f);
+    free(a);
+    free(c);
+    return size;
+}
