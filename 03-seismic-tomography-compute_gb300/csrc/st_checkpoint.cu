@@ -371,6 +371,7 @@ extern "C" int st_rtm_shot_checkpointed(st_solver* s, const st_shot* shot, const
                                         int segment_steps, int max_slots, float* image, float* illum, float* refl,
                                         st_checkpoint_stats* stats) {
     ST_CHECK(s && shot && image && illum, ST_ERR_ARG, "null argument");
+    ST_TRY(require_no_terrain(s));
     ST_CHECK(snap_kind >= ST_SNAP_BF16 && snap_kind <= ST_SNAP_FP32, ST_ERR_ARG,
              "RTM snapshot kind must be BF16, FP16 or FP32 (got %d)", snap_kind);
     const int64_t nrec = shot->rec.nx * shot->rec.ny;

@@ -171,6 +171,7 @@ int gradient_scratch(st_solver* s, const st_shot* shot, int snap_kind, GradScrat
 
 int check_grad_args(st_solver* s, const st_shot* shot, int snap_kind) {
     ST_CHECK(s && shot, ST_ERR_ARG, "null argument");
+    ST_TRY(require_no_terrain(s));
     ST_CHECK(snap_kind >= ST_SNAP_BF16 && snap_kind <= ST_SNAP_FP32, ST_ERR_ARG,
              "gradient snapshot kind must be BF16, FP16 or FP32 (got %d)", snap_kind);
     ST_CHECK((s->L.nz * snap_bytes(snap_kind)) % 16 == 0, ST_ERR_UNSUPPORTED,

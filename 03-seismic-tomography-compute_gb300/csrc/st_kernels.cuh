@@ -33,6 +33,8 @@ struct StepArgs {
     unsigned* flags;         // FLAG_GUARD / FLAG_TIMEOUT
     unsigned long long timeout_ns;
     int stable_sponge;       // 1: out = D * (update + forcing) (damped new field), 0: the reference rule
+    const int* zlim;         // terrain: per (x, y) column (x * ny + y), points with z < zlim are set to 0
+                             // after the update (free surface / seafloor masks), or null
 };
 
 // Sponge factor of interior point (ix, iy, iz): D(d) for the distance d to the

@@ -219,6 +219,7 @@ int st_shot_forward(st_solver* s, const st_shot* shot, float* seis, int snap_kin
 
 int st_shot_adjoint(st_solver* s, const st_shot* shot, const float* data, float* src_trace) {
     ST_CHECK(s && shot && src_trace, ST_ERR_ARG, "null argument");
+    ST_TRY(require_no_terrain(s));
     const int64_t nrec = shot->rec.nx * shot->rec.ny;
     ST_CHECK(nrec == 0 || data, ST_ERR_ARG, "receiver data missing");
     ST_CHECK(shot->src_ix >= 0 && shot->src_ix < s->L.nx && shot->src_iy >= 0 && shot->src_iy < s->L.ny &&
@@ -236,6 +237,7 @@ int st_shot_adjoint(st_solver* s, const st_shot* shot, const float* data, float*
 int st_rtm_shot(st_solver* s, const st_shot* shot, const float* data, int snap_kind, void* snaps,
                 unsigned* snap_amax, float* image, float* illum, float* refl) {
     ST_CHECK(s && shot && image && illum, ST_ERR_ARG, "null argument");
+    ST_TRY(require_no_terrain(s));
     ST_CHECK(snap_kind >= ST_SNAP_BF16 && snap_kind <= ST_SNAP_FP32, ST_ERR_ARG,
              "RTM snapshot kind must be BF16, FP16 or FP32 (got %d)", snap_kind);
     const int64_t nrec = shot->rec.nx * shot->rec.ny;
@@ -267,6 +269,7 @@ int st_rtm_shot(st_solver* s, const st_shot* shot, const float* data, int snap_k
 int st_rtm_shot_host(st_solver* s, const double* vp, int64_t vp_count, const st_shot* shot, const float* data_host,
                      int snap_kind, double* image_host, double* illum_host, double* refl_host) {
     ST_CHECK(s && shot, ST_ERR_ARG, "null argument");
+    ST_TRY(require_no_terrain(s));
     ST_CUDA(cudaSetDevice(s->device));
     if (vp) ST_TRY(st_solver_set_velocity_field(s, vp, vp_count));
     const int64_t nrec = shot->rec.nx * shot->rec.ny;

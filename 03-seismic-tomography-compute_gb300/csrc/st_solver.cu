@@ -205,6 +205,7 @@ StepArgs base_args(st_solver* s, float* out) {
     a.flags = s->flags;
     a.rsx = a.rsy = 1;
     a.stable_sponge = s->sponge_mode == ST_SPONGE_STABLE;
+    a.zlim = s->zlim;
     return a;
 }
 
@@ -425,6 +426,7 @@ int st_solver_destroy(st_solver* s) {
     cudaFree(s->aux_buf);
     cudaFree(s->data_buf);
     cudaFree(s->ckpt_buf);
+    cudaFree(s->zlim);
     for (int k = 0; k < 3; ++k)
         if (s->ev[k]) cudaEventDestroy(s->ev[k]);
     if (s->stream) cudaStreamDestroy(s->stream);

@@ -87,6 +87,7 @@ struct st_solver {
     void* ckpt_buf = nullptr;       // checkpointed adjoint: working set, state slots, segment snapshots
     size_t ckpt_cap = 0;
     int sponge_mode = ST_SPONGE_REFERENCE;  // ST_SPONGE_STABLE: damp the new field (Cerjan form)
+    int* zlim = nullptr;                // terrain: per-column z limits (st_solver_set_terrain), or null
     st_slice_stream* slices = nullptr;  // RTM slice stream (configure_rtm), borrowed
     int slice_interval = 0;             // capture every slice_interval steps
     // phase boundaries of the last shot-level call, recorded on `stream`:
@@ -125,4 +126,11 @@ int launch_rec_force(st_solver* s, const st_receiver_grid& R, const float* row);
 int checkpointed_adjoint(st_solver* s, const st_shot* shot, int snap_kind, int segment_steps, int max_slots, int epi,
                          const float* force, float* image, float* illum, float* grad_c, float* seis,
                          const std::function<int()>& before_backward, st_checkpoint_stats* stats);
+// The exact-adjoint entry points transpose the unmasked step, so they refuse
+// while a terrain (st_solver_set_terrain) is attached.
+inline int require_no_terrain(const st_solver* s) {
+    ST_CHECK(!s->zlim, ST_ERR_UNSUPPORTED, "exact-adjoint paths are unavailable while a terrain is attached");
+    return ST_OK;
+}
+
 }  // namespace stg

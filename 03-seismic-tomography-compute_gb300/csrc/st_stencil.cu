@@ -61,9 +61,12 @@ constexpr int SM_SMEM = 232448;               // shared memory per SM (227 KB us
 constexpr unsigned FULL = 0xffffffffu;
 
 // EPI_IMAGE_T: imaging with its operands (snapshot, image, illumination tiles)
-// staged through the TMA ring instead of loaded at use.
-enum Epilogue : int { EPI_NONE = 0, EPI_IMAGE = 1, EPI_GRAD = 2, EPI_IMAGE_T = 3 };
+// staged through the TMA ring instead of loaded at use. EPI_MASK: a forward
+// step that also applies the terrain's per-column z limits (StepArgs::zlim);
+// kept apart from EPI_NONE so the plain forward step carries no mask code.
+enum Epilogue : int { EPI_NONE = 0, EPI_IMAGE = 1, EPI_GRAD = 2, EPI_IMAGE_T = 3, EPI_MASK = 4 };
 constexpr bool is_image(int e) { return e == EPI_IMAGE || e == EPI_IMAGE_T; }
+constexpr bool is_forward(int e) { return e == EPI_NONE || e == EPI_MASK; }
 
 // Per-variant tiling. Forward variants give each thread 2 adjacent rows
 // (32-row tiles, 2 CTAs per SM): fewer instructions per point. The imaging
@@ -75,7 +78,7 @@ constexpr bool is_image(int e) { return e == EPI_IMAGE || e == EPI_IMAGE_T; }
 // of each plane to the stage (3-deep ring).
 template <int EPI, int SNAP_IN>
 struct Geo {
-    static constexpr int RPT = EPI == EPI_NONE ? 2 : 1;  // rows per thread
+    static constexpr int RPT = is_forward(EPI) ? 2 : 1;  // rows per thread
     static constexpr int TYV = 16 * RPT;                 // tile rows
     static constexpr int CUR_H = TYV + 2;
     static constexpr int CUR_BYTES = CUR_W * CUR_H * 4;
@@ -273,6 +276,13 @@ __device__ __forceinline__ void process_row(const StepArgs& a, const RowCtx& R, 
 #pragma unroll
         for (int k = 0; k < 4; ++k) res[k] *= D[k];
     }
+    if constexpr (EPI == EPI_MASK) {  // terrain masks: the column's points above its z limit hold 0
+        const long long col = (long long)x * a.ny + R.iy;
+        const int zl = a.zlim[col] - (int)(cbase - col * a.nz);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < zl) res[k] = 0.0f;
+    }
     if (rec_here && a.seis_row) {
 #pragma unroll
         for (int k = 0; k < 4; ++k)
@@ -403,8 +413,8 @@ __global__ void __launch_bounds__(NTHREADS, (Geo<EPI, SNAP_IN>::MINB))
         snap_inv = m > 0.0f ? SNAP_QMAX / m : 0.0f;
     }
     float snap_scale = 1.0f;
-    const bool vec_acc = EPI != EPI_NONE && (a.nz & 3) == 0 && zvalid == 4;
-    if constexpr (EPI != EPI_NONE) snap_scale = __uint_as_float(*a.amax_in) / SNAP_QMAX;
+    const bool vec_acc = !is_forward(EPI) && (a.nz & 3) == 0 && zvalid == 4;
+    if constexpr (!is_forward(EPI)) snap_scale = __uint_as_float(*a.amax_in) / SNAP_QMAX;
 
     const bool tab_smem = a.sw <= DTAB_MAX;
     if (tab_smem)
@@ -663,7 +673,7 @@ int launch_variant(const Layout& L, const FieldMaps& mcur, const FieldMaps& mpre
     // The forward variants run best as one wave of long x-chunks; the imaging
     // and gradient variants (one row per thread, more resident CTAs) keep more
     // loads in flight with at least four waves of shorter chunks.
-    const int chunks = fd_step_grid_chunks(L, G::TYV, G::MINB, EPI == EPI_NONE ? 1 : 4);
+    const int chunks = fd_step_grid_chunks(L, G::TYV, G::MINB, is_forward(EPI) ? 1 : 4);
     a.x_chunk = (int)((L.nx + chunks - 1) / chunks);
     const int nch = (int)((L.nx + a.x_chunk - 1) / a.x_chunk);
     dim3 grid((unsigned)((L.nz + TZ - 1) / TZ), (unsigned)((L.ny + G::TYV - 1) / G::TYV), (unsigned)nch);
@@ -896,6 +906,7 @@ int launch_fd_step(const Layout& L, const FieldMaps& mcur, const FieldMaps& mpre
     a.NZP = (int)L.NZP;
     a.plane = L.plane;
     if (a.timeout_ns == 0) a.timeout_ns = 2000000000ull;
+    ST_CHECK(!a.zlim || epi == EPI_NONE, ST_ERR_UNSUPPORTED, "terrain limits apply to plain forward steps only");
     const CUtensorMap& ms = msnap ? *msnap : mc.ctr[0];  // unused unless epi == gradient
     if (epi == EPI_IMAGE && imaps) {
         // operands staged by TMA: snapshot store map (box {64, 16}), image and illumination maps
@@ -929,6 +940,15 @@ int launch_fd_step(const Layout& L, const FieldMaps& mcur, const FieldMaps& mpre
             case SNAP_FP16: return launch_variant<SNAP_NONE, SNAP_FP16, EPI_GRAD>(L, mcur, mprev, mc, ms, a, st);
             case SNAP_FP32: return launch_variant<SNAP_NONE, SNAP_FP32, EPI_GRAD>(L, mcur, mprev, mc, ms, a, st);
             default: ST_CHECK(false, ST_ERR_ARG, "gradient step needs a snapshot kind");
+        }
+    }
+    if (a.zlim) {
+        switch (snap_out) {
+            case SNAP_NONE: return launch_variant<SNAP_NONE, SNAP_NONE, EPI_MASK>(L, mcur, mprev, mc, ms, a, st);
+            case SNAP_BF16: return launch_variant<SNAP_BF16, SNAP_NONE, EPI_MASK>(L, mcur, mprev, mc, ms, a, st);
+            case SNAP_FP16: return launch_variant<SNAP_FP16, SNAP_NONE, EPI_MASK>(L, mcur, mprev, mc, ms, a, st);
+            case SNAP_FP32: return launch_variant<SNAP_FP32, SNAP_NONE, EPI_MASK>(L, mcur, mprev, mc, ms, a, st);
+            default: ST_CHECK(false, ST_ERR_ARG, "bad snapshot kind %d", snap_out);
         }
     }
     switch (snap_out) {

@@ -19,6 +19,7 @@ from .config import (  # noqa: F401
 )
 from .rtm import RTMConfig, RTMEngine, RTMImageCondition, SliceAxis, SliceSpec  # noqa: F401
 from .rays import SampledRays  # noqa: F401
+from .terrain import BathymetryPoint, TerrainBoundary, generate_bathymetry  # noqa: F401
 from .slices import (  # noqa: F401
     CapturedSlice, MmapSnapshotWriter, MmapStats, SliceStream, capture_slice_frames, deserialize_slice,
 )

@@ -26,6 +26,7 @@ ST_ERR_UNSUPPORTED = -6
 ST_FIELD_CURRENT, ST_FIELD_PREVIOUS, ST_FIELD_NEXT, ST_FIELD_VELOCITY = 0, 1, 2, 3
 ST_SNAP_NONE, ST_SNAP_BF16, ST_SNAP_FP16, ST_SNAP_FP32 = 0, 1, 2, 3
 ST_SPONGE_REFERENCE, ST_SPONGE_STABLE = 0, 1
+ST_TERRAIN_FREE_SURFACE, ST_TERRAIN_SEAFLOOR = 1, 2
 
 
 class SeismicError(RuntimeError):
@@ -76,6 +77,10 @@ class ShotC(C.Structure):
 
 class SliceSpecC(C.Structure):
     _fields_ = [("axis", C.c_int32), ("index", C.c_int64), ("stride", C.c_int64)]
+
+
+class BathymetryPointC(C.Structure):
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("depth", C.c_double)]
 
 
 class RayModelC(C.Structure):
@@ -190,6 +195,20 @@ SIGNATURES = {
     "st_slice_stream_stats": [_vp, _i64],
     "st_slice_stream_destroy": [_vp],
     "st_solver_set_slice_stream": [_vp, _vp, C.c_int],
+    "st_terrain_create": [C.POINTER(GridParams), C.c_double, C.c_int, C.POINTER(_vp)],
+    "st_terrain_destroy": [_vp],
+    "st_terrain_set_bathymetry_data": [_vp, C.POINTER(BathymetryPointC), C.c_int64],
+    "st_terrain_generate_synthetic_bathymetry": [_vp, C.c_double, C.c_double],
+    "st_terrain_bathymetry": [_vp, _d],
+    "st_terrain_seafloor": [_vp, C.c_int64, C.c_int64, _d, _i64],
+    "st_terrain_update_velocity_mask": [_vp, _vp, C.c_int, C.c_double, C.c_double],
+    "st_terrain_build_boundary_mask": [_vp, _vp, C.c_int],
+    "st_terrain_apply_free_surface_bc": [_vp, _vp, C.c_int],
+    "st_terrain_apply_seafloor_bc": [_vp, _vp, C.c_int],
+    "st_terrain_apply_absorbing_bc": [_vp, _vp, C.c_int, C.c_int, C.c_double],
+    "st_generate_bathymetry": [C.c_int64, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                               C.c_double, C.c_double, _d],
+    "st_solver_set_terrain": [_vp, _vp, C.c_int],
     "st_csr_get": [_vp, _i64, _i64, _d],
     "st_csr_device_arrays": [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)],
     "st_csr_stream": [_vp, C.POINTER(_vp)],

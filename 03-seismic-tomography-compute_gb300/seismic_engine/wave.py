@@ -262,6 +262,17 @@ class WaveEquationSolver:
         return FaultStats(s.total_nan_count, s.total_inf_count, s.cells_repaired, s.timesteps_recovered,
                           s.global_abort_count)
 
+    # ---- terrain-aware propagation (GB300 addition)
+    def set_terrain(self, terrain, free_surface: bool = True, seafloor: bool = True):
+        """Attach a TerrainBoundary: every step then zeroes, in each (x, y)
+        column, the points above the free-surface plane and / or the seafloor
+        index, right after the update (fused into the stencil). The limits
+        are copied; terrain=None detaches. The exact-adjoint entry points
+        refuse while a terrain is attached."""
+        flags = (_lib.ST_TERRAIN_FREE_SURFACE if free_surface else 0) | (_lib.ST_TERRAIN_SEAFLOOR if seafloor else 0)
+        call("st_solver_set_terrain", self._h, terrain.handle if terrain is not None else None,
+             flags if terrain is not None else 0)
+
     # ---- RTM slice streaming (wave_equation.cpp:510-575)
     def configure_rtm(self, cfg):
         """WaveEquationSolver::configure_rtm: with enable_rtm and

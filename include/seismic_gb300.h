@@ -243,6 +243,54 @@ int st_rtm_engine_finalize_image(st_rtm_engine* e);
 int st_rtm_engine_reset_image(st_rtm_engine* e);
 int st_rtm_engine_result(st_rtm_engine* e, double* image, double* illumination, double* reflectivity);
 
+/* ------------------------------------------------ seismic::TerrainBoundary */
+/* Irregular seafloor terrain (solver/boundary.h:9-52, boundary.cpp). The
+ * bathymetry grid (nx*ny depths, column (ix, iy) at ix*ny + iy) is built on
+ * the host; the field operations run on the GPU on the reference layout
+ * (halo = the grid's halo_width), FP64, host (on_device = 0: copied in and
+ * out) or device pointers (1: on the terrain's own stream, synchronous). */
+typedef struct st_bathymetry_point { double x, y, depth; } st_bathymetry_point; /* BathymetryPoint */
+typedef struct st_terrain st_terrain;
+/* TerrainBoundary(grid, water_depth) (boundary.cpp:8-14): flat bathymetry. */
+int st_terrain_create(const st_grid_params* grid, double water_depth, int device, st_terrain** out);
+int st_terrain_destroy(st_terrain* t);
+/* set_bathymetry_data (boundary.cpp:16-32): each point sets its cell's depth. */
+int st_terrain_set_bathymetry_data(st_terrain* t, const st_bathymetry_point* points, int64_t n);
+/* generate_synthetic_bathymetry (boundary.cpp:34-57). */
+int st_terrain_generate_synthetic_bathymetry(st_terrain* t, double gradient, double roughness);
+/* bathymetry() (boundary.h:38): nx*ny depths. */
+int st_terrain_bathymetry(st_terrain* t, double* out);
+/* seafloor_depth / seafloor_index (boundary.cpp:71-86); either output may be NULL. */
+int st_terrain_seafloor(st_terrain* t, int64_t gx, int64_t gy, double* depth, int64_t* index);
+/* update_velocity_mask (boundary.cpp:158-186) on a padded velocity. */
+int st_terrain_update_velocity_mask(st_terrain* t, double* velocity, int on_device, double water_vp,
+                                    double sediment_vp);
+/* build_boundary_mask (boundary.cpp:188-214): 1 subsurface, 2 water, 0 halo. */
+int st_terrain_build_boundary_mask(st_terrain* t, uint8_t* mask, int on_device);
+/* apply_free_surface_bc / apply_seafloor_bc / apply_absorbing_bc
+ * (boundary.cpp:88-156), in place, with the reference's index ranges (the
+ * seafloor range of a column whose seafloor lies below the grid runs on
+ * into the following cells, bounded by the array). */
+int st_terrain_apply_free_surface_bc(st_terrain* t, double* field, int on_device);
+int st_terrain_apply_seafloor_bc(st_terrain* t, double* field, int on_device);
+int st_terrain_apply_absorbing_bc(st_terrain* t, double* field, int on_device, int sponge_width, double damping);
+/* generate_bathymetry (pybind/bindings.cpp:255-270): nx*ny synthetic depths. */
+int st_generate_bathymetry(int64_t nx, int64_t ny, double dx, double dy, double origin_x, double origin_y,
+                           double water_depth, double gradient, double roughness, double* out);
+/* Terrain-aware propagation (no reference counterpart: the reference never
+ * applies its terrain while stepping). With a terrain attached every
+ * propagator step sets the points of each (x, y) column above its z limit
+ * to 0 right after the update, before receivers sample it: limit 1 for
+ * ST_TERRAIN_FREE_SURFACE (the apply_free_surface_bc plane), the seafloor
+ * index for ST_TERRAIN_SEAFLOOR (the apply_seafloor_bc range, clamped to the
+ * column), the larger of the two for both. The limits are fused into the
+ * stencil kernel (one load per row). The exact-adjoint entry points
+ * (st_shot_adjoint, st_rtm_shot*, st_shot_gradient*, st_fwi_gradient*)
+ * return ST_ERR_UNSUPPORTED while a terrain is attached. t = NULL or
+ * flags = 0 detaches. */
+enum st_terrain_flags { ST_TERRAIN_FREE_SURFACE = 1, ST_TERRAIN_SEAFLOOR = 2 };
+int st_solver_set_terrain(st_solver* s, st_terrain* t, int flags);
+
 /* ---------------------------------------- RTM slice frames and the mmap ring */
 /* The on-disk slice stream of the reference's RTM visualisation path:
  * RTMEngine::extract_slices / capture_single_slice (rtm/rtm_engine.cpp:

@@ -27,7 +27,7 @@ mkdir -p "$OUT"
 g++ -std=c++17 -O3 -ffast-math -fno-finite-math-only $ARCHFLAGS -fPIC -shared -w \
   -include functional -I"$HERE/mpi_stub" -I"$SRC" \
   "$SRC/core/grid.cpp" "$SRC/core/mpi_context.cpp" "$SRC/core/config.cpp" \
-  "$SRC/core/fault_tolerance.cpp" "$SRC/solver/wave_equation.cpp" \
+  "$SRC/core/fault_tolerance.cpp" "$SRC/solver/wave_equation.cpp" "$SRC/solver/boundary.cpp" \
   "$SRC/rtm/rtm_engine.cpp" "$SRC/rtm/mmap_writer.cpp" "$SRC/sparse/csr_matrix.cpp" \
   "$HERE/ref_stubs.cpp" "$HERE/ref_harness.cpp" \
   -o "$OUT/libseismic_ref.so.tmp" -Wl,--no-undefined -lpthread

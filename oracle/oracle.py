@@ -380,6 +380,11 @@ class Reference:
         L.ref_mmap_write.argtypes = [C.c_char_p, C.c_int64, C.c_int, _u8, _i64, _i64]
         L.ref_mmap_read_frame.argtypes = [C.c_char_p, C.c_int64, _u8, C.c_int64]
         L.ref_mmap_read_frame.restype = C.c_int64
+        L.ref_terrain.argtypes = ([C.c_int64] * 3 + [C.c_double] * 6 + [C.c_int, C.c_double, C.c_int, C.c_double,
+                                                                        C.c_double, C.c_int, _d, _d, _i64,
+                                                                        C.c_double, C.c_double, _d,
+                                                                        C.POINTER(C.c_uint8), _d, _d, _d, C.c_int,
+                                                                        C.c_double])
         L.ref_mmap_count_frames.argtypes = [C.c_char_p]
         L.ref_mmap_count_frames.restype = C.c_int64
 
@@ -405,6 +410,25 @@ class Reference:
                         vals[o + 2 * n:o + 3 * n].reshape(d0, d1)))
             o += 3 * n
         return out
+
+    def terrain(self, n, d, origin, water_depth, synthetic=False, gradient=0.0, roughness=0.0, points=None,
+                water_vp=1500.0, sediment_vp=3000.0, velocity=None, fields=None, sponge_width=3, damping=0.5):
+        """TerrainBoundary on a single-rank grid (halo 1): returns dict(bathy,
+        sf_index, velocity, mask, free, seafloor, absorbing)."""
+        nx, ny, nz = (int(v) for v in n)
+        npad = (nx + 2) * (ny + 2) * (nz + 2)
+        pts = np.ascontiguousarray(points if points is not None else np.zeros((0, 3)), np.float64).reshape(-1)
+        bathy = np.zeros(nx * ny)
+        sfi = np.zeros(nx * ny, np.int64)
+        vel = np.array(velocity if velocity is not None else np.zeros(npad), np.float64, copy=True).reshape(-1)
+        mask = np.zeros(npad, np.uint8)
+        f = [np.array(fields[k], np.float64, copy=True).reshape(-1) for k in range(3)]
+        self.lib.ref_terrain(nx, ny, nz, *(float(v) for v in d), *(float(v) for v in origin), 1, float(water_depth),
+                             int(synthetic), float(gradient), float(roughness), pts.size // 3, _p(pts, _d),
+                             _p(bathy, _d), _p(sfi, _i64), float(water_vp), float(sediment_vp), _p(vel, _d),
+                             mask.ctypes.data_as(C.POINTER(C.c_uint8)), _p(f[0], _d), _p(f[1], _d), _p(f[2], _d),
+                             int(sponge_width), float(damping))
+        return dict(bathy=bathy, sf_index=sfi, velocity=vel, mask=mask, free=f[0], seafloor=f[1], absorbing=f[2])
 
     def mmap_write(self, path, max_bytes, frames):
         """MmapSnapshotWriter open / write_frame per frame / close; returns

@@ -280,3 +280,50 @@ int64_t ref_mmap_read_frame(const char* path, int64_t index, uint8_t* out, int64
 int64_t ref_mmap_count_frames(const char* path) { return seismic::MmapSnapshotWriter::count_frames(path); }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- terrain
+#include "solver/boundary.h"
+
+extern "C" {
+
+// TerrainBoundary (solver/boundary.cpp) on a single-rank grid with halo hw:
+// the bathymetry (flat, generate_synthetic_bathymetry(gradient, roughness)
+// when synthetic, then set_bathymetry_data(points) for n_points (x, y, depth)
+// triples), seafloor_index per column, update_velocity_mask on `velocity`,
+// build_boundary_mask into `mask`, and apply_free_surface_bc /
+// apply_seafloor_bc / apply_absorbing_bc on three halo-padded fields (in
+// place). Every array in the reference's (nx+2hw)(ny+2hw)(nz+2hw) layout.
+int ref_terrain(int64_t nx, int64_t ny, int64_t nz, double dx, double dy, double dz, double ox, double oy,
+                double oz, int hw, double water_depth, int synthetic, double gradient, double roughness,
+                int n_points, const double* points, double* bathy, int64_t* sf_index, double water_vp,
+                double sediment_vp, double* velocity, uint8_t* mask, double* f_free, double* f_sea, double* f_abs,
+                int sponge_width, double damping) {
+    seismic::GridParams p{nx, ny, nz, dx, dy, dz, ox, oy, oz, hw};
+    const int coords[3] = {0, 0, 0}, dims[3] = {1, 1, 1};
+    seismic::CartesianGrid grid(p, coords, dims);
+    seismic::TerrainBoundary tb(grid, water_depth);
+    if (synthetic) tb.generate_synthetic_bathymetry(gradient, roughness);
+    std::vector<seismic::BathymetryPoint> pts;
+    for (int k = 0; k < n_points; ++k) pts.push_back({points[3 * k], points[3 * k + 1], points[3 * k + 2]});
+    if (n_points) tb.set_bathymetry_data(pts);
+    std::memcpy(bathy, tb.bathymetry().data(), nx * ny * sizeof(double));
+    for (int64_t ix = 0; ix < nx; ++ix)
+        for (int64_t iy = 0; iy < ny; ++iy) sf_index[ix * ny + iy] = tb.seafloor_index(ix, iy);
+    const auto& loc = grid.local();
+    const int64_t n = loc.total_cells_with_halo;
+    std::vector<double> v(velocity, velocity + n);
+    tb.update_velocity_mask(v, water_vp, sediment_vp);
+    std::memcpy(velocity, v.data(), n * sizeof(double));
+    tb.build_boundary_mask(loc, hw);
+    std::memcpy(mask, tb.mask().data(), n);
+    std::vector<double> a(f_free, f_free + n), b(f_sea, f_sea + n), c(f_abs, f_abs + n);
+    tb.apply_free_surface_bc(a, loc, hw);
+    tb.apply_seafloor_bc(b, loc, hw);
+    tb.apply_absorbing_bc(c, loc, hw, sponge_width, damping);
+    std::memcpy(f_free, a.data(), n * sizeof(double));
+    std::memcpy(f_sea, b.data(), n * sizeof(double));
+    std::memcpy(f_abs, c.data(), n * sizeof(double));
+    return 0;
+}
+
+}  // extern "C"
