@@ -93,6 +93,7 @@ void set_receivers_args(StepArgs& a, const st_receiver_grid& R) {
 double cfl_damp(st_solver* s) {
     // the coefficient array already carries damp^2; recover damp from it is
     // not possible per point, so recompute the reference rule on the host copy
+    if (ensure_vel_host(s) != ST_OK) return 1.0;  // (a failed download reports through the next CUDA call)
     double vmax = 0.0;
     for (double v : s->vel_host)
         if (std::isfinite(v) && v > vmax) vmax = v;
@@ -212,6 +213,7 @@ int st_solver_set_velocity_device(st_solver* s, const float* vel) {
             for (long long zr = 0; zr < NZh; ++zr) row[zr] = src[clampi(zr - 1, nz - 1)];
         }
     }
+    s->vel_host_valid = true;
     const double damp = cfl_damp(s);
     vel_interior_to_coeff_kernel<<<nblocks(L.elems), 256, 0, s->stream>>>(vel, s->c, L,
                                                                            s->cfg.dt * s->cfg.dt * damp * damp);

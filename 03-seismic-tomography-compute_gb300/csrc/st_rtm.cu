@@ -271,7 +271,7 @@ int st_rtm_shot_host(st_solver* s, const double* vp, int64_t vp_count, const st_
     ST_CHECK(s && shot, ST_ERR_ARG, "null argument");
     ST_TRY(require_no_terrain(s));
     ST_CUDA(cudaSetDevice(s->device));
-    if (vp) ST_TRY(st_solver_set_velocity_field(s, vp, vp_count));
+    if (vp) ST_TRY(vp_count >= ref_elems(s) ? upload_velocity(s, vp) : st_solver_set_velocity_field(s, vp, vp_count));
     const int64_t nrec = shot->rec.nx * shot->rec.ny;
     const size_t npts = (size_t)(s->L.nx * s->L.ny * s->L.nz);
     const size_t dbytes = (size_t)nrec * (size_t)std::max(shot->nt, 0) * sizeof(float);

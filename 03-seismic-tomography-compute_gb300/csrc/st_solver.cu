@@ -143,6 +143,17 @@ int ensure_staging(st_solver* s) {
     return ST_OK;
 }
 
+// Brings the host copy of the model up to date after a device-side upload.
+int ensure_vel_host(st_solver* s) {
+    if (s->vel_host_valid) return ST_OK;
+    ST_CUDA(cudaSetDevice(s->device));
+    ST_CUDA(cudaMemcpyAsync(s->vel_host.data(), s->vel_dev, (size_t)ref_elems(s) * sizeof(double),
+                            cudaMemcpyDeviceToHost, s->stream));
+    ST_CUDA(cudaStreamSynchronize(s->stream));
+    s->vel_host_valid = true;
+    return ST_OK;
+}
+
 // Largest finite velocity (compute_local_max_velocity, wave_equation.cpp:435-443).
 double host_vmax(const st_solver* s) {
     double vmax = 0.0;
@@ -153,8 +164,8 @@ double host_vmax(const st_solver* s) {
 
 // Square of the reference's CFL damping factor (wave_equation.cpp:316-387):
 // 1 unless max(vmax*dt/d) > 1, then min(1, safety/(vmax*dt/min d))^2.
-double cfl_damp2(st_solver* s) {
-    const double vmax = host_vmax(s), dt = s->cfg.dt;
+double cfl_damp2_of(st_solver* s, double vmax) {
+    const double dt = s->cfg.dt;
     const double cfl = std::max({vmax * dt / s->grid.dx, vmax * dt / s->grid.dy, vmax * dt / s->grid.dz});
     if (cfl <= 1.0) return 1.0;
     const double ratio = vmax * dt / std::min({s->grid.dx, s->grid.dy, s->grid.dz});
@@ -166,6 +177,43 @@ double cfl_damp2(st_solver* s) {
         s->cfl_warned = true;
     }
     return f * f;
+}
+
+double cfl_damp2(st_solver* s) { return cfl_damp2_of(s, host_vmax(s)); }
+
+// Largest finite velocity of a device FP64 array, as the bits of a
+// non-negative double (monotonic as unsigned integers); 0 when none is
+// positive, as host_vmax.
+__global__ void vmax_finite_kernel(const double* __restrict__ v, long long n, unsigned long long* out) {
+    double m = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double x = v[i];
+        if (isfinite(x) && x > m) m = x;
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0.0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+// Uploads a whole reference-layout velocity straight to the device (one
+// copy from the caller's buffer, the CFL maximum found on the device) and
+// rebuilds the coefficients; the host mirror is refreshed only when read.
+int upload_velocity(st_solver* s, const double* vp) {
+    const size_t bytes = (size_t)ref_elems(s) * sizeof(double);
+    if (!s->vel_dev) ST_CUDA(cudaMalloc(&s->vel_dev, bytes));
+    ST_CUDA(cudaMemcpyAsync(s->vel_dev, vp, bytes, cudaMemcpyHostToDevice, s->stream));
+    ST_CUDA(cudaMemsetAsync(s->counter, 0, sizeof(unsigned long long), s->stream));
+    vmax_finite_kernel<<<152 * 8, 256, 0, s->stream>>>(s->vel_dev, ref_elems(s), s->counter);
+    count_launch();
+    ST_CUDA(cudaGetLastError());
+    unsigned long long bits = 0;
+    ST_CUDA(cudaMemcpyAsync(&bits, s->counter, sizeof(bits), cudaMemcpyDeviceToHost, s->stream));
+    ST_CUDA(cudaStreamSynchronize(s->stream));
+    double vmax;
+    std::memcpy(&vmax, &bits, sizeof(vmax));
+    ST_TRY(launch_vel_to_coeff(s->vel_dev, s->c, s->L, s->cfg.dt * s->cfg.dt * cfl_damp2_of(s, vmax), s->stream));
+    s->vel_host_valid = false;
+    s->coeff_dirty = false;
+    return ST_OK;
 }
 
 int refresh_coeff(st_solver* s) {
@@ -427,6 +475,7 @@ int st_solver_destroy(st_solver* s) {
     cudaFree(s->data_buf);
     cudaFree(s->ckpt_buf);
     cudaFree(s->zlim);
+    cudaFree(s->vel_dev);
     for (int k = 0; k < 3; ++k)
         if (s->ev[k]) cudaEventDestroy(s->ev[k]);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -437,6 +486,7 @@ int st_solver_destroy(st_solver* s) {
 int st_solver_initialize_velocity(st_solver* s, double vp0) {
     ST_CHECK(s, ST_ERR_ARG, "null solver");
     std::fill(s->vel_host.begin(), s->vel_host.end(), vp0);
+    s->vel_host_valid = true;
     s->coeff_dirty = true;
     return ST_OK;
 }
@@ -444,6 +494,7 @@ int st_solver_initialize_velocity(st_solver* s, double vp0) {
 int st_solver_set_velocity_field(st_solver* s, const double* vp, int64_t count) {
     ST_CHECK(s && (vp || count <= 0), ST_ERR_ARG, "null argument");
     const int64_t n = std::min<int64_t>(count, (int64_t)s->vel_host.size());
+    ST_TRY(ensure_vel_host(s));
     if (n > 0) std::memcpy(s->vel_host.data(), vp, (size_t)n * sizeof(double));
     s->coeff_dirty = true;
     return ST_OK;
@@ -551,6 +602,7 @@ int st_solver_get_field(st_solver* s, int which, double* out, int64_t count) {
     const int64_t n = ref_elems(s);
     ST_CHECK(count >= n, ST_ERR_ARG, "output holds %lld values, field has %lld", (long long)count, (long long)n);
     if (which == ST_FIELD_VELOCITY) {
+        ST_TRY(ensure_vel_host(s));
         std::memcpy(out, s->vel_host.data(), (size_t)n * sizeof(double));
         return ST_OK;
     }
@@ -740,7 +792,7 @@ int st_solver_stream(st_solver* s, void** out) {
 
 int st_shot_forward_host(st_solver* s, const double* vp, int64_t vp_count, const st_shot* shot, double* seis_host) {
     ST_CHECK(s && shot, ST_ERR_ARG, "null argument");
-    if (vp) ST_TRY(st_solver_set_velocity_field(s, vp, vp_count));
+    if (vp) ST_TRY(vp_count >= ref_elems(s) ? upload_velocity(s, vp) : st_solver_set_velocity_field(s, vp, vp_count));
     const int64_t nrec = shot->rec.nx * shot->rec.ny;
     const size_t ns = (size_t)nrec * (size_t)shot->nt;
     ST_CUDA(cudaSetDevice(s->device));

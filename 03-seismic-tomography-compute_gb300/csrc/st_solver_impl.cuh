@@ -61,7 +61,9 @@ struct st_solver {
     double amp_limit = 1e10;
     double cfl_safety = 0.49;
     int max_repair_attempts = 3;
-    stg::PinnedVec vel_host;  // reference layout, authoritative velocity
+    stg::PinnedVec vel_host;  // reference layout; authoritative unless vel_host_valid is false
+    double* vel_dev = nullptr;   // device copy of the last velocity uploaded by upload_velocity
+    bool vel_host_valid = true;  // false: vel_dev holds the model, vel_host is refreshed on demand
     float* f[3] = {nullptr, nullptr, nullptr};
     int ic = 0, ip = 1, in = 2;
     float* c = nullptr;
@@ -101,6 +103,8 @@ namespace stg {
 int64_t ref_elems(const st_solver* s);
 int ensure_staging(st_solver* s);
 int refresh_coeff(st_solver* s);
+int ensure_vel_host(st_solver* s);
+int upload_velocity(st_solver* s, const double* vp);
 int read_flags(st_solver* s, unsigned* out);
 StepArgs base_args(st_solver* s, float* out);
 // epi: 0 none, 1 imaging, 2 gradient (msnap = the snapshot store's map)

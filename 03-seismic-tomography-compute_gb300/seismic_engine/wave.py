@@ -372,13 +372,22 @@ def rtm_shot_checkpointed(solver: WaveEquationSolver, src, wavelet, nt: int, rec
 
 
 def rtm_shot_host(solver: WaveEquationSolver, vel_ref, src, wavelet, nt: int, rec, data_host,
-                  snap_kind: int = _lib.ST_SNAP_BF16, want=("image", "illumination", "reflectivity")):
+                  snap_kind: int = _lib.ST_SNAP_BF16, want=("image", "illumination", "reflectivity"), out=None):
     """Host-buffer RTM (every copy included). data_host: FP32 numpy [nt, nrec]
     (pinned memory gives full copy speed). Returns a dict of FP64 interior
-    arrays named like RTMImageCondition (rtm/rtm_engine.h:25-29)."""
+    arrays named like RTMImageCondition (rtm/rtm_engine.h:25-29); `out` may
+    supply them (C-contiguous float64 arrays of nx*ny*nz values, e.g. pinned
+    buffers reused across shots)."""
     shot, _keep = _shot_c(src, wavelet, nt, rec)
     n = solver.nx * solver.ny * solver.nz
-    outs = {k: np.empty(n) for k in want}
+    outs = {}
+    for k in want:
+        a = None if out is None else out.get(k)
+        if a is None:
+            a = np.empty(n)
+        elif not (a.dtype == np.float64 and a.flags.c_contiguous and a.size == n):
+            raise ValueError(f"out[{k!r}] must be a C-contiguous float64 array of {n} values")
+        outs[k] = a
     nul = C.cast(None, C.POINTER(C.c_double))
     if vel_ref is None:
         vp, nv = nul, 0
