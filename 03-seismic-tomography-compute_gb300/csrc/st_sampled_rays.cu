@@ -41,8 +41,8 @@ struct st_ray_picks {
     int* cell = nullptr;          // [n_samples] cell of each sample, pick-major
     long long* cell_ptr = nullptr;  // [n_cells + 1] offsets into t_pick
     int* t_pick = nullptr;        // [n_samples] pick of each sample, cell-major
-    int* pick_order = nullptr;    // [n_picks] picks by ascending sample count
-    int* cell_order = nullptr;    // [n_cells] cells by ascending sample count
+    int* pick_order = nullptr;    // [n_picks] picks by descending sample count
+    int* cell_order = nullptr;    // [n_cells] cells by descending sample count
     double* stage_vp = nullptr;   // host-call staging: [n_cells]
     double* stage_res = nullptr;  // [n_picks]
     double* stage_out = nullptr;  // [max(n_cells, n_picks)]
@@ -154,13 +154,15 @@ __global__ void cell_histogram_kernel(const int* __restrict__ cell, long long ns
         atomicAdd(cnt + cell[k], 1ull);
 }
 
-// keys[j] = count of item j, vals[j] = j (for the count-ordered schedules).
+// keys[j] = 2^32 - 1 - count of item j, vals[j] = j: an ascending sort
+// lists the items by descending sample count (the count-ordered schedules
+// start the longest loops first, so the light ones fill the tail).
 template <class T>
 __global__ void count_keys_kernel(const T* __restrict__ cnt, long long n, unsigned long long* __restrict__ keys,
                                   unsigned* __restrict__ vals) {
     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n;
          j += (long long)gridDim.x * blockDim.x) {
-        keys[j] = (unsigned long long)cnt[j];
+        keys[j] = 0xffffffffull - (unsigned long long)cnt[j];
         vals[j] = (unsigned)j;
     }
 }
@@ -409,7 +411,7 @@ int build_samples(st_ray_picks* p, const double* src, const double* sta, const d
     count_keys_kernel<<<blocks_for(np, 256), 256, 0, st>>>(count, np, ok, ov);
     count_launch();
     ST_CUDA(cudaGetLastError());
-    ST_TRY(radix_sort_u64(ok, ov, ok2, ov2, np, 25, otmp, st));
+    ST_TRY(radix_sort_u64(ok, ov, ok2, ov2, np, 32, otmp, st));
     ST_CUDA(cudaMemcpyAsync(p->pick_order, ov, (size_t)np * 4, cudaMemcpyDeviceToDevice, st));
     count_keys_kernel<<<blocks_for(p->n_cells, 256), 256, 0, st>>>(cnt, p->n_cells, ok, ov);
     count_launch();
