@@ -360,6 +360,147 @@ class RTMEngine {
     RTMImageCondition res_;
 };
 
+// ---------------------------------------------------------------- solver/boundary.h:9-52
+struct BathymetryPoint {
+    double x, y, depth;
+};
+
+// TerrainBoundary over the GPU library: the bathymetry is built on the host,
+// the field operations run on the device (host vectors are copied in and
+// out). The grid must outlive the object, as in the reference.
+class TerrainBoundary {
+   public:
+    TerrainBoundary(const CartesianGrid& grid, double water_depth, int device = 0) : grid_(grid) {
+        const GridParams& g = grid.params();
+        const st_grid_params p{g.nx_global, g.ny_global, g.nz_global, g.dx, g.dy, g.dz,
+                               g.origin_x, g.origin_y, g.origin_z, g.halo_width};
+        check(st_terrain_create(&p, water_depth, device, &h_));
+    }
+    ~TerrainBoundary() { st_terrain_destroy(h_); }
+    TerrainBoundary(const TerrainBoundary&) = delete;
+    TerrainBoundary& operator=(const TerrainBoundary&) = delete;
+
+    void set_bathymetry_data(const std::vector<BathymetryPoint>& data) {
+        std::vector<st_bathymetry_point> pts(data.size());
+        for (size_t k = 0; k < data.size(); ++k) pts[k] = {data[k].x, data[k].y, data[k].depth};
+        check(st_terrain_set_bathymetry_data(h_, pts.data(), (int64_t)pts.size()));
+    }
+    void generate_synthetic_bathymetry(double gradient, double roughness) {
+        check(st_terrain_generate_synthetic_bathymetry(h_, gradient, roughness));
+    }
+    bool is_subsurface(int64_t gx, int64_t gy, int64_t gz) const {
+        return grid_.params().origin_z + gz * grid_.params().dz >= seafloor_depth(gx, gy);
+    }
+    bool is_water(int64_t gx, int64_t gy, int64_t gz) const { return !is_subsurface(gx, gy, gz); }
+    double seafloor_depth(int64_t gx, int64_t gy) const {
+        double d = 0.0;
+        check(st_terrain_seafloor(h_, gx, gy, &d, nullptr));
+        return d;
+    }
+    int64_t seafloor_index(int64_t gx, int64_t gy) const {
+        int64_t i = 0;
+        check(st_terrain_seafloor(h_, gx, gy, nullptr, &i));
+        return i;
+    }
+    // The reference's signatures take the local grid and halo width; one
+    // device domain has the grid's own.
+    void apply_free_surface_bc(std::vector<double>& field, const LocalGrid&, int) {
+        check(st_terrain_apply_free_surface_bc(h_, sized(field), 0));
+    }
+    void apply_seafloor_bc(std::vector<double>& field, const LocalGrid&, int) {
+        check(st_terrain_apply_seafloor_bc(h_, sized(field), 0));
+    }
+    void apply_absorbing_bc(std::vector<double>& field, const LocalGrid&, int, int sponge_width, double damping) {
+        check(st_terrain_apply_absorbing_bc(h_, sized(field), 0, sponge_width, damping));
+    }
+    void update_velocity_mask(std::vector<double>& velocity, double water_vp, double sediment_vp) const {
+        check(st_terrain_update_velocity_mask(h_, sized(velocity), 0, water_vp, sediment_vp));
+    }
+    const std::vector<double>& bathymetry() const {
+        bathy_.resize((size_t)(grid_.params().nx_global * grid_.params().ny_global));
+        check(st_terrain_bathymetry(h_, bathy_.data()));
+        return bathy_;
+    }
+    void build_boundary_mask(const LocalGrid&, int) {
+        mask_.assign((size_t)grid_.local().total_cells_with_halo, 0);
+        check(st_terrain_build_boundary_mask(h_, mask_.data(), 0));
+    }
+    const std::vector<uint8_t>& mask() const { return mask_; }
+    st_terrain* handle() const { return h_; }
+
+   private:
+    double* sized(std::vector<double>& f) const {
+        if ((int64_t)f.size() < grid_.local().total_cells_with_halo) throw std::invalid_argument("field too small");
+        return f.data();
+    }
+    const CartesianGrid& grid_;
+    st_terrain* h_ = nullptr;
+    mutable std::vector<double> bathy_;
+    std::vector<uint8_t> mask_;
+};
+
+// ---------------------------------------------------------------- rtm/mmap_writer.h:24-124
+constexpr int64_t DEFAULT_MMAP_MAX_BYTES = 4LL * 1024LL * 1024LL * 1024LL;
+constexpr int64_t MMAP_FILE_MAGIC = 0x52544D534E4150LL;
+
+// The slice-ring file writer (the library's C++ writer, the reference's file
+// format); frames are serialized slices, e.g. from st_capture_slice_frames.
+class MmapSnapshotWriter {
+   public:
+    struct Stats {
+        int64_t frames_written, frames_dropped_buffer_full, total_bytes_written, mmap_cycles;
+    };
+    MmapSnapshotWriter() = default;
+    ~MmapSnapshotWriter() { close(); }
+    MmapSnapshotWriter(const MmapSnapshotWriter&) = delete;
+    MmapSnapshotWriter& operator=(const MmapSnapshotWriter&) = delete;
+
+    bool open(const std::string& filename, int64_t max_bytes = DEFAULT_MMAP_MAX_BYTES) {
+        close();
+        if (st_mmap_writer_open(filename.c_str(), max_bytes, &h_) != 0) return false;
+        filename_ = filename;
+        max_bytes_ = max_bytes;
+        return true;
+    }
+    void close() {
+        if (h_) st_mmap_writer_close(h_);
+        h_ = nullptr;
+    }
+    bool is_open() const { return h_ != nullptr; }
+    bool write_frame(const uint8_t* frame_data, int64_t frame_size) {
+        return h_ && frame_data && frame_size > 0 && st_mmap_writer_write_frame(h_, frame_data, frame_size) == 0;
+    }
+    int64_t frame_count() const { return info()[0]; }
+    int64_t write_offset() const { return info()[1]; }
+    int64_t used_bytes() const { return write_offset(); }
+    int64_t capacity_bytes() const { return max_bytes_; }
+    Stats stats() const {
+        const auto i = info();
+        return Stats{i[3], i[4], i[5], i[6]};
+    }
+    std::string filename() const { return filename_; }
+    static bool read_frame(const std::string& filename, int64_t frame_index, std::vector<uint8_t>& out_data) {
+        int64_t n = 0;
+        if (st_mmap_read_frame(filename.c_str(), frame_index, nullptr, 0, &n) != 0) return false;
+        out_data.resize((size_t)n);
+        return st_mmap_read_frame(filename.c_str(), frame_index, out_data.data(), n, &n) == 0;
+    }
+    static int64_t count_frames(const std::string& filename) {
+        int64_t n = -1;
+        return st_mmap_count_frames(filename.c_str(), &n) == 0 ? n : -1;
+    }
+
+   private:
+    std::vector<int64_t> info() const {
+        std::vector<int64_t> out(7, 0);
+        if (h_) check(st_mmap_writer_info(h_, out.data()));
+        return out;
+    }
+    st_mmap_writer* h_ = nullptr;
+    std::string filename_;
+    int64_t max_bytes_ = 0;
+};
+
 // ---------------------------------------------------------------- sparse/aligned_alloc.h:25-91
 // 64-byte aligned vector; new elements are always value-initialised (the
 // reference's AlignedVector(n, 0.0) leaves them uninitialised) and copies are

@@ -9,7 +9,8 @@
 
 int main(int argc, char** argv) {
     seismic::MpiContext mpi(argc, argv);
-    seismic::TomographyConfig cfg = argc > 1 ? seismic::load_config(argv[1]) : seismic::TomographyConfig{};
+    seismic::TomographyConfig cfg =
+        argc > 1 && argv[1][0] ? seismic::load_config(argv[1]) : seismic::TomographyConfig{};
     cfg.solver.dt = 0.001;
     cfg.solver.sponge_width = 4;
     cfg.solver.sponge_damping = 0.015;
@@ -50,5 +51,29 @@ int main(int argc, char** argv) {
     std::printf("cg_rel %.3e\n", std::sqrt(r / bb));
     std::printf("nnz %lld %lld\n", (long long)A.nnz(), (long long)A.rows());
     std::printf("dot %.17g\n", seismic::SparseOps::dot_product(b, x));
+
+    // terrain: bathymetry from points, the water-column velocity and the seafloor condition
+    seismic::TerrainBoundary terrain(grid, 50.0);
+    terrain.set_bathymetry_data({{15.0, 15.0, 120.0}, {105.0, 95.0, 30.0}});
+    std::vector<double> tv(grid.local().total_cells_with_halo, 0.0);
+    terrain.update_velocity_mask(tv, 1500.0, 3000.0);
+    std::vector<double> tf(grid.local().total_cells_with_halo, 1.0);
+    terrain.apply_seafloor_bc(tf, grid.local(), 1);
+    double tsum = 0.0, fsum = 0.0;
+    for (double v : tv) tsum += v;
+    for (double v : tf) fsum += v;
+    std::printf("terrain %lld %lld %.17g %.17g\n", (long long)terrain.seafloor_index(1, 1),
+                (long long)terrain.seafloor_index(10, 9), tsum, fsum);
+
+    // the slice ring: two frames through the writer, read back
+    const char* ring = argc > 2 ? argv[2] : "face_demo_ring.dat";
+    seismic::MmapSnapshotWriter w;
+    const std::vector<uint8_t> f1(300, 7), f2(500, 9);
+    const bool ok = w.open(ring, 4096) && w.write_frame(f1.data(), 300) && w.write_frame(f2.data(), 500);
+    w.close();
+    std::vector<uint8_t> back;
+    const bool rd = seismic::MmapSnapshotWriter::read_frame(ring, 1, back);
+    std::printf("ring %d %lld %d %lld\n", ok ? 1 : 0, (long long)seismic::MmapSnapshotWriter::count_frames(ring),
+                rd ? 1 : 0, (long long)back.size());
     return 0;
 }

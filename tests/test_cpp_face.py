@@ -34,10 +34,11 @@ def test_cpp_face_compiles_and_links():
 
 
 @pytest.mark.gpu
-def test_cpp_face_matches_python_face():
+def test_cpp_face_matches_python_face(tmp_path):
     import seismic_engine as se
     exe = build_demo()
-    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    ring = str(tmp_path / "ring.dat")
+    r = subprocess.run([exe, "", ring], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     vals = {}
     for line in r.stdout.splitlines():
@@ -60,3 +61,14 @@ def test_cpp_face_matches_python_face():
     assert vals["image"][0] == pytest.approx(float(eng.result().image.sum()), rel=1e-12)
     assert vals["cg_rel"][0] < 1e-5
     assert vals["nnz"][0] > 0 and vals["nnz"][1] == 512
+    # terrain through the C++ class vs the Python class
+    g = se.GridParams(20, 18, 22, 10.0, 10.0, 10.0)
+    t = se.TerrainBoundary(g, 50.0)
+    t.set_bathymetry_data([(15.0, 15.0, 120.0), (105.0, 95.0, 30.0)])
+    tv = t.update_velocity_mask(np.zeros(t.padded_size), 1500.0, 3000.0)
+    tf = t.apply_seafloor_bc(np.ones(t.padded_size))
+    assert vals["terrain"][:2] == [t.seafloor_index(1, 1), t.seafloor_index(10, 9)] == [12.0, 3.0]
+    assert vals["terrain"][2] == float(tv.sum()) and vals["terrain"][3] == float(tf.sum())
+    # the ring file: two frames written, frame 1 read back (500 bytes)
+    assert vals["ring"] == [1.0, 2.0, 1.0, 500.0]
+    assert se.MmapSnapshotWriter.read_frame(ring, 0) == bytes([7]) * 300
