@@ -145,3 +145,34 @@ def test_refusals_and_empty(se):
     # invalid picks only: time 0, no gradient, no samples
     v = se.SampledRays(model, [[5.0, 5, 5]], [[75.0, 75, 75]], [1.0], valid=[0])
     assert v.n_samples == 0 and v.forward_model(np.full(512, 2000.0))[0] == 0.0
+
+
+def test_full_size_matrix_properties(se):
+    """At the benchmark's size (2M picks, 26.8M samples on 100^3 cells): the
+    forward model equals A (1/v) with the sampled-ray CSR, and the gradient
+    equals -(A^T (w r)) / v^2 (all velocities valid, residuals finite), to
+    the FP32 precision of the matrix and the SpMV."""
+    import torch
+    ps = se.workloads.obs_picks()
+    rays = se.SampledRays(ps.model, ps.src_xyz, ps.sta_xyz, ps.weight)
+    vp = torch.from_numpy(ps.vp.reshape(-1)).cuda()
+    res = torch.from_numpy(np.random.default_rng(1).standard_normal(rays.n_picks) * 0.05).cuda()
+    t = rays.forward_model(vp)
+    g = rays.compute_gradient(vp, res)
+    A = rays.matrix()
+    assert A.rows() == rays.n_picks and A.cols() == rays.n_cells
+    y = torch.zeros(rays.n_picks, device="cuda")
+    s = (1.0 / vp).float()
+    A.spmv_device(s, y)
+    r32 = (torch.from_numpy(ps.weight).cuda() * res).float()
+    z = torch.zeros(rays.n_cells, device="cuda")
+    A.spmv_device(r32, z, transpose=True)
+    torch.cuda.synchronize()
+    torch.cuda.ExternalStream(A.stream_ptr()).synchronize()
+    e_t = float(torch.linalg.norm(y.double() - t) / torch.linalg.norm(t))
+    g_ref = -z.double() / (vp * vp)
+    e_g = float(torch.linalg.norm(g_ref - g) / torch.linalg.norm(g))
+    print(f"full size: forward vs A(1/v) {e_t:.2e}, gradient vs -A^T(wr)/v^2 {e_g:.2e}")
+    assert e_t < 1e-6 and e_g < 1e-5
+    A.close()
+    rays.close()
