@@ -388,6 +388,25 @@ def run_sampled_rays(args):
                           "h2d_bytes": int(2 * vp_h.nbytes + res_h.nbytes), "d2h_bytes": int(t_h.nbytes + g_h.nbytes)}
     out["host_matches_device"] = bool(np.array_equal(t_h, times.cpu().numpy()) and
                                       np.array_equal(g_h, grad.cpu().numpy()))
+    # the whole driver (inversion.py:118-274) on the device: 3 iterations of forward, misfit, gradient,
+    # smoothing, regularisation, normalisation and a 10-trial line search, observed times = the
+    # forward model of a perturbed model
+    from types import SimpleNamespace
+    from seismic_engine.inversion import AdjointStateInversion
+    n = ps.model[0]
+    model = SimpleNamespace(nx=n, ny=n, nz=n, dx=ps.model[3], dy=ps.model[4], dz=ps.model[5],
+                            origin_x=0.0, origin_y=0.0, origin_z=0.0, vp=ps.vp.copy(), vp_min=1450.0,
+                            vp_max=8500.0)
+    t_obs = rays.forward_model(vp * 1.02).cpu().numpy()
+    obs = SimpleNamespace(picks=[])
+    inv = AdjointStateInversion(model, obs, None, max_iterations=3, step_length=10.0, smoothing_sigma=2.0,
+                                misfit_type="l2", rays=rays, observed=t_obs, weights=ps.weight)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res_inv = inv.run()
+    torch.cuda.synchronize()
+    out["driver"] = {"iterations": res_inv["iterations"], "ms_per_iteration": 1e3 * (time.perf_counter() - t0) /
+                     max(res_inv["iterations"], 1), "misfit_history": res_inv["misfit_history"]}
     if not args.no_cpu_baseline:
         from oracle import Oracle
         orc = Oracle()
