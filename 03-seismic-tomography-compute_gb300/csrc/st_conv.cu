@@ -11,10 +11,14 @@
 // in[rows + s][128 x 32] . W_tap[32 x 32]^T: an implicit GEMM with M = 128
 // voxels, N = 32 output channels and K = 27 x 32.
 //
-// Data path per CTA (persistent, one per SM, 6 warps):
-//   warp 0  TMA producer: for each tile loads three 128 + 2(W+3)-row windows
-//           (planes d-1, d, d+1) as 16-byte channel-block columns
-//           ([kd][cb][row][8 channels], no swizzle) into a 2-stage ring;
+// Data path per CTA (persistent, one per SM, 6 warps). The work is cut into
+// units: one in-plane tile position (128 rows) for a run of consecutive
+// planes d0..d1-1, so a CTA marches along d and every plane window it loads
+// serves three consecutive tiles (taps kd = 2, 1, 0):
+//   warp 0  TMA producer: loads the 128 + 2(W+3)-row window of each plane the
+//           unit needs (d0 .. d1+1 in padded planes) as 16-byte channel-block
+//           columns ([cb][row][8 channels], no swizzle) into a ring of four
+//           window slots, a slot refilled once its last tile's MMAs are done;
 //   warp 1  allocates 64 TMEM columns (two FP32 accumulators of 128 x 32) and
 //           issues 54 tcgen05.mma.kind::f16 (BF16 x BF16 -> FP32, M=128,
 //           N=32, K=16) per tile: every tap is a 16-byte-aligned start row
@@ -40,7 +44,10 @@ constexpr int CH = 32;
 constexpr int TM = 128;
 constexpr int NTAP = 27;
 constexpr int W_BYTES = NTAP * CH * CH * 2;  // 55,296: [tap][cb][co][8 ci]
-constexpr int NSTAGE = 2;
+// plane-window slots: three in use by a tile, the rest loading ahead; the
+// host takes MAX_SLOT where it fits in shared memory, else MIN_SLOT (six
+// measured 3% faster than four on a 100^3 volume, eight no faster than six)
+constexpr int MIN_SLOT = 4, MAX_SLOT = 6;
 constexpr int CONV_THREADS = 192;
 constexpr int TMEM_COLS = 64;
 constexpr int SMEM_LIMIT = 232448 - 1024;
@@ -55,7 +62,8 @@ struct ConvArgs {
     int D, H, W;
     int relu;
     int rows_box, nload;    // TMA box rows and boxes per window column
-    int tiles, tiles_per_plane;
+    int tiles_per_plane;    // in-plane tile positions (units' columns)
+    int dchunk, units;      // planes per unit, units = tiles_per_plane * ceil(D / dchunk)
     unsigned* flags;
     unsigned long long timeout_ns;
 };
@@ -127,11 +135,24 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32]) {
 }
 
 struct ConvSmem {
-    uint64_t full[NSTAGE], empty[NSTAGE], tfull[2], tempty[2], wbar;
+    uint64_t full[MAX_SLOT], empty[MAX_SLOT], tfull[2], tempty[2], wbar;
     uint32_t tmem_base;
     int abort;
 };
 
+// Unit u: in-plane tile column u % tiles_per_plane, planes [d0, d1).
+struct ConvUnit {
+    int col, d0, d1;
+};
+__device__ __forceinline__ ConvUnit unit_of(const ConvArgs& a, int u) {
+    ConvUnit r;
+    r.col = u % a.tiles_per_plane;
+    r.d0 = (u / a.tiles_per_plane) * a.dchunk;
+    r.d1 = min(a.D, r.d0 + a.dchunk);
+    return r;
+}
+
+template <int NSLOT>
 __global__ void __launch_bounds__(CONV_THREADS, 1)
     conv3d_tc_kernel(const __grid_constant__ CUtensorMap m0, const __grid_constant__ CUtensorMap m1,
                      const __grid_constant__ CUtensorMap m2, const __grid_constant__ CUtensorMap m3,
@@ -143,15 +164,15 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
     const int PL = (a.H + 2) * W2;
     const int win_rows = a.rows_box * a.nload;          // rows per (kd, cb) column
     const uint32_t lbo_a = (uint32_t)win_rows * 16u;    // channel-block stride
-    const uint32_t stage_bytes = 12u * lbo_a;
+    const uint32_t slot_bytes = 4u * lbo_a;           // one plane window, 4 channel-block columns
     unsigned char* wsm = smem;                           // weights
-    unsigned char* stages = smem + W_BYTES;              // 128-byte aligned (W_BYTES = 54 KB)
-    ConvSmem* cs = reinterpret_cast<ConvSmem*>(stages + NSTAGE * stage_bytes);
+    unsigned char* slots = smem + W_BYTES;               // 128-byte aligned (W_BYTES = 54 KB)
+    ConvSmem* cs = reinterpret_cast<ConvSmem*>(slots + NSLOT * slot_bytes);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint64_t lim = a.timeout_ns;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < NSTAGE; ++s) {
+        for (int s = 0; s < NSLOT; ++s) {
             mbar_init(&cs->full[s], 1);
             mbar_init(&cs->empty[s], 1);
         }
@@ -176,78 +197,95 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
     const uint32_t tmem = cs->tmem_base;
     const CUtensorMap* maps[4] = {&m0, &m1, &m2, &m3};
 
-    int my_tiles = 0;
-    for (int t = blockIdx.x; t < a.tiles; t += gridDim.x) ++my_tiles;
-
+    // Window fills are numbered g = 0, 1, ... in the CTA's unit order; fill g
+    // goes to slot g % NSLOT. A unit of planes [d0, d1) takes d1 - d0 + 2 fills
+    // (padded planes d0 .. d1 + 1); its k-th tile reads fills g0 + k + kd.
     if (warp == 0) {
         if (lane == 0) {
-            // weights once, then the input windows of every tile
             mbar_arrive_expect_tx(&cs->wbar, W_BYTES);
             bulk_load(wsm, a.w, W_BYTES, &cs->wbar);
-            int issued[NSTAGE] = {0, 0};
-            for (int i = 0; i < my_tiles; ++i) {
-                const int t = blockIdx.x + i * gridDim.x;
-                const int s = i % NSTAGE;
-                if (i >= NSTAGE && !mbar_wait_bounded(&cs->empty[s], ((i / NSTAGE) & 1) ^ 1, lim)) {
-                    atomicOr(a.flags, CONV_FLAG_TIMEOUT);
-                    cs->abort = 1;
-                    break;
-                }
-                if (read_abort(&cs->abort)) break;
-                const int d = t / a.tiles_per_plane;
-                const int p0 = (t % a.tiles_per_plane) * TM;
-                unsigned char* st = stages + s * stage_bytes;
-                mbar_arrive_expect_tx(&cs->full[s], 12u * (uint32_t)a.nload * (uint32_t)a.rows_box * 16u);
-                for (int kd = 0; kd < 3; ++kd) {
-                    const int q0 = (d + kd) * PL + p0 - (W2 + 1);
+            int g = 0;
+            bool stop = false;
+            for (int u = blockIdx.x; u < a.units && !stop; u += gridDim.x) {
+                const ConvUnit U = unit_of(a, u);
+                const int p0 = U.col * TM;
+                const int nfill = U.d1 - U.d0 + 2;
+                for (int j = 0; j < nfill; ++j, ++g) {
+                    const int slot = g % NSLOT;
+                    if (g >= NSLOT && !mbar_wait_bounded(&cs->empty[slot], ((g / NSLOT) - 1) & 1, lim)) {
+                        atomicOr(a.flags, CONV_FLAG_TIMEOUT);
+                        cs->abort = 1;
+                        stop = true;
+                        break;
+                    }
+                    if (read_abort(&cs->abort)) {
+                        stop = true;
+                        break;
+                    }
+                    unsigned char* sb = slots + slot * slot_bytes;
+                    const int q0 = (U.d0 + j) * PL + p0 - (W2 + 1);
+                    mbar_arrive_expect_tx(&cs->full[slot], 4u * (uint32_t)a.nload * (uint32_t)a.rows_box * 16u);
                     for (int cb = 0; cb < 4; ++cb)
                         for (int l = 0; l < a.nload; ++l)
-                            tma_load_2d(st + (kd * 4 + cb) * lbo_a + l * a.rows_box * 16, maps[cb], &cs->full[s], 0,
+                            tma_load_2d(sb + cb * lbo_a + l * a.rows_box * 16, maps[cb], &cs->full[slot], 0,
                                         q0 + l * a.rows_box);
                 }
-                issued[s] += 1;
             }
             // drain: every issued window has landed before the CTA may exit
-            for (int s = 0; s < NSTAGE; ++s)
-                if (issued[s] > 0 && !mbar_wait_bounded(&cs->full[s], (issued[s] - 1) & 1, lim))
-                    atomicOr(a.flags, CONV_FLAG_TIMEOUT);
+            for (int f = (g > NSLOT ? g - NSLOT : 0); f < g; ++f)
+                if (!mbar_wait_bounded(&cs->full[f % NSLOT], (f / NSLOT) & 1, lim)) atomicOr(a.flags, CONV_FLAG_TIMEOUT);
         }
     } else if (warp == 1) {
         if (lane == 0) {
             bool ok = mbar_wait_bounded(&cs->wbar, 0, lim);
-            int committed = 0;
-            for (int i = 0; ok && i < my_tiles; ++i) {
-                const int s = i % NSTAGE, acc = i & 1;
-                if (i >= 2 && !mbar_wait_bounded(&cs->tempty[acc], ((i >> 1) & 1) ^ 1, lim)) {
-                    ok = false;
-                    break;
-                }
-                if (!mbar_wait_bounded(&cs->full[s], (i / NSTAGE) & 1, lim)) {
-                    ok = false;
-                    break;
-                }
-                if (read_abort(&cs->abort)) break;
-                tc_fence_after();
-                const uint32_t st = smem_u32(stages + s * stage_bytes);
-                const uint32_t wb = smem_u32(wsm);
-                const uint32_t d_tmem = tmem + (uint32_t)(acc * CH);
-                for (int kd = 0; kd < 3; ++kd)
-                    for (int kh = 0; kh < 3; ++kh)
-                        for (int kw = 0; kw < 3; ++kw) {
-                            const int tap = (kd * 3 + kh) * 3 + kw;
-                            const uint32_t roff = (uint32_t)(W2 + 1 + (kh - 1) * W2 + (kw - 1)) * 16u;
+            int committed = 0, i = 0, g0 = 0;
+            const uint32_t wb = smem_u32(wsm);
+            for (int u = blockIdx.x; ok && u < a.units; u += gridDim.x) {
+                const ConvUnit U = unit_of(a, u);
+                const int nt = U.d1 - U.d0;
+                for (int k = 0; ok && k < nt; ++k, ++i) {
+                    const int acc = i & 1;
+                    if (i >= 2 && !mbar_wait_bounded(&cs->tempty[acc], ((i >> 1) & 1) ^ 1, lim)) {
+                        ok = false;
+                        break;
+                    }
+                    uint32_t sbase[3];
+                    for (int kd = 0; kd < 3; ++kd) {
+                        const int f = g0 + k + kd;
+                        if (!mbar_wait_bounded(&cs->full[f % NSLOT], (f / NSLOT) & 1, lim)) ok = false;
+                        sbase[kd] = smem_u32(slots + (f % NSLOT) * slot_bytes);
+                    }
+                    if (!ok || read_abort(&cs->abort)) {
+                        ok = ok && !read_abort(&cs->abort);
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t d_tmem = tmem + (uint32_t)(acc * CH);
+                    for (int kd = 0; kd < 3; ++kd)
+                        for (int kh = 0; kh < 3; ++kh)
+                            for (int kw = 0; kw < 3; ++kw) {
+                                const int tap = (kd * 3 + kh) * 3 + kw;
+                                const uint32_t roff = (uint32_t)(W2 + 1 + (kh - 1) * W2 + (kw - 1)) * 16u;
 #pragma unroll
-                            for (int ks = 0; ks < 2; ++ks) {
-                                const uint64_t ad =
-                                    smem_desc(st + (uint32_t)(kd * 4 + 2 * ks) * lbo_a + roff, lbo_a, 128u);
-                                const uint64_t bd = smem_desc(wb + (uint32_t)tap * 2048u + (uint32_t)ks * 1024u,
-                                                              512u, 128u);
-                                mma_bf16(d_tmem, ad, bd, (tap | ks) != 0);
+                                for (int ks = 0; ks < 2; ++ks) {
+                                    const uint64_t ad = smem_desc(sbase[kd] + (uint32_t)(2 * ks) * lbo_a + roff, lbo_a,
+                                                                  128u);
+                                    const uint64_t bd = smem_desc(wb + (uint32_t)tap * 2048u + (uint32_t)ks * 1024u,
+                                                                  512u, 128u);
+                                    mma_bf16(d_tmem, ad, bd, (tap | ks) != 0);
+                                }
                             }
-                        }
-                mma_commit(&cs->empty[s]);
-                mma_commit(&cs->tfull[acc]);
-                ++committed;
+                    mma_commit(&cs->tfull[acc]);
+                    // the window of plane d (tap kd = 0) has served its last tile; at
+                    // the unit's end so have the two after it
+                    mma_commit(&cs->empty[(g0 + k) % NSLOT]);
+                    if (k == nt - 1) {
+                        mma_commit(&cs->empty[(g0 + k + 1) % NSLOT]);
+                        mma_commit(&cs->empty[(g0 + k + 2) % NSLOT]);
+                    }
+                    ++committed;
+                }
+                g0 += nt + 2;
             }
             if (!ok) {
                 atomicOr(a.flags, CONV_FLAG_TIMEOUT);
@@ -267,64 +305,70 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
         float bias[CH];
 #pragma unroll
         for (int c = 0; c < CH; ++c) bias[c] = a.bias ? a.bias[c] : 0.0f;
-        for (int i = 0; i < my_tiles; ++i) {
-            const int t = blockIdx.x + i * gridDim.x;
-            const int acc = i & 1;
-            // warp-uniform outcome: the TMEM load below is a warp-collective
-            const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&cs->tfull[acc], (i >> 1) & 1, lim));
-            if (!ok) {
-                if (lane == 0) atomicOr(a.flags, CONV_FLAG_TIMEOUT);
-                cs->abort = 1;
-                break;
-            }
-            tc_fence_after();
-            float v[CH];
-            tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * CH), v);
-            tc_fence_before();
-            mbar_arrive(&cs->tempty[acc]);
-            const int d = t / a.tiles_per_plane;
-            const int p = (t % a.tiles_per_plane) * TM + row;
-            if (p >= PL) continue;
-            const int h = p / W2, w = p - h * W2;
-            const bool inside = h >= 1 && h <= a.H && w >= 1 && w <= a.W;
-            const long long q = (long long)(d + 1) * PL + p;
-            if (inside) {
-                if (a.add) {
-                    const uint4* ap = reinterpret_cast<const uint4*>(a.add + q * CH);
+        int i = 0;
+        bool stop = false;
+        for (int u = blockIdx.x; u < a.units && !stop; u += gridDim.x) {
+            const ConvUnit U = unit_of(a, u);
+            for (int d = U.d0; d < U.d1; ++d, ++i) {
+                const int acc = i & 1;
+                // warp-uniform outcome: the TMEM load below is a warp-collective
+                const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&cs->tfull[acc], (i >> 1) & 1, lim));
+                if (!ok) {
+                    if (lane == 0) atomicOr(a.flags, CONV_FLAG_TIMEOUT);
+                    cs->abort = 1;
+                    stop = true;
+                    break;
+                }
+                tc_fence_after();
+                float v[CH];
+                tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * CH), v);
+                tc_fence_before();
+                mbar_arrive(&cs->tempty[acc]);
+                const int p = U.col * TM + row;
+                if (p >= PL) continue;
+                const int h = p / W2, w = p - h * W2;
+                const bool inside = h >= 1 && h <= a.H && w >= 1 && w <= a.W;
+                const long long q = (long long)(d + 1) * PL + p;
+                if (inside) {
+                    if (a.add) {
+                        const uint4* ap = reinterpret_cast<const uint4*>(a.add + q * CH);
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        const uint4 u = ap[j];
-                        const __nv_bfloat162* b2 = reinterpret_cast<const __nv_bfloat162*>(&u);
+                        for (int j = 0; j < 4; ++j) {
+                            const uint4 uu = ap[j];
+                            const __nv_bfloat162* b2 = reinterpret_cast<const __nv_bfloat162*>(&uu);
 #pragma unroll
-                        for (int e = 0; e < 4; ++e) {
-                            const float2 f = __bfloat1622float2(b2[e]);
-                            v[8 * j + 2 * e] += f.x;
-                            v[8 * j + 2 * e + 1] += f.y;
+                            for (int e = 0; e < 4; ++e) {
+                                const float2 f = __bfloat1622float2(b2[e]);
+                                v[8 * j + 2 * e] += f.x;
+                                v[8 * j + 2 * e + 1] += f.y;
+                            }
                         }
                     }
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) {
+                        v[c] += bias[c];
+                        if (a.relu) v[c] = fmaxf(v[c], 0.0f);
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) v[c] = 0.0f;
                 }
+                if (a.out_f32) {
+                    float4* op = reinterpret_cast<float4*>(static_cast<float*>(a.out) + q * CH);
 #pragma unroll
-                for (int c = 0; c < CH; ++c) {
-                    v[c] += bias[c];
-                    if (a.relu) v[c] = fmaxf(v[c], 0.0f);
-                }
-            } else {
+                    for (int j = 0; j < 8; ++j)
+                        op[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+                } else {
+                    uint4* op = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(a.out) + q * CH);
 #pragma unroll
-                for (int c = 0; c < CH; ++c) v[c] = 0.0f;
-            }
-            if (a.out_f32) {
-                float4* op = reinterpret_cast<float4*>(static_cast<float*>(a.out) + q * CH);
+                    for (int j = 0; j < 4; ++j) {
+                        uint4 uu;
+                        __nv_bfloat162* b2 = reinterpret_cast<__nv_bfloat162*>(&uu);
 #pragma unroll
-                for (int j = 0; j < 8; ++j) op[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
-            } else {
-                uint4* op = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(a.out) + q * CH);
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    uint4 u;
-                    __nv_bfloat162* b2 = reinterpret_cast<__nv_bfloat162*>(&u);
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) b2[e] = __floats2bfloat162_rn(v[8 * j + 2 * e], v[8 * j + 2 * e + 1]);
-                    op[j] = u;
+                        for (int e = 0; e < 4; ++e)
+                            b2[e] = __floats2bfloat162_rn(v[8 * j + 2 * e], v[8 * j + 2 * e + 1]);
+                        op[j] = uu;
+                    }
                 }
             }
         }
@@ -418,7 +462,11 @@ int st_conv3d_bf16(const void* in, const void* packed_w, const float* bias, cons
         ++nload;
         rows_box = (int)((((win + nload - 1) / nload) + 7) / 8 * 8);
     }
-    const size_t smem = (size_t)W_BYTES + (size_t)NSTAGE * 12 * 16 * nload * rows_box + sizeof(ConvSmem) + 128;
+    auto smem_of = [&](int ns) {
+        return (size_t)W_BYTES + (size_t)ns * 4 * 16 * nload * rows_box + sizeof(ConvSmem) + 128;
+    };
+    const int nslot = smem_of(MAX_SLOT) <= (size_t)SMEM_LIMIT ? MAX_SLOT : MIN_SLOT;
+    const size_t smem = smem_of(nslot);
     ST_CHECK(smem <= (size_t)SMEM_LIMIT, ST_ERR_UNSUPPORTED, "volume width %lld too large for the conv tiles",
              (long long)W);
     const __nv_bfloat16* src = static_cast<const __nv_bfloat16*>(in);
@@ -439,21 +487,36 @@ int st_conv3d_bf16(const void* in, const void* packed_w, const float* bias, cons
     a.rows_box = rows_box;
     a.nload = nload;
     a.tiles_per_plane = (int)((PL + TM - 1) / TM);
-    a.tiles = (int)(D * a.tiles_per_plane);
-    a.flags = flags;
-    a.timeout_ns = 2000000000ull;
-    static std::mutex mu;
-    static size_t configured = 0;
-    {
-        std::lock_guard<std::mutex> lk(mu);
-        if (configured < smem) {
-            ST_CUDA(cudaFuncSetAttribute(conv3d_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            configured = smem;
+    // planes per unit: the fewest rounds of units over the SMs, each unit
+    // paying two extra window loads (its first two planes)
+    const long long nsm = num_sms_conv();
+    long long best_cost = -1;
+    for (long long dc = 1; dc <= D; ++dc) {
+        const long long units = (long long)a.tiles_per_plane * ((D + dc - 1) / dc);
+        const long long rounds = (units + nsm - 1) / nsm;
+        const long long cost = rounds * (dc + 2);
+        if (best_cost < 0 || cost < best_cost) {
+            best_cost = cost;
+            a.dchunk = (int)dc;
         }
     }
-    const int grid = std::min(a.tiles, num_sms_conv());
+    a.units = (int)((long long)a.tiles_per_plane * ((D + a.dchunk - 1) / a.dchunk));
+    a.flags = flags;
+    a.timeout_ns = 2000000000ull;
+    auto kern = nslot == MAX_SLOT ? conv3d_tc_kernel<MAX_SLOT> : conv3d_tc_kernel<MIN_SLOT>;
+    static std::mutex mu;
+    static size_t configured[2] = {0, 0};
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        size_t& c = configured[nslot == MAX_SLOT ? 1 : 0];
+        if (c < smem) {
+            ST_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            c = smem;
+        }
+    }
+    const int grid = std::min(a.units, num_sms_conv());
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    conv3d_tc_kernel<<<grid, CONV_THREADS, smem, st>>>(maps[0], maps[1], maps[2], maps[3], a);
+    kern<<<grid, CONV_THREADS, smem, st>>>(maps[0], maps[1], maps[2], maps[3], a);
     count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;

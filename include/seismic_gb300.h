@@ -435,8 +435,8 @@ int st_fwi_gradient_checkpointed(st_solver* s, const st_shot* shot, const float*
  * ring) and never planes 0 and D+1, which the caller zeroes once.
  * out = relu?(conv(in) + bias + add), BF16 or,
  * with out_fp32, FP32. packed_w: 55,296 bytes from st_conv3d_pack_weights.
- * Asynchronous on `stream` (a cudaStream_t); W <= 156 (ST_ERR_UNSUPPORTED
- * beyond: the shared-memory windows). st_conv3d_check
+ * Asynchronous on `stream` (a cudaStream_t); W <= 269 (ST_ERR_UNSUPPORTED
+ * beyond: the shared-memory plane windows). st_conv3d_check
  * synchronises the stream and reports a bounded-wait timeout of any earlier
  * conv launch (ST_ERR_TIMEOUT), clearing it. */
 int st_conv3d_pack_weights(const float* w_oidhw, void* packed_w, int transpose, void* stream);

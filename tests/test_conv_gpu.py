@@ -68,7 +68,8 @@ def rel(a, b):
     return float((a - b).norm() / max(float(b.norm()), 1e-300))
 
 
-@pytest.mark.parametrize("D,H,W", [(3, 5, 7), (5, 13, 100), (2, 9, 156), (4, 33, 31)])
+# (25, 40, 40): units of 3 planes (the last of 1) march along d through the window ring
+@pytest.mark.parametrize("D,H,W", [(3, 5, 7), (5, 13, 100), (2, 9, 156), (3, 4, 269), (4, 33, 31), (25, 40, 40)])
 def test_conv_matches_torch(lib, D, H, W):
     import torch
     import torch.nn.functional as F
@@ -112,7 +113,7 @@ def test_transposed_packing_is_the_adjoint(lib):
 def test_too_wide_volume_is_refused(lib):
     import torch
     from seismic_engine import _lib
-    D, H, W = 2, 3, 158
+    D, H, W = 2, 3, 270  # the widest accepted is 269 (four plane windows of 128 + 2 (W + 3) rows)
     x = torch.zeros((D + 2, H + 2, W + 2, 32), dtype=torch.bfloat16, device="cuda")
     y = torch.zeros_like(x)
     wpk = torch.zeros(27 * 32 * 32, dtype=torch.bfloat16, device="cuda")
