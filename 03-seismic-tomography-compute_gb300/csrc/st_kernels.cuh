@@ -35,6 +35,11 @@ struct StepArgs {
     int stable_sponge;       // 1: out = D * (update + forcing) (damped new field), 0: the reference rule
     const int* zlim;         // terrain: per (x, y) column (x * ny + y), points with z < zlim are set to 0
                              // after the update (free surface / seafloor masks), or null
+    // two-step imaging launch only: the second step's output field, forcing
+    // row and snapshot scale
+    float* out2;
+    const float* force_row2;
+    const unsigned* amax_in2;
 };
 
 // Sponge factor of interior point (ix, iy, iz): D(d) for the distance d to the
@@ -52,10 +57,12 @@ __device__ __forceinline__ float sponge_D(const Layout& L, const float* dtab, in
 
 // Tensor maps of one device field for the two tile heights of the stencil
 // kernels ([0]: 16-row tiles, [1]: 32-row tiles): cur boxes {TZ+8, rows+2, 1}
-// starting at (z0, y0, x), centre boxes {TZ, rows, 1}.
+// starting at (z0, y0, x), centre boxes {TZ, rows, 1}; cur2 is the two-step
+// kernel's box {TZ+8, 16+4, 1} (a two-cell y halo).
 struct FieldMaps {
     CUtensorMap cur[2];
     CUtensorMap ctr[2];
+    CUtensorMap cur2;
 };
 
 // Tile width of the stencil kernels along z.
@@ -63,8 +70,9 @@ constexpr int FD_TZ = 64;
 
 int build_field_maps(FieldMaps* m, const float* base, const Layout& L);
 // x-chunks per CTA column for a tile height and resident CTAs per SM, with at
-// least min_waves waves of resident CTAs when the grid allows it.
-int fd_step_grid_chunks(const Layout& L, int tyv, int minb, int min_waves);
+// least min_waves waves of resident CTAs when the grid allows it; each chunk
+// re-reads halo extra x-planes.
+int fd_step_grid_chunks(const Layout& L, int tyv, int minb, int min_waves, int halo = 2);
 
 // Maps of the staged imaging variant: the snapshot store (box {64, 16} at
 // (z, y, x, t)) and the compact image / illumination volumes (box {64, 16}).
@@ -83,6 +91,14 @@ int make_compact_map(CUtensorMap* map, const float* base, const Layout& L, int b
 int launch_fd_step(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
                    StepArgs a, int snap_out, int snap_in, int epi, const CUtensorMap* msnap, cudaStream_t st,
                    const ImageMaps* imaps = nullptr);
+// Launch two adjoint steps with fused imaging (fd_step2_image_kernel): reads
+// cur = lambda_t and prev = lambda_{t+1}, writes a.out = lambda_{t-1}' (the
+// output of step t) and a.out2 = the output of step t-1, from snapshots
+// a.snap_t and a.snap_t - 1 (scales a.amax_in, a.amax_in2) and the receiver
+// forcing rows a.force_row (step t) and a.force_row2 (step t-1). Needs
+// staged image maps (nz % 4 == 0).
+int launch_fd_step2_image(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
+                          StepArgs a, int snap_in, const ImageMaps& imaps, cudaStream_t st);
 // 4-D map over a snapshot store for the gradient step's halo tile.
 int build_snap_map_grad(CUtensorMap* m, const void* base, int kind, const Layout& L, long long nt);
 

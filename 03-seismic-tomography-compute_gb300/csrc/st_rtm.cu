@@ -168,7 +168,26 @@ int rtm_backward_impl(st_solver* s, const st_shot* shot, const float* data, int 
     }
     const long long src = dev_index(s, shot->src_ix, shot->src_iy, shot->src_iz);
     const long long q_src = receiver_at(R, shot->src_ix, shot->src_iy, shot->src_iz);
+    // pairs of steps share one launch unless a step's field is needed on its
+    // own (slice capture, source trace)
+    const bool pairs = staged && s->adjoint_steps == 2 && !s->slices && !src_trace;
     for (int t = nt - 1; t >= 0; --t) {
+        if (pairs && t >= 1) {
+            StepArgs a = base_args(s, nullptr);
+            if (nrec > 0) {
+                set_receivers(a, R);
+                a.force_row = data + (size_t)(t - 1) * nrec;
+                if (t >= 2) a.force_row2 = data + (size_t)(t - 2) * nrec;
+            }
+            a.snap_t = t;
+            a.amax_in = amax + t;
+            a.amax_in2 = amax + t - 1;
+            a.image = image;
+            a.illum = illum;
+            ST_TRY(fused_step2(s, a, snap_kind, imaps));
+            --t;
+            continue;
+        }
         StepArgs a = base_args(s, nullptr);
         if (nrec > 0 && t >= 1) {
             set_receivers(a, R);

@@ -271,6 +271,24 @@ int fused_step(st_solver* s, StepArgs a, int snap_out, int snap_in, int epi, con
     return ST_OK;
 }
 
+int fused_step2(st_solver* s, StepArgs a, int snap_in, const ImageMaps& imaps) {
+    if (!s->f4) {
+        const size_t fb = (size_t)s->L.elems * sizeof(float);
+        ST_CUDA(cudaMalloc(&s->f4, fb));
+        ST_CUDA(cudaMemsetAsync(s->f4, 0, fb, s->stream));  // its halo stays zero: only interiors are written
+        ST_TRY(build_field_maps(&s->map4, s->f4, s->L));
+    }
+    a.out = s->f[s->in];
+    a.out2 = s->f4;
+    ST_TRY(launch_fd_step2_image(s->L, s->maps[s->ic], s->maps[s->ip], s->map_c, a, snap_in, imaps, s->stream));
+    // cur takes the spare (the field after step t-1), whose old buffer becomes
+    // the spare; prev = the field after step t, and the old prev is free
+    std::swap(s->f[s->ic], s->f4);
+    std::swap(s->maps[s->ic], s->map4);
+    std::swap(s->ip, s->in);
+    return ST_OK;
+}
+
 long long dev_index(const st_solver* s, int64_t ix, int64_t iy, int64_t iz) { return s->L.at(ix, iy, iz); }
 
 // Reference padded index -> device index, -1 when outside the padded array.
@@ -464,6 +482,7 @@ int st_solver_destroy(st_solver* s) {
     cudaSetDevice(s->device);
     clear_snaps(s);
     for (int k = 0; k < 3; ++k) cudaFree(s->f[k]);
+    cudaFree(s->f4);
     cudaFree(s->c);
     cudaFree(s->dtab);
     cudaFree(s->staging);
@@ -748,6 +767,13 @@ int st_solver_get_snapshots(st_solver* s, double* out, int64_t count) {
 int st_solver_fault_stats(st_solver* s, st_fault_stats* out) {
     ST_CHECK(s && out, ST_ERR_ARG, "null argument");
     *out = s->stats;
+    return ST_OK;
+}
+
+int st_solver_set_step_fusion(st_solver* s, int steps) {
+    ST_CHECK(s, ST_ERR_ARG, "null argument");
+    ST_CHECK(steps == 1 || steps == 2, ST_ERR_ARG, "adjoint steps per launch must be 1 or 2 (got %d)", steps);
+    s->adjoint_steps = steps;
     return ST_OK;
 }
 

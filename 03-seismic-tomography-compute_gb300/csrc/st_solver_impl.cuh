@@ -75,6 +75,9 @@ struct st_solver {
     double* dsum = nullptr;
     stg::FieldMaps maps[3];  // TMA maps of f[0..2]
     stg::FieldMaps map_c;    // TMA maps of c
+    float* f4 = nullptr;     // spare field of the two-step imaging launches (allocated on first use)
+    stg::FieldMaps map4;     // its TMA maps
+    int adjoint_steps = 2;   // adjoint steps per imaging launch: 2 (fused pairs) or 1
     bool coeff_dirty = true;
     std::vector<float*> snapshots;  // save_snapshot: interior FP32 copies
     st_fault_stats stats{};
@@ -110,6 +113,9 @@ StepArgs base_args(st_solver* s, float* out);
 // epi: 0 none, 1 imaging, 2 gradient (msnap = the snapshot store's map)
 int fused_step(st_solver* s, StepArgs a, int snap_out, int snap_in, int epi, const CUtensorMap* msnap,
                const ImageMaps* imaps = nullptr);
+// Two adjoint steps with fused imaging in one launch (launch_fd_step2_image):
+// afterwards cur = the field after step t-1 and prev = the field after step t.
+int fused_step2(st_solver* s, StepArgs a, int snap_in, const ImageMaps& imaps);
 int zero_fields(st_solver* s);
 long long dev_index(const st_solver* s, int64_t ix, int64_t iy, int64_t iz);
 bool finite_sample(const double* w, int64_t len, int64_t t, float* out);

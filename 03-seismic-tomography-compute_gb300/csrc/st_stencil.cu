@@ -320,7 +320,7 @@ __device__ __forceinline__ void process_row(const StepArgs& a, const RowCtx& R, 
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 float f = fin[k];
-                float ad = u0[k] / (a.stable_sponge ? cv[k] * D[k] : cv[k]);
+                float ad = __fdividef(u0[k], a.stable_sponge ? cv[k] * D[k] : cv[k]);
                 if (!isfinite(f)) f = 0.0f;
                 if (!isfinite(ad)) ad = 0.0f;
                 im[k] = fmaf(f, ad, im[k]);
@@ -332,7 +332,7 @@ __device__ __forceinline__ void process_row(const StepArgs& a, const RowCtx& R, 
             const float sc = __uint_as_float(*a.amax_in) / SNAP_QMAX;
             for (int k = 0; k < zvalid; ++k) {
                 float f = snap_load<SNAP_IN>(a.snap_in, cbase + k) * sc;
-                float ad = u0[k] / (a.stable_sponge ? cv[k] * D[k] : cv[k]);
+                float ad = __fdividef(u0[k], a.stable_sponge ? cv[k] * D[k] : cv[k]);
                 if (!isfinite(f)) f = 0.0f;
                 if (!isfinite(ad)) ad = 0.0f;
                 a.image[cbase + k] += f * ad;
@@ -686,6 +686,419 @@ int launch_variant(const Layout& L, const FieldMaps& mcur, const FieldMaps& mpre
     return ST_OK;
 }
 
+// ---------------------------------------------------------------- two adjoint steps per launch
+//
+// fd_step2_image_kernel runs the adjoint steps t and t-1 of the imaging pass in
+// one launch: sub-step A computes lambda' = step(lambda_t, lambda_{t+1}) on the
+// 16 x 64 tile plus a one-cell y/z ring (recomputed by every tile that needs
+// it), sub-step B computes lambda'' = step(lambda', lambda_t) on the tile from
+// the ring held in shared memory, and the imaging condition accumulates both
+// steps' terms into one read-modify-write of the image and illumination. Each
+// point is updated by the same arithmetic, in the same order, as two launches
+// of fd_step_kernel<SNAP_NONE, SNAP_IN, EPI_IMAGE_T>, so the results are
+// bit-identical; HBM traffic falls from 2 x 34 to 40 bytes per point (read
+// lambda_t, lambda_{t+1}, c, two snapshots, image, illumination; write
+// lambda', lambda'', image, illumination).
+//
+// Planes i = 0 .. n+3 of a CTA's chunk [xa, xb) (n = xb - xa) are interior
+// x = xa - 2 + i. Stage i of the TMA ring carries lambda_t of plane i (rows
+// y0-2 .. y0+17), lambda_{t+1} and c of plane i (rows y0-1 .. y0+16) and, one
+// plane behind, the two snapshot, image and illumination tiles of interior
+// x = xa - 3 + i. Iteration i runs sub-step A on plane i-1 and sub-step B
+// (with imaging and the stores) on plane i-2.
+template <int SNAP_IN>
+struct Geo2 {
+    static constexpr int TYV = 16;
+    static constexpr int W = TZ + 8;            // z from z0 - 4
+    static constexpr int CUR_H = TYV + 4;       // rows y0 - 2 .. y0 + 17
+    static constexpr int RING_H = TYV + 2;      // rows y0 - 1 .. y0 + 16
+    static constexpr int CUR_BYTES = W * CUR_H * 4;
+    static constexpr int RING_BYTES = W * RING_H * 4;
+    static constexpr int RING_PAD = ((RING_BYTES + 127) / 128) * 128;
+    static constexpr int SNAP_TILE = TZ * TYV * snap_bytes(SNAP_IN);
+    static constexpr int SNAP_PAD = ((SNAP_TILE + 127) / 128) * 128;
+    static constexpr int CTR = TZ * TYV * 4;
+    static constexpr int OFF_PREV = ((CUR_BYTES + 127) / 128) * 128;
+    static constexpr int OFF_C = OFF_PREV + RING_PAD;
+    static constexpr int OFF_SA = OFF_C + RING_PAD;
+    static constexpr int OFF_SB = OFF_SA + SNAP_PAD;
+    static constexpr int OFF_IMG = OFF_SB + SNAP_PAD;
+    static constexpr int OFF_ILL = OFF_IMG + CTR;
+    static constexpr int STAGE_BYTES = OFF_ILL + CTR;
+    static constexpr int TX_FIELDS = CUR_BYTES + 2 * RING_BYTES;
+    static constexpr int TX_IMAGE = 2 * SNAP_TILE + 2 * CTR;
+    static constexpr int STAGES = 3;
+    static constexpr int SMEM = STAGES * STAGE_BYTES + 2 * RING_PAD + EXTRA_BYTES;
+    static constexpr int FIT = SM_SMEM / (SMEM + 1024);
+    static constexpr int MINB = FIT < 4 ? FIT : 4;
+};
+
+// Receiver row index of y (iry) or column index of x (irx) on the receiver
+// grid, or -1.
+__device__ __forceinline__ int rec_line(int v, int v0, int sv, int nv) {
+    const int d = v - v0;
+    if (d < 0 || d % sv) return -1;
+    return d / sv < nv ? d / sv : -1;
+}
+
+// Sponge factor for distance d >= 0 to the nearest face.
+__device__ __forceinline__ float sponge_tab(const StepArgs& a, const float* dtab, int d) {
+    return d < a.sw ? dtab[d] : 1.0f;
+}
+
+__device__ __forceinline__ void ld4(const float* p, float v[4]) { f4_to(*reinterpret_cast<const float4*>(p), v); }
+__device__ __forceinline__ void st4(float* p, const float v[4]) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+
+// Four adjoint point updates in fd_step_kernel's order: the update (the
+// guarded form where the fast one is out of range), the receiver forcing
+// c * force[q] at point rk (rk < 0: none), then the stable damping.
+__device__ __forceinline__ void adj_update4(const StepArgs& a, const float u0[4], const float pv[4],
+                                            const float um[4], const float up[4], const float ym[4],
+                                            const float yp[4], float zm0, float zp3, const float cv[4],
+                                            const float D[4], const float* force, int q, int rk, float res[4],
+                                            int* fired) {
+    float upd[4];
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float zm = k == 0 ? zm0 : u0[k - 1];
+        const float zp = k == 3 ? zp3 : u0[k + 1];
+        upd[k] = D[k] * pv[k];
+        res[k] = update_fast(u0[k], upd[k], um[k], up[k], ym[k], yp[k], zm, zp, cv[k], a.ax, a.ay, a.az);
+        bad = bad || !(fabsf(res[k]) <= a.amp);
+    }
+    if (bad) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (fabsf(res[k]) <= a.amp) continue;
+            const float zm = k == 0 ? zm0 : u0[k - 1];
+            const float zp = k == 3 ? zp3 : u0[k + 1];
+            res[k] = update_guarded(u0[k], upd[k], um[k], up[k], ym[k], yp[k], zm, zp, cv[k], a.ax, a.ay, a.az,
+                                    a.amp, fired);
+        }
+    }
+    if (rk >= 0) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k == rk) res[k] = fmaf(cv[k], force[q], res[k]);
+    }
+    if (a.stable_sponge) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) res[k] *= D[k];
+    }
+}
+
+// Sub-step A on the four z of one row at interior plane x: T is plane x's
+// lambda_t tile, tr the group's offset there (rows from y0 - 2), P / Cc its
+// lambda_{t+1} and c tiles (offset tr - W, rows from y0 - 1); um / up are
+// lambda_t at x - 1 / x + 1; dyz the y/z sponge distances of the four points.
+// Points outside the interior hold 0. Returns c of the four points in cv.
+__device__ __forceinline__ void step2_a_vec(const StepArgs& a, const float* dtab, const float* T, const float* P,
+                                            const float* Cc, int tr, int dx, const int dyz[4], bool far, bool inside,
+                                            const float um[4], const float up[4], int q, int rk, float res[4],
+                                            float cv[4], int* fired) {
+    constexpr int W = TZ + 8;
+    float u0[4], ym[4], yp[4], pv[4], D[4];
+    ld4(Cc + tr - W, cv);
+    if (!inside) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) res[k] = 0.0f;
+        return;
+    }
+    ld4(T + tr, u0);
+    ld4(P + tr - W, pv);
+    ld4(T + tr - W, ym);
+    ld4(T + tr + W, yp);
+    if (far && dx >= a.sw) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) D[k] = 1.0f;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) D[k] = sponge_tab(a, dtab, min(dx, dyz[k]));
+    }
+    adj_update4(a, u0, pv, um, up, ym, yp, T[tr - 1], T[tr + 4], cv, D, a.force_row, q, rk, res, fired);
+}
+
+template <int SNAP_IN>
+__global__ void __launch_bounds__(NTHREADS, (Geo2<SNAP_IN>::MINB))
+    fd_step2_image_kernel(const __grid_constant__ CUtensorMap map_cur, const __grid_constant__ CUtensorMap map_prev,
+                          const __grid_constant__ CUtensorMap map_c, const __grid_constant__ CUtensorMap map_snap,
+                          const __grid_constant__ CUtensorMap map_img, const __grid_constant__ CUtensorMap map_ill,
+                          const StepArgs a) {
+    using G = Geo2<SNAP_IN>;
+    constexpr int W = G::W;
+    constexpr int STAGES = G::STAGES;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float* lbuf = reinterpret_cast<float*>(smem + STAGES * G::STAGE_BYTES);  // two lambda' planes
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + STAGES * G::STAGE_BYTES + 2 * G::RING_PAD);
+    float* dtab_s = reinterpret_cast<float*>(smem + STAGES * G::STAGE_BYTES + 2 * G::RING_PAD + 128);
+
+    const int tid = threadIdx.x;
+    const int tz4 = tid % TZ4;
+    const int yr = tid / TZ4;
+    const int z0 = blockIdx.x * TZ;
+    const int y0 = blockIdx.y * G::TYV;
+    const int xa = blockIdx.z * a.x_chunk;
+    const int xb = min(xa + a.x_chunk, a.nx);
+    if (xa >= xb) return;  // uniform over the CTA
+    const int nplanes = xb - xa + 4;
+
+    // the thread's tasks: the centre group (row yc, z zc .. zc+3); the lanes of
+    // warp 0 also take the ring rows y0-1 (lanes 0-15) and y0+16 (lanes 16-31)
+    // at z-group lane % 16, the lanes of the last warp the ring points z0-1
+    // (even lanes) and z0+64 (odd lanes) of row y0 + lane / 2
+    const int warp = tid >> 5, lane = tid & 31;
+    const int zc = z0 + 4 * tz4;
+    const int yc = y0 + yr;
+    const bool cin = yc < a.ny && zc < a.nz;
+    const bool has_yr = warp == 0;
+    const int zcr = z0 + 4 * (lane & 15);
+    const int yring = lane < 16 ? y0 - 1 : y0 + G::TYV;
+    const bool yrin = has_yr && yring >= 0 && yring < a.ny && zcr < a.nz;
+    const bool has_zr = warp == NTHREADS / 32 - 1;
+    const int yz = y0 + (lane >> 1);
+    const int zring = (lane & 1) ? z0 + TZ : z0 - 1;
+    const bool zrin = has_zr && yz < a.ny && zring >= 0 && zring < a.nz;
+    // y/z distances to the nearest face (sponge), fixed over the march; far_c:
+    // the centre group is beyond the sponge along y and z
+    int dyz_c[4], dyz_r[4];
+    const int dyc = min(yc, a.ny - 1 - yc), dyr = min(yring, a.ny - 1 - yring);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        dyz_c[k] = min(dyc, min(zc + k, a.nz - 1 - (zc + k)));
+        dyz_r[k] = min(dyr, min(zcr + k, a.nz - 1 - (zcr + k)));
+    }
+    const bool far_c = min(min(dyz_c[0], dyz_c[1]), min(dyz_c[2], dyz_c[3])) >= a.sw;
+    const int dyz_z = min(min(yz, a.ny - 1 - yz), min(zring, a.nz - 1 - zring));
+    // receiver rows of the tasks; rk / rkr: the receiver plane's point in the
+    // centre / ring-row group
+    const bool recs = a.force_row || a.force_row2;
+    const int rk = (recs && a.rz >= zc && a.rz < zc + 4) ? a.rz - zc : -1;
+    const int rkr = (recs && has_yr && a.rz >= zcr && a.rz < zcr + 4) ? a.rz - zcr : -1;
+    const int iry_c = rk >= 0 ? rec_line(yc, a.ry0, a.rsy, a.rny) : -1;
+    const int iry_r = rkr >= 0 ? rec_line(yring, a.ry0, a.rsy, a.rny) : -1;
+    const int iry_z = recs && has_zr && zring == a.rz ? rec_line(yz, a.ry0, a.rsy, a.rny) : -1;
+    const bool any_rec = iry_c >= 0 || iry_r >= 0 || iry_z >= 0;
+
+    const bool tab_smem = a.sw <= DTAB_MAX;
+    if (tab_smem)
+        for (int i = tid; i < a.sw; i += NTHREADS) dtab_s[i] = a.dtab[i];
+    const float* dtab = tab_smem ? dtab_s : a.dtab;
+    const float scale_a = __uint_as_float(*a.amax_in) / SNAP_QMAX;
+    const float scale_b = __uint_as_float(*a.amax_in2) / SNAP_QMAX;
+
+    auto st_cur = [&](int s) { return reinterpret_cast<float*>(smem + s * G::STAGE_BYTES); };
+    auto st_prev = [&](int s) { return reinterpret_cast<float*>(smem + s * G::STAGE_BYTES + G::OFF_PREV); };
+    auto st_c = [&](int s) { return reinterpret_cast<float*>(smem + s * G::STAGE_BYTES + G::OFF_C); };
+    auto st_sa = [&](int s) { return smem + s * G::STAGE_BYTES + G::OFF_SA; };
+    auto st_sb = [&](int s) { return smem + s * G::STAGE_BYTES + G::OFF_SB; };
+    auto st_img = [&](int s) { return reinterpret_cast<float*>(smem + s * G::STAGE_BYTES + G::OFF_IMG); };
+    auto st_ill = [&](int s) { return reinterpret_cast<float*>(smem + s * G::STAGE_BYTES + G::OFF_ILL); };
+    auto lb = [&](int i) { return lbuf + (i & 1) * (G::RING_PAD / 4); };
+
+    if (tid == 0) {
+        for (int s = 0; s < STAGES; ++s) mbar_init(&bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    auto issue = [&](int i) {
+        const int s = i % STAGES;
+        const int xd = xa - 1 + i;  // device x of interior plane xa - 2 + i
+        const int xi = xa - 3 + i;  // interior plane of the imaging operands
+        const bool img = xi >= xa && xi < xb;
+        mbar_arrive_expect_tx(&bar[s], G::TX_FIELDS + (img ? G::TX_IMAGE : 0));
+        tma_load_3d(st_cur(s), &map_cur, &bar[s], z0, y0 - 1, xd);
+        tma_load_3d(st_prev(s), &map_prev, &bar[s], z0, y0, xd);
+        tma_load_3d(st_c(s), &map_c, &bar[s], z0, y0, xd);
+        if (img) {
+            tma_load_4d(st_sa(s), &map_snap, &bar[s], z0, y0, xi, a.snap_t);
+            tma_load_4d(st_sb(s), &map_snap, &bar[s], z0, y0, xi, a.snap_t - 1);
+            tma_load_3d(st_img(s), &map_img, &bar[s], z0, y0, xi);
+            tma_load_3d(st_ill(s), &map_ill, &bar[s], z0, y0, xi);
+        }
+    };
+    int issued = 0;
+    if (tid == 0) {
+        issued = min(STAGES, nplanes);
+        for (int i = 0; i < issued; ++i) issue(i);
+    }
+
+    const int tcen = (yr + 2) * W + 4 * tz4 + 4;                 // centre in a lambda_t tile
+    const int tyr = (yring - y0 + 2) * W + (zcr - z0) + 4;       // ring row in a lambda_t tile
+    const int tzr = (yz - y0 + 2) * W + (zring - z0 + 4);        // ring point in a lambda_t tile
+    const int rcen = tcen - W, ryr = tyr - W, rzr = tzr - W;     // the same in ring-geometry tiles
+    const int ccen = yr * TZ + 4 * tz4;                          // centre in the compact tiles
+    // lambda_t queues (x-1, x, x+1) of the three tasks, lambda' queue of the
+    // centre (planes i-3, i-2, i-1) and c of the centre at plane i-2
+    float um[4] = {0, 0, 0, 0}, u0[4] = {0, 0, 0, 0};
+    float rm[4] = {0, 0, 0, 0}, r0[4] = {0, 0, 0, 0};
+    float zm_ = 0.0f, z0_ = 0.0f;
+    float lm[4] = {0, 0, 0, 0}, l0[4] = {0, 0, 0, 0};
+    float cprev[4] = {0, 0, 0, 0};
+    int irx_prev = -1;  // receiver column of plane i-2
+    int fired = 0;
+    int timed_out = 0;
+
+    int i = 0;
+    for (; i < nplanes; ++i) {
+        const int s = i % STAGES;
+        if (!mbar_wait_bounded(&bar[s], (i / STAGES) & 1, a.timeout_ns)) timed_out = 1;
+        float up[4], rp[4] = {0, 0, 0, 0}, zp_ = 0.0f;
+        ld4(st_cur(s) + tcen, up);
+        if (has_yr) ld4(st_cur(s) + tyr, rp);
+        if (has_zr) zp_ = st_cur(s)[tzr];
+        float lp[4] = {0, 0, 0, 0}, cnow[4] = {0, 0, 0, 0};
+        int irx = -1;
+        if (i >= 2) {
+            // sub-step A on plane i-1 (interior x = xa - 3 + i); it writes the
+            // ring buffer of plane i-1, which no thread reads before the
+            // barrier that ends this iteration
+            const int sp = (i - 1) % STAGES;
+            const int x = xa - 3 + i;
+            const bool xin = x >= 0 && x < a.nx;
+            const int dx = min(x, a.nx - 1 - x);
+            if (any_rec && xin) irx = rec_line(x, a.rx0, a.rsx, a.rnx);
+            const int irx_a = a.force_row ? irx : -1;  // step t's forcing
+            const float* T = st_cur(sp);
+            const float* P = st_prev(sp);
+            const float* Cc = st_c(sp);
+            float* Lw = lb(i - 1);
+            const bool rc = irx_a >= 0 && iry_c >= 0;
+            step2_a_vec(a, dtab, T, P, Cc, tcen, dx, dyz_c, far_c, xin && cin, um, up, rc ? irx_a * a.rny + iry_c : 0,
+                        rc ? rk : -1, lp, cnow, &fired);
+            st4(Lw + rcen, lp);
+            if (has_yr) {
+                float res[4], cv_[4];
+                const bool rr = irx_a >= 0 && iry_r >= 0;
+                step2_a_vec(a, dtab, T, P, Cc, tyr, dx, dyz_r, false, xin && yrin, rm, rp, rr ? irx_a * a.rny + iry_r : 0,
+                            rr ? rkr : -1, res, cv_, &fired);
+                st4(Lw + ryr, res);
+            }
+            if (has_zr) {
+                float res = 0.0f;
+                if (xin && zrin) {
+                    const float D = sponge_tab(a, dtab, min(dx, dyz_z));
+                    const float u = T[tzr], c = Cc[rzr];
+                    const float upd = D * P[rzr];
+                    const float ym = T[tzr - W], yp = T[tzr + W], zm = T[tzr - 1], zp = T[tzr + 1];
+                    res = update_fast(u, upd, zm_, zp_, ym, yp, zm, zp, c, a.ax, a.ay, a.az);
+                    if (!(fabsf(res) <= a.amp))
+                        res = update_guarded(u, upd, zm_, zp_, ym, yp, zm, zp, c, a.ax, a.ay, a.az, a.amp, &fired);
+                    if (irx_a >= 0 && iry_z >= 0) res = fmaf(c, a.force_row[irx_a * a.rny + iry_z], res);
+                    if (a.stable_sponge) res *= D;
+                }
+                Lw[rzr] = res;
+            }
+        }
+        if (i >= 4 && cin) {
+            // sub-step B, imaging and stores on plane i-2 (interior x = xa - 4 + i),
+            // from the ring buffer of plane i-2 (complete since the last barrier)
+            const int x = xa - 4 + i;
+            const float* Lr = lb(i - 2);
+            const int dx = min(x, a.nx - 1 - x);
+            float ym[4], yp[4], D[4], res[4];
+            ld4(Lr + rcen - W, ym);
+            ld4(Lr + rcen + W, yp);
+            if (far_c && dx >= a.sw) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) D[k] = 1.0f;
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) D[k] = sponge_tab(a, dtab, min(dx, dyz_c[k]));
+            }
+            const bool rc = a.force_row2 && irx_prev >= 0 && iry_c >= 0;
+            adj_update4(a, l0, um, lm, lp, ym, yp, Lr[rcen - 1], Lr[rcen + 4], cprev, D, a.force_row2,
+                        rc ? irx_prev * a.rny + iry_c : 0, rc ? rk : -1, res, &fired);
+            const long long ob = (long long)(x + 1) * a.plane + (long long)(yc + 1) * a.NZP + zc + Layout::ZOFF;
+            st4(a.out + ob, l0);
+            st4(a.out2 + ob, res);
+            // imaging: step t pairs lambda_t with the snapshot of t, step t-1
+            // pairs lambda' with the snapshot of t-1, in that order
+            const int sp = (i - 1) % STAGES;
+            float fa[4], fb[4], im[4], il[4];
+            snap_smem4<SNAP_IN>(st_sa(sp), ccen, fa);
+            snap_smem4<SNAP_IN>(st_sb(sp), ccen, fb);
+            ld4(st_img(sp) + ccen, im);
+            ld4(st_ill(sp) + ccen, il);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float w = a.stable_sponge ? cprev[k] * D[k] : cprev[k];
+                float f = fa[k] * scale_a;
+                float ad = __fdividef(um[k], w);
+                if (!isfinite(f)) f = 0.0f;
+                if (!isfinite(ad)) ad = 0.0f;
+                im[k] = fmaf(f, ad, im[k]);
+                il[k] = fmaf(f, f, il[k]);
+                f = fb[k] * scale_b;
+                ad = __fdividef(l0[k], w);
+                if (!isfinite(f)) f = 0.0f;
+                if (!isfinite(ad)) ad = 0.0f;
+                im[k] = fmaf(f, ad, im[k]);
+                il[k] = fmaf(f, f, il[k]);
+            }
+            const long long cb = ((long long)x * a.ny + yc) * a.nz + zc;
+            st4(a.image + cb, im);
+            st4(a.illum + cb, il);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            um[k] = u0[k];
+            u0[k] = up[k];
+            rm[k] = r0[k];
+            r0[k] = rp[k];
+            lm[k] = l0[k];
+            l0[k] = lp[k];
+            cprev[k] = cnow[k];
+        }
+        zm_ = z0_;
+        z0_ = zp_;
+        irx_prev = irx;
+        // every thread is done with the slot of plane i-1 and the ring buffer
+        // of plane i-2: refill the one, let the next iteration overwrite the other
+        if (__syncthreads_or(timed_out)) break;
+        if (tid == 0 && i >= 1 && issued < nplanes) issue(issued++);
+    }
+
+    if (i < nplanes) {
+        // A wait gave up: drain the copies still in flight (bounded), then leave.
+        if (tid == 0) {
+            for (int j = i; j < issued; ++j) mbar_wait_bounded(&bar[j % STAGES], (j / STAGES) & 1, a.timeout_ns);
+            atomicOr(a.flags, FLAG_TIMEOUT);
+        }
+        __syncthreads();
+        return;
+    }
+    if (fired) atomicOr(a.flags, FLAG_GUARD);
+}
+
+template <int SI>
+int launch_step2_variant(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
+                         const ImageMaps& im, StepArgs a, cudaStream_t st) {
+    using G = Geo2<SI>;
+    static bool configured = false;
+    static std::mutex mu;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!configured) {
+            ST_CUDA(cudaFuncSetAttribute(fd_step2_image_kernel<SI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         G::SMEM));
+            configured = true;
+        }
+    }
+    const int chunks = fd_step_grid_chunks(L, G::TYV, G::MINB, 1, 4);
+    a.x_chunk = (int)((L.nx + chunks - 1) / chunks);
+    const int nch = (int)((L.nx + a.x_chunk - 1) / a.x_chunk);
+    dim3 grid((unsigned)((L.nz + TZ - 1) / TZ), (unsigned)((L.ny + G::TYV - 1) / G::TYV), (unsigned)nch);
+    fd_step2_image_kernel<SI><<<grid, NTHREADS, G::SMEM, st>>>(mcur.cur2, mprev.cur[0], mc.cur[0], im.snap, im.image,
+                                                              im.illum, a);
+    ::stg::count_launch();
+    ST_CUDA(cudaGetLastError());
+    return ST_OK;
+}
+
 int num_sms() {
     static int n = 0;
     if (n == 0) {
@@ -864,10 +1277,11 @@ int build_field_maps(FieldMaps* m, const float* base, const Layout& L) {
         ST_TRY(make_field_map(&m->cur[t], base, L, TZ + 8, rows + 2));
         ST_TRY(make_field_map(&m->ctr[t], base, L, TZ, rows));
     }
+    ST_TRY(make_field_map(&m->cur2, base, L, TZ + 8, 16 + 4));
     return ST_OK;
 }
 
-int fd_step_grid_chunks(const Layout& L, int tyv, int minb, int min_waves) {
+int fd_step_grid_chunks(const Layout& L, int tyv, int minb, int min_waves, int halo) {
     const long long gx = (L.nz + TZ - 1) / TZ, gy = (L.ny + tyv - 1) / tyv;
     const long long tiles = gx * gy;
     // tuning override: SEISMIC_GB300_XCHUNKS=<chunks> (1..nx)
@@ -876,7 +1290,7 @@ int fd_step_grid_chunks(const Layout& L, int tyv, int minb, int min_waves) {
         if (v >= 1) return (int)std::min<long long>(v, L.nx);
     }
     // Split the x range into chunks so that the CTA count fills whole waves of
-    // resident CTAs (SMs x resident CTAs per SM); each chunk re-reads two halo
+    // resident CTAs (SMs x resident CTAs per SM); each chunk re-reads `halo`
     // planes, a cost weighed in against shorter chunks.
     const double slots = (double)num_sms() * minb;
     long long best = 1;
@@ -888,7 +1302,7 @@ int fd_step_grid_chunks(const Layout& L, int tyv, int minb, int min_waves) {
         const double waves = (double)(tiles * ch) / slots;
         const double fill = waves / std::ceil(waves);
         const double len = std::ceil((double)L.nx / (double)ch);
-        const double eff = fill / (1.0 + 2.0 / len);
+        const double eff = fill / (1.0 + (double)halo / len);
         if (eff > best_eff + 1e-9) {
             best_eff = eff;
             best = ch;
@@ -957,6 +1371,27 @@ int launch_fd_step(const Layout& L, const FieldMaps& mcur, const FieldMaps& mpre
         case SNAP_FP16: return launch_variant<SNAP_FP16, SNAP_NONE, EPI_NONE>(L, mcur, mprev, mc, ms, a, st);
         case SNAP_FP32: return launch_variant<SNAP_FP32, SNAP_NONE, EPI_NONE>(L, mcur, mprev, mc, ms, a, st);
         default: ST_CHECK(false, ST_ERR_ARG, "bad snapshot kind %d", snap_out);
+    }
+}
+
+int launch_fd_step2_image(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
+                          StepArgs a, int snap_in, const ImageMaps& imaps, cudaStream_t st) {
+    a.nx = (int)L.nx;
+    a.ny = (int)L.ny;
+    a.nz = (int)L.nz;
+    a.NZP = (int)L.NZP;
+    a.plane = L.plane;
+    if (a.timeout_ns == 0) a.timeout_ns = 2000000000ull;
+    ST_CHECK(image_maps_supported(snap_in, L), ST_ERR_UNSUPPORTED, "two-step imaging needs staged image maps");
+    ST_CHECK(a.out && a.out2 && a.image && a.illum && a.amax_in && a.amax_in2 && a.snap_t >= 1, ST_ERR_ARG,
+             "two-step imaging: missing operands");
+    ST_CHECK(!a.zlim && !a.seis_row && !a.snap_out && a.inj_x < 0, ST_ERR_UNSUPPORTED,
+             "two-step imaging: adjoint steps only");
+    switch (snap_in) {
+        case SNAP_BF16: return launch_step2_variant<SNAP_BF16>(L, mcur, mprev, mc, imaps, a, st);
+        case SNAP_FP16: return launch_step2_variant<SNAP_FP16>(L, mcur, mprev, mc, imaps, a, st);
+        case SNAP_FP32: return launch_step2_variant<SNAP_FP32>(L, mcur, mprev, mc, imaps, a, st);
+        default: ST_CHECK(false, ST_ERR_ARG, "imaging step needs a snapshot kind");
     }
 }
 

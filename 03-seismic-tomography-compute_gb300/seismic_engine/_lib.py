@@ -125,6 +125,7 @@ SIGNATURES = {
     "st_solver_get_snapshots": [_vp, _d, C.c_int64],
     "st_solver_fault_stats": [_vp, C.POINTER(FaultStatsC)],
     "st_solver_device_field": [_vp, C.c_int, C.POINTER(_vp)],
+    "st_solver_set_step_fusion": [_vp, C.c_int],
     "st_solver_stream": [_vp, C.POINTER(_vp)],
     "st_solver_last_phase_ms": [_vp, C.POINTER(C.c_float)],
     "st_launch_count": [C.POINTER(C.c_longlong)],

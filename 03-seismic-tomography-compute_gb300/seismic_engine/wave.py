@@ -304,6 +304,11 @@ class WaveEquationSolver:
             self._slices = None
 
     # ---- GB300 additions
+    def set_step_fusion(self, steps: int):
+        """Adjoint steps per launch of the RTM imaging pass: 2 (default) or 1;
+        the results are bit-identical either way."""
+        call("st_solver_set_step_fusion", self._h, int(steps))
+
     def device_field_ptr(self, which: int) -> int:
         p = C.c_void_p()
         call("st_solver_device_field", self._h, which, C.byref(p))

@@ -170,8 +170,15 @@ int st_solver_fault_stats(st_solver* s, st_fault_stats* out);
 
 /* ----------------------------------------------------- GB300 shot entry points */
 /* Device pointers to the solver's fields in the device layout (for zero-copy
- * torch views): which = ST_FIELD_*. */
+ * torch views): which = ST_FIELD_*. Valid until the next call that steps the
+ * solver (the imaging pass exchanges field buffers). */
 int st_solver_device_field(st_solver* s, int which, float** out);
+/* Adjoint time steps per launch of the RTM imaging pass (st_rtm_shot and its
+ * host variant): 2 (default) runs steps t and t-1 in one launch with the
+ * imaging of both fused, 1 one step per launch; the image, illumination and
+ * fields are bit-identical either way. The imaging pass of
+ * RTMEngine::process_shot (rtm/rtm_engine.cpp:59-110), restructured. */
+int st_solver_set_step_fusion(st_solver* s, int steps);
 /* The CUDA stream the handle orders its work on (a cudaStream_t). */
 int st_solver_stream(st_solver* s, void** out);
 /* Device time of the two phases of the last st_rtm_shot on this handle, from

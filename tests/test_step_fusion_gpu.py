@@ -1,0 +1,101 @@
+"""The RTM imaging pass with two adjoint steps per launch against one step
+per launch, through the C ABI: image, illumination and the final adjoint
+fields must be bit-identical (each point is updated by the same arithmetic in
+the same order), for odd and even step counts, both sponge rules, every
+snapshot kind, receivers whose forcing lands on the recomputed ring of a
+tile, grids that end inside a tile, and different x-chunkings of the grid.
+The two-step path is also the default one the oracle parity tests of
+test_rtm_gpu.py run."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def se():
+    import importlib.util
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location(
+        "st_build", os.path.join(repo, "03-seismic-tomography-compute_gb300", "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.build()
+    import seismic_engine
+    return seismic_engine
+
+
+def run_rtm(se, n, nt, sponge, rec_z, kind, steps, seed=3):
+    import torch
+    nx, ny, nz = n
+    rng = np.random.default_rng(seed)
+    vel = 1500.0 + 1500.0 * rng.random((nx, ny, nz))
+    d = 10.0
+    dt = se.workloads.cfl_dt(d, 3000.0)
+    s = se.WaveEquationSolver(se.GridParams(nx, ny, nz, d, d, d),
+                              se.SolverConfig(dt=dt, nt=nt, sponge_width=6, sponge_damping=0.015))
+    try:
+        s.set_sponge_mode(sponge)
+        s.set_velocity_field(se.workloads.to_reference_layout(vel))
+        s.set_step_fusion(steps)
+        rec = se.workloads.ReceiverGrid(1, 2, (nx - 2) // 2, 0, 1, ny, rec_z)
+        data = torch.from_numpy((rng.standard_normal((nt, rec.count)) * 1e-3).astype(np.float32)).cuda()
+        wav = se.workloads.ricker(25.0, dt, nt)
+        image = torch.zeros(nx * ny * nz, device="cuda")
+        illum = torch.zeros(nx * ny * nz, device="cuda")
+        # the source sits three cells from the receiver plane, so that the
+        # forward and adjoint fields overlap within a few steps
+        src_z = rec_z - 3 if rec_z >= 3 else rec_z + 3
+        assert se.rtm_shot(s, (nx // 2, ny // 2, src_z), wav, nt, rec, data, image, illum, snap_kind=kind) == 0
+        torch.cuda.synchronize()
+        return (image.cpu().numpy(), illum.cpu().numpy(), s.get_field(0), s.get_field(1))
+    finally:
+        s.close()
+
+
+# nz is a multiple of 8 throughout: 16-bit snapshot rows are then whole
+# 16-byte units, the condition for the staged (and two-step) imaging path
+CASES = [
+    # (nx, ny, nz), nt, sponge rule, receiver plane z
+    ((28, 24, 32), 41, "reference", 5),
+    ((40, 20, 72), 40, "stable", 63),   # second z tile holds 8 z; forcing on its ring point z0 - 1
+    ((70, 33, 64), 23, "stable", 31),   # third y tile holds one row
+    ((9, 17, 40), 12, "stable", 39),    # forcing on the last z; ring rows y0 - 1 / y0 + 16 carry receivers
+]
+
+
+@pytest.mark.parametrize("n,nt,sponge,rec_z", CASES)
+def test_two_steps_per_launch_bit_identical(se, n, nt, sponge, rec_z):
+    one = run_rtm(se, n, nt, sponge, rec_z, 1, steps=1)
+    two = run_rtm(se, n, nt, sponge, rec_z, 1, steps=2)
+    assert np.abs(one[0]).max() > 0 and np.abs(one[1]).max() > 0
+    for a, b, what in zip(one, two, ("image", "illumination", "current field", "previous field")):
+        assert np.array_equal(a, b), f"{what}: max |diff| {np.abs(a - b).max():.3e}"
+
+
+@pytest.mark.parametrize("kind", [2, 3])
+def test_two_steps_per_launch_snapshot_kinds(se, kind):
+    one = run_rtm(se, (28, 24, 32), 30, "stable", 5, kind, steps=1)
+    two = run_rtm(se, (28, 24, 32), 30, "stable", 5, kind, steps=2)
+    for a, b in zip(one, two):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("chunks", ["1", "3", "7"])
+def test_two_steps_per_launch_any_chunking(se, monkeypatch, chunks):
+    base = run_rtm(se, (40, 20, 72), 17, "stable", 63, 1, steps=1)
+    monkeypatch.setenv("SEISMIC_GB300_XCHUNKS", chunks)
+    two = run_rtm(se, (40, 20, 72), 17, "stable", 63, 1, steps=2)
+    for a, b in zip(base, two):
+        assert np.array_equal(a, b)
+
+
+def test_step_fusion_argument_checked(se):
+    s = se.WaveEquationSolver(se.GridParams(8, 8, 8, 10.0, 10.0, 10.0), se.SolverConfig(dt=1e-3, nt=4))
+    try:
+        with pytest.raises(Exception):
+            s.set_step_fusion(3)
+    finally:
+        s.close()
