@@ -37,6 +37,9 @@ import numpy as np  # noqa: E402
 
 ALG_BYTES_FWD = 18   # read u, prev, c + write out (16) + BF16 snapshot store (2)
 ALG_BYTES_BWD = 34   # 16 + BF16 snapshot read (2) + image and illumination read-modify-write (16)
+# two adjoint steps per launch: read lambda_t, lambda_{t+1}, c (12) + two BF16 snapshots (4) + image and
+# illumination read-modify-write (16) + write both steps' fields (8), per point per launch
+ALG_BYTES_BWD2 = 40
 METRIC = "stencil Gpts/s"
 
 
@@ -49,6 +52,8 @@ def parse():
     ap.add_argument("--nt", type=int, default=2000, help="time steps per shot (2000 = the workload)")
     ap.add_argument("--n", type=int, default=256, help="grid edge (256 = the workload)")
     ap.add_argument("--snap", choices=["bf16", "fp16", "fp32"], default="bf16")
+    ap.add_argument("--adjoint-steps", type=int, choices=[1, 2], default=2,
+                    help="adjoint time steps per launch of the imaging pass (results are identical)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU sample time")
@@ -440,6 +445,7 @@ def run_gpu(args):
     cfg = se.SolverConfig(dt=w.dt, nt=w.nt, sponge_width=w.sponge_width, sponge_damping=w.sponge_damping,
                           sponge_mode=w.sponge_mode)
     s = se.WaveEquationSolver(grid, cfg, device=torch.cuda.current_device())
+    s.set_step_fusion(args.adjoint_steps)
     vel_true = se.workloads.to_reference_layout(w.vel)
     vel_mig = se.workloads.to_reference_layout(w.vel_migration)
     # observed data (input preparation, untimed)
@@ -486,12 +492,20 @@ def run_gpu(args):
     pts_step = 2.0 * w.nt * npts
     value = world * pts_step * args.steps / (el_ms / 1e3) / 1e9
     hbm_peak, peak_kind = measured_peaks()
-    bwd_launch_ms = statistics.mean(bwd_ms) / w.nt
+    # the imaging pass runs nt / 2 two-step launches (an odd nt adds one single step)
+    paired = args.adjoint_steps == 2 and w.nt % 2 == 0 and w.nz % 8 == 0
+    if paired:
+        bwd_kernel = "fd_step2_image_kernel<BF16> (two adjoint steps + imaging)"
+        bwd_bytes, bwd_launches, traffic_key = ALG_BYTES_BWD2, w.nt // 2, "fd_step2_image_bf16_256"
+    else:
+        bwd_kernel = "fd_step_kernel<SNAP_NONE, BF16, imaging> (adjoint step + imaging)"
+        bwd_bytes, bwd_launches, traffic_key = ALG_BYTES_BWD, w.nt, "fd_step_adjoint_image_bf16_256"
+    bwd_launch_ms = statistics.mean(bwd_ms) / bwd_launches
     fwd_launch_ms = statistics.mean(fwd_ms) / w.nt
-    bw_bwd = ALG_BYTES_BWD * npts / (bwd_launch_ms / 1e3) / 1e9
+    bw_bwd = bwd_bytes * npts / (bwd_launch_ms / 1e3) / 1e9
     bw_fwd = ALG_BYTES_FWD * npts / (fwd_launch_ms / 1e3) / 1e9
-    alg_total = (ALG_BYTES_FWD + ALG_BYTES_BWD) * npts * w.nt * args.steps
-    traffic = profile_traffic("fd_step_adjoint_image_bf16_256")
+    alg_total = (ALG_BYTES_FWD * w.nt + bwd_bytes * bwd_launches) * npts * args.steps
+    traffic = profile_traffic(traffic_key) if args.snap == "bf16" and w.nx == 256 else None
     line = {
         "metric": METRIC, "value": value, "unit": "Gpts/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": el_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -499,10 +513,11 @@ def run_gpu(args):
         "data": "synthetic (seeded layered model + Gaussian anomalies, Ricker source)",
         "config": config_dict(w, args.snap, world),
         "hbm_gbs_algorithmic": alg_total / (el_ms / 1e3) / 1e9,
-        "roofline": {"bound": "hbm", "kernel": "fd_step_kernel<SNAP_NONE, BF16, imaging> (adjoint step + imaging)",
+        "roofline": {"bound": "hbm", "kernel": bwd_kernel,
                      "achieved": bw_bwd, "peak": hbm_peak, "unit": "GB/s", "frac": bw_bwd / hbm_peak,
                      "peak_kind": f"{peak_kind} copy bandwidth", "traffic": traffic,
-                     "alg_bytes_per_launch": ALG_BYTES_BWD * npts, "launch_ms": bwd_launch_ms},
+                     "alg_bytes_per_launch": bwd_bytes * npts, "launch_ms": bwd_launch_ms,
+                     "steps_per_launch": 2 if paired else 1},
         "roofline_forward": {"bound": "hbm", "kernel": "fd_step_kernel<BF16, NONE> (forward step + snapshot store)",
                              "achieved": bw_fwd, "peak": hbm_peak, "unit": "GB/s", "frac": bw_fwd / hbm_peak,
                              "alg_bytes_per_launch": ALG_BYTES_FWD * npts, "launch_ms": fwd_launch_ms},
