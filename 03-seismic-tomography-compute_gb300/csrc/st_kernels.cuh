@@ -35,11 +35,20 @@ struct StepArgs {
     int stable_sponge;       // 1: out = D * (update + forcing) (damped new field), 0: the reference rule
     const int* zlim;         // terrain: per (x, y) column (x * ny + y), points with z < zlim are set to 0
                              // after the update (free surface / seafloor masks), or null
-    // two-step imaging launch only: the second step's output field, forcing
-    // row and snapshot scale
+    // two-step launches only: the second step's output field; adjoint: its
+    // forcing row and snapshot scale; forward: its receiver samples, source
+    // injection (inj_steps bit 0: the first step injects inj_val, bit 1: the
+    // second inj_val2, both at inj_x/y/z), the snapshot of the previous field
+    // (snap_out2, scale amax_cur2) and the max of the second output (amax_next2)
     float* out2;
     const float* force_row2;
     const unsigned* amax_in2;
+    float* seis_row2;
+    int inj_steps;
+    float inj_val2;
+    void* snap_out2;
+    const unsigned* amax_cur2;
+    unsigned* amax_next2;
 };
 
 // Sponge factor of interior point (ix, iy, iz): D(d) for the distance d to the
@@ -99,6 +108,14 @@ int launch_fd_step(const Layout& L, const FieldMaps& mcur, const FieldMaps& mpre
 // staged image maps (nz % 4 == 0).
 int launch_fd_step2_image(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
                           StepArgs a, int snap_in, const ImageMaps& imaps, cudaStream_t st);
+// Launch two forward steps t, t+1 (fd_step2_kernel, forward mode): reads
+// cur = u_t, prev = u_{t-1}; writes a.out = u_{t+1}, a.out2 = u_{t+2};
+// samples a.seis_row / a.seis_row2; injects per a.inj_steps; with snapshots
+// stores u_t to a.snap_out (scale a.amax_cur) and u_{t-1} to a.snap_out2
+// (scale a.amax_cur2, when not null) and max-reduces |u_{t+1}|, |u_{t+2}|
+// into a.amax_next, a.amax_next2. Needs nz % 4 == 0.
+int launch_fd_step2_forward(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
+                            StepArgs a, int snap_out, cudaStream_t st);
 // 4-D map over a snapshot store for the gradient step's halo tile.
 int build_snap_map_grad(CUtensorMap* m, const void* base, int kind, const Layout& L, long long nt);
 
@@ -116,6 +133,9 @@ int launch_vel_to_coeff(const double* vel_ref, float* c, const Layout& L, double
 int launch_count_nonfinite(const float* f, long long n, unsigned long long* out, cudaStream_t st);
 int launch_sumsq_finite(const float* f, long long n, double* out, cudaStream_t st);
 int launch_interior_copy(const float* f, const Layout& L, float* out, cudaStream_t st);
+// Snapshot of field f (device layout) with scale amax, as the stepping kernels store it.
+int launch_snapshot_of_field(const float* f, const Layout& L, void* snap, int kind, const unsigned* amax,
+                             cudaStream_t st);
 int launch_finalize_image(const float* image, const float* illum, float* refl, long long n, cudaStream_t st);
 int launch_scatter_scaled(float* f, const long long* idx, int n, const float* val, const float* c,
                           cudaStream_t st);

@@ -110,7 +110,50 @@ int shot_forward_impl(st_solver* s, const st_shot* shot, float* seis, int snap_k
     float w = 0.0f;
     if (nt > 0 && finite_sample(shot->wavelet, shot->wavelet_len, 0, &w))
         ST_TRY(launch_add_point(s->f[s->ic], src, w, snap_kind != SNAP_NONE ? amax : nullptr, s->stream));
+    // pairs of steps share one launch unless a step's field is needed on its
+    // own (slice capture) or a terrain is attached; a pair leaves the snapshot
+    // of its first output pending: the next pair stores it from its previous
+    // field, a single step or the end of the pass stores it here
+    const bool pairs = s->fused_steps == 2 && !s->zlim && !(slices && s->slices) && L.nz % 4 == 0;
+    bool pending = false;
+    auto store_pending = [&](int t) -> int {
+        if (!pending) return ST_OK;
+        pending = false;
+        return launch_snapshot_of_field(s->f[s->ip], L, static_cast<char*>(snaps) + (size_t)(t - 1) * per,
+                                        snap_kind, amax + t - 1, s->stream);
+    };
     for (int t = 0; t < nt; ++t) {
+        if (pairs && t + 1 < nt) {
+            StepArgs a = base_args(s, nullptr);
+            float w1 = 0.0f, w2 = 0.0f;
+            const bool i1 = finite_sample(shot->wavelet, shot->wavelet_len, t + 1, &w1);
+            const bool i2 = t + 2 < nt && finite_sample(shot->wavelet, shot->wavelet_len, t + 2, &w2);
+            if (i1 || i2) {
+                set_injection(a, shot->src_ix, shot->src_iy, shot->src_iz, w1);
+                a.inj_val2 = w2;
+                a.inj_steps = (i1 ? 1 : 0) | (i2 ? 2 : 0);
+            }
+            if (nrec > 0 && seis) {
+                set_receivers(a, R);
+                a.seis_row = seis + (size_t)t * (size_t)nrec;
+                a.seis_row2 = seis + (size_t)(t + 1) * (size_t)nrec;
+            }
+            if (snap_kind != SNAP_NONE) {
+                a.snap_out = static_cast<char*>(snaps) + (size_t)t * per;
+                a.amax_cur = amax + t;
+                if (pending) {
+                    a.snap_out2 = static_cast<char*>(snaps) + (size_t)(t - 1) * per;
+                    a.amax_cur2 = amax + t - 1;
+                }
+                a.amax_next = amax + t + 1;
+                a.amax_next2 = amax + t + 2;
+                pending = true;
+            }
+            ST_TRY(fused_step2_forward(s, a, snap_kind));
+            ++t;
+            continue;
+        }
+        if (snap_kind != SNAP_NONE) ST_TRY(store_pending(t));
         StepArgs a = base_args(s, nullptr);
         float wn = 0.0f;
         if (t + 1 < nt && finite_sample(shot->wavelet, shot->wavelet_len, t + 1, &wn))
@@ -130,6 +173,7 @@ int shot_forward_impl(st_solver* s, const st_shot* shot, float* seis, int snap_k
             ST_TRY(slice_stream_capture(s->slices, S, t, s->stream));
         }
     }
+    if (snap_kind != SNAP_NONE) ST_TRY(store_pending(nt));
     return ST_OK;
 }
 
@@ -170,7 +214,7 @@ int rtm_backward_impl(st_solver* s, const st_shot* shot, const float* data, int 
     const long long q_src = receiver_at(R, shot->src_ix, shot->src_iy, shot->src_iz);
     // pairs of steps share one launch unless a step's field is needed on its
     // own (slice capture, source trace)
-    const bool pairs = staged && s->adjoint_steps == 2 && !s->slices && !src_trace;
+    const bool pairs = staged && s->fused_steps == 2 && !s->slices && !src_trace;
     for (int t = nt - 1; t >= 0; --t) {
         if (pairs && t >= 1) {
             StepArgs a = base_args(s, nullptr);

@@ -271,21 +271,40 @@ int fused_step(st_solver* s, StepArgs a, int snap_out, int snap_in, int epi, con
     return ST_OK;
 }
 
-int fused_step2(st_solver* s, StepArgs a, int snap_in, const ImageMaps& imaps) {
-    if (!s->f4) {
-        const size_t fb = (size_t)s->L.elems * sizeof(float);
-        ST_CUDA(cudaMalloc(&s->f4, fb));
-        ST_CUDA(cudaMemsetAsync(s->f4, 0, fb, s->stream));  // its halo stays zero: only interiors are written
-        ST_TRY(build_field_maps(&s->map4, s->f4, s->L));
-    }
-    a.out = s->f[s->in];
-    a.out2 = s->f4;
-    ST_TRY(launch_fd_step2_image(s->L, s->maps[s->ic], s->maps[s->ip], s->map_c, a, snap_in, imaps, s->stream));
-    // cur takes the spare (the field after step t-1), whose old buffer becomes
-    // the spare; prev = the field after step t, and the old prev is free
+namespace {
+int ensure_spare(st_solver* s) {
+    if (s->f4) return ST_OK;
+    const size_t fb = (size_t)s->L.elems * sizeof(float);
+    ST_CUDA(cudaMalloc(&s->f4, fb));
+    ST_CUDA(cudaMemsetAsync(s->f4, 0, fb, s->stream));  // its halo stays zero: only interiors are written
+    return build_field_maps(&s->map4, s->f4, s->L);
+}
+
+// After a two-step launch (first output in f[in], second in the spare): cur
+// takes the spare, whose old buffer (the old cur) becomes the spare; prev =
+// the first output, and the old prev is free.
+void rotate_after_pair(st_solver* s) {
     std::swap(s->f[s->ic], s->f4);
     std::swap(s->maps[s->ic], s->map4);
     std::swap(s->ip, s->in);
+}
+}  // namespace
+
+int fused_step2(st_solver* s, StepArgs a, int snap_in, const ImageMaps& imaps) {
+    ST_TRY(ensure_spare(s));
+    a.out = s->f[s->in];
+    a.out2 = s->f4;
+    ST_TRY(launch_fd_step2_image(s->L, s->maps[s->ic], s->maps[s->ip], s->map_c, a, snap_in, imaps, s->stream));
+    rotate_after_pair(s);
+    return ST_OK;
+}
+
+int fused_step2_forward(st_solver* s, StepArgs a, int snap_out) {
+    ST_TRY(ensure_spare(s));
+    a.out = s->f[s->in];
+    a.out2 = s->f4;
+    ST_TRY(launch_fd_step2_forward(s->L, s->maps[s->ic], s->maps[s->ip], s->map_c, a, snap_out, s->stream));
+    rotate_after_pair(s);
     return ST_OK;
 }
 
@@ -772,8 +791,8 @@ int st_solver_fault_stats(st_solver* s, st_fault_stats* out) {
 
 int st_solver_set_step_fusion(st_solver* s, int steps) {
     ST_CHECK(s, ST_ERR_ARG, "null argument");
-    ST_CHECK(steps == 1 || steps == 2, ST_ERR_ARG, "adjoint steps per launch must be 1 or 2 (got %d)", steps);
-    s->adjoint_steps = steps;
+    ST_CHECK(steps == 1 || steps == 2, ST_ERR_ARG, "time steps per launch must be 1 or 2 (got %d)", steps);
+    s->fused_steps = steps;
     return ST_OK;
 }
 

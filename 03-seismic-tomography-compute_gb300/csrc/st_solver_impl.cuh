@@ -77,7 +77,7 @@ struct st_solver {
     stg::FieldMaps map_c;    // TMA maps of c
     float* f4 = nullptr;     // spare field of the two-step imaging launches (allocated on first use)
     stg::FieldMaps map4;     // its TMA maps
-    int adjoint_steps = 2;   // adjoint steps per imaging launch: 2 (fused pairs) or 1
+    int fused_steps = 2;     // time steps per launch of the shot-level passes: 2 (fused pairs) or 1
     bool coeff_dirty = true;
     std::vector<float*> snapshots;  // save_snapshot: interior FP32 copies
     st_fault_stats stats{};
@@ -116,6 +116,9 @@ int fused_step(st_solver* s, StepArgs a, int snap_out, int snap_in, int epi, con
 // Two adjoint steps with fused imaging in one launch (launch_fd_step2_image):
 // afterwards cur = the field after step t-1 and prev = the field after step t.
 int fused_step2(st_solver* s, StepArgs a, int snap_in, const ImageMaps& imaps);
+// Two forward steps t, t+1 in one launch (launch_fd_step2_forward):
+// afterwards cur = u_{t+2} and prev = u_{t+1}.
+int fused_step2_forward(st_solver* s, StepArgs a, int snap_out);
 int zero_fields(st_solver* s);
 long long dev_index(const st_solver* s, int64_t ix, int64_t iy, int64_t iz);
 bool finite_sample(const double* w, int64_t len, int64_t t, float* out);

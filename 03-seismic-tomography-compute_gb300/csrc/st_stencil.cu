@@ -686,28 +686,40 @@ int launch_variant(const Layout& L, const FieldMaps& mcur, const FieldMaps& mpre
     return ST_OK;
 }
 
-// ---------------------------------------------------------------- two adjoint steps per launch
+// ---------------------------------------------------------------- two time steps per launch
 //
-// fd_step2_image_kernel runs the adjoint steps t and t-1 of the imaging pass in
-// one launch: sub-step A computes lambda' = step(lambda_t, lambda_{t+1}) on the
-// 16 x 64 tile plus a one-cell y/z ring (recomputed by every tile that needs
-// it), sub-step B computes lambda'' = step(lambda', lambda_t) on the tile from
-// the ring held in shared memory, and the imaging condition accumulates both
-// steps' terms into one read-modify-write of the image and illumination. Each
+// fd_step2_kernel<MODE, SK> runs two time steps in one launch: sub-step A
+// computes u' = step(u, u_prev) on the 16 x 64 tile plus a one-cell y/z ring
+// (recomputed by every tile that needs it), sub-step B computes
+// u'' = step(u', u) on the tile from the ring held in shared memory. Each
 // point is updated by the same arithmetic, in the same order, as two launches
-// of fd_step_kernel<SNAP_NONE, SNAP_IN, EPI_IMAGE_T>, so the results are
-// bit-identical; HBM traffic falls from 2 x 34 to 40 bytes per point (read
-// lambda_t, lambda_{t+1}, c, two snapshots, image, illumination; write
-// lambda', lambda'', image, illumination).
+// of fd_step_kernel, so the results are bit-identical.
+//
+// MODE_ADJ (the RTM imaging pass; SK = the snapshot kind read): adjoint steps
+// t and t-1 with the receiver forcing of each, and the imaging terms of both
+// steps accumulated in one read-modify-write of the image and illumination:
+// 40 bytes per point per launch instead of 2 x 34 (read lambda_t,
+// lambda_{t+1}, c, two snapshots, image, illumination; write lambda',
+// lambda'', image, illumination).
+// MODE_FWD (SK = the snapshot kind stored, or SNAP_NONE): forward steps t and
+// t+1 with the receiver sampling and source injection of each. The launch
+// stores the snapshots of its two input fields, u_t and u_{t-1}, whose scales
+// are complete by then; the snapshot of u_{t+1} is left to the next launch,
+// which reads it as its previous field. |u'| and |u''| are max-reduced into
+// the scales of steps t+1 and t+2. 24 bytes per point per launch with 16-bit
+// snapshots instead of 2 x 18.
 //
 // Planes i = 0 .. n+3 of a CTA's chunk [xa, xb) (n = xb - xa) are interior
-// x = xa - 2 + i. Stage i of the TMA ring carries lambda_t of plane i (rows
-// y0-2 .. y0+17), lambda_{t+1} and c of plane i (rows y0-1 .. y0+16) and, one
-// plane behind, the two snapshot, image and illumination tiles of interior
-// x = xa - 3 + i. Iteration i runs sub-step A on plane i-1 and sub-step B
-// (with imaging and the stores) on plane i-2.
-template <int SNAP_IN>
+// x = xa - 2 + i. Stage i of the TMA ring carries the current field of plane
+// i (rows y0-2 .. y0+17), the previous field and c of plane i (rows y0-1 ..
+// y0+16) and, for imaging, one plane behind, the two snapshot, image and
+// illumination tiles of interior x = xa - 3 + i. Iteration i runs sub-step A
+// on plane i-1 and sub-step B (with the stores) on plane i-2.
+enum Step2Mode : int { MODE_ADJ = 0, MODE_FWD = 1 };
+
+template <int MODE, int SK>
 struct Geo2 {
+    static constexpr bool IMG = MODE == MODE_ADJ;
     static constexpr int TYV = 16;
     static constexpr int W = TZ + 8;            // z from z0 - 4
     static constexpr int CUR_H = TYV + 4;       // rows y0 - 2 .. y0 + 17
@@ -715,9 +727,9 @@ struct Geo2 {
     static constexpr int CUR_BYTES = W * CUR_H * 4;
     static constexpr int RING_BYTES = W * RING_H * 4;
     static constexpr int RING_PAD = ((RING_BYTES + 127) / 128) * 128;
-    static constexpr int SNAP_TILE = TZ * TYV * snap_bytes(SNAP_IN);
+    static constexpr int SNAP_TILE = IMG ? TZ * TYV * snap_bytes(SK) : 0;
     static constexpr int SNAP_PAD = ((SNAP_TILE + 127) / 128) * 128;
-    static constexpr int CTR = TZ * TYV * 4;
+    static constexpr int CTR = IMG ? TZ * TYV * 4 : 0;
     static constexpr int OFF_PREV = ((CUR_BYTES + 127) / 128) * 128;
     static constexpr int OFF_C = OFF_PREV + RING_PAD;
     static constexpr int OFF_SA = OFF_C + RING_PAD;
@@ -730,7 +742,10 @@ struct Geo2 {
     static constexpr int STAGES = 3;
     static constexpr int SMEM = STAGES * STAGE_BYTES + 2 * RING_PAD + EXTRA_BYTES;
     static constexpr int FIT = SM_SMEM / (SMEM + 1024);
-    static constexpr int MINB = FIT < 4 ? FIT : 4;
+#ifndef STEP2_FWD_MINB
+#define STEP2_FWD_MINB 2
+#endif
+    static constexpr int MINB = FIT < STEP2_FWD_MINB ? FIT : STEP2_FWD_MINB;
 };
 
 // Receiver row index of y (iry) or column index of x (irx) on the receiver
@@ -751,8 +766,8 @@ __device__ __forceinline__ void st4(float* p, const float v[4]) {
     *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
 }
 
-// Four adjoint point updates in fd_step_kernel's order: the update (the
-// guarded form where the fast one is out of range), the receiver forcing
+// Four point updates in fd_step_kernel's order: the update (the guarded form
+// where the fast one is out of range), the adjoint receiver forcing
 // c * force[q] at point rk (rk < 0: none), then the stable damping.
 __device__ __forceinline__ void adj_update4(const StepArgs& a, const float u0[4], const float pv[4],
                                             const float um[4], const float up[4], const float ym[4],
@@ -790,27 +805,8 @@ __device__ __forceinline__ void adj_update4(const StepArgs& a, const float u0[4]
     }
 }
 
-// Sub-step A on the four z of one row at interior plane x: T is plane x's
-// lambda_t tile, tr the group's offset there (rows from y0 - 2), P / Cc its
-// lambda_{t+1} and c tiles (offset tr - W, rows from y0 - 1); um / up are
-// lambda_t at x - 1 / x + 1; dyz the y/z sponge distances of the four points.
-// Points outside the interior hold 0. Returns c of the four points in cv.
-__device__ __forceinline__ void step2_a_vec(const StepArgs& a, const float* dtab, const float* T, const float* P,
-                                            const float* Cc, int tr, int dx, const int dyz[4], bool far, bool inside,
-                                            const float um[4], const float up[4], int q, int rk, float res[4],
-                                            float cv[4], int* fired) {
-    constexpr int W = TZ + 8;
-    float u0[4], ym[4], yp[4], pv[4], D[4];
-    ld4(Cc + tr - W, cv);
-    if (!inside) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) res[k] = 0.0f;
-        return;
-    }
-    ld4(T + tr, u0);
-    ld4(P + tr - W, pv);
-    ld4(T + tr - W, ym);
-    ld4(T + tr + W, yp);
+__device__ __forceinline__ void sponge4(const StepArgs& a, const float* dtab, int dx, const int dyz[4], bool far,
+                                        float D[4]) {
     if (far && dx >= a.sw) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) D[k] = 1.0f;
@@ -818,21 +814,23 @@ __device__ __forceinline__ void step2_a_vec(const StepArgs& a, const float* dtab
 #pragma unroll
         for (int k = 0; k < 4; ++k) D[k] = sponge_tab(a, dtab, min(dx, dyz[k]));
     }
-    adj_update4(a, u0, pv, um, up, ym, yp, T[tr - 1], T[tr + 4], cv, D, a.force_row, q, rk, res, fired);
 }
 
-template <int SNAP_IN>
-__global__ void __launch_bounds__(NTHREADS, (Geo2<SNAP_IN>::MINB))
-    fd_step2_image_kernel(const __grid_constant__ CUtensorMap map_cur, const __grid_constant__ CUtensorMap map_prev,
-                          const __grid_constant__ CUtensorMap map_c, const __grid_constant__ CUtensorMap map_snap,
-                          const __grid_constant__ CUtensorMap map_img, const __grid_constant__ CUtensorMap map_ill,
-                          const StepArgs a) {
-    using G = Geo2<SNAP_IN>;
+template <int MODE, int SK>
+__global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
+    fd_step2_kernel(const __grid_constant__ CUtensorMap map_cur, const __grid_constant__ CUtensorMap map_prev,
+                    const __grid_constant__ CUtensorMap map_c, const __grid_constant__ CUtensorMap map_snap,
+                    const __grid_constant__ CUtensorMap map_img, const __grid_constant__ CUtensorMap map_ill,
+                    const StepArgs a) {
+    using G = Geo2<MODE, SK>;
+    constexpr bool ADJ = MODE == MODE_ADJ;
+    constexpr bool SNAPS = !ADJ && SK != SNAP_NONE;
     constexpr int W = G::W;
     constexpr int STAGES = G::STAGES;
     extern __shared__ __align__(128) unsigned char smem[];
-    float* lbuf = reinterpret_cast<float*>(smem + STAGES * G::STAGE_BYTES);  // two lambda' planes
+    float* lbuf = reinterpret_cast<float*>(smem + STAGES * G::STAGE_BYTES);  // two ring planes
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + STAGES * G::STAGE_BYTES + 2 * G::RING_PAD);
+    float* red = reinterpret_cast<float*>(smem + STAGES * G::STAGE_BYTES + 2 * G::RING_PAD + 64);
     float* dtab_s = reinterpret_cast<float*>(smem + STAGES * G::STAGE_BYTES + 2 * G::RING_PAD + 128);
 
     const int tid = threadIdx.x;
@@ -872,22 +870,43 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<SNAP_IN>::MINB))
     }
     const bool far_c = min(min(dyz_c[0], dyz_c[1]), min(dyz_c[2], dyz_c[3])) >= a.sw;
     const int dyz_z = min(min(yz, a.ny - 1 - yz), min(zring, a.nz - 1 - zring));
-    // receiver rows of the tasks; rk / rkr: the receiver plane's point in the
-    // centre / ring-row group
-    const bool recs = a.force_row || a.force_row2;
+    // receivers: forcing (adjoint) at every task, sampling (forward) at the
+    // centre only; rk / rkr: the receiver plane's point in the centre /
+    // ring-row group
+    const bool recs = ADJ ? (a.force_row || a.force_row2) : (a.seis_row || a.seis_row2);
     const int rk = (recs && a.rz >= zc && a.rz < zc + 4) ? a.rz - zc : -1;
-    const int rkr = (recs && has_yr && a.rz >= zcr && a.rz < zcr + 4) ? a.rz - zcr : -1;
+    const int rkr = (ADJ && recs && has_yr && a.rz >= zcr && a.rz < zcr + 4) ? a.rz - zcr : -1;
     const int iry_c = rk >= 0 ? rec_line(yc, a.ry0, a.rsy, a.rny) : -1;
     const int iry_r = rkr >= 0 ? rec_line(yring, a.ry0, a.rsy, a.rny) : -1;
-    const int iry_z = recs && has_zr && zring == a.rz ? rec_line(yz, a.ry0, a.rsy, a.rny) : -1;
+    const int iry_z = ADJ && recs && has_zr && zring == a.rz ? rec_line(yz, a.ry0, a.rsy, a.rny) : -1;
     const bool any_rec = iry_c >= 0 || iry_r >= 0 || iry_z >= 0;
+    // forward source injection (a.inj_steps bit 0: sub-step A, bit 1: B) at
+    // point inj_kc / inj_kr of the centre / ring-row group, or the ring point
+    const bool inj = !ADJ && a.inj_x >= 0;
+    const int inj_kc = (inj && a.inj_y == yc && a.inj_z >= zc && a.inj_z < zc + 4) ? a.inj_z - zc : -1;
+    const int inj_kr = (inj && has_yr && a.inj_y == yring && a.inj_z >= zcr && a.inj_z < zcr + 4) ? a.inj_z - zcr
+                                                                                                  : -1;
+    const bool inj_z = inj && has_zr && a.inj_y == yz && a.inj_z == zring;
 
     const bool tab_smem = a.sw <= DTAB_MAX;
     if (tab_smem)
         for (int i = tid; i < a.sw; i += NTHREADS) dtab_s[i] = a.dtab[i];
     const float* dtab = tab_smem ? dtab_s : a.dtab;
-    const float scale_a = __uint_as_float(*a.amax_in) / SNAP_QMAX;
-    const float scale_b = __uint_as_float(*a.amax_in2) / SNAP_QMAX;
+    // imaging: snapshot scales of steps t and t-1; forward: inverse scales of
+    // the two stored snapshots (u_t and u_{t-1})
+    float scale_a = 0.0f, scale_b = 0.0f;
+    if constexpr (ADJ) {
+        scale_a = __uint_as_float(*a.amax_in) / SNAP_QMAX;
+        scale_b = __uint_as_float(*a.amax_in2) / SNAP_QMAX;
+    }
+    if constexpr (SNAPS) {
+        const float m = __uint_as_float(*a.amax_cur);
+        scale_a = m > 0.0f ? SNAP_QMAX / m : 0.0f;
+        if (a.snap_out2) {
+            const float mp = __uint_as_float(*a.amax_cur2);
+            scale_b = mp > 0.0f ? SNAP_QMAX / mp : 0.0f;
+        }
+    }
 
     auto st_cur = [&](int s) { return reinterpret_cast<float*>(smem + s * G::STAGE_BYTES); };
     auto st_prev = [&](int s) { return reinterpret_cast<float*>(smem + s * G::STAGE_BYTES + G::OFF_PREV); };
@@ -908,16 +927,18 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<SNAP_IN>::MINB))
         const int s = i % STAGES;
         const int xd = xa - 1 + i;  // device x of interior plane xa - 2 + i
         const int xi = xa - 3 + i;  // interior plane of the imaging operands
-        const bool img = xi >= xa && xi < xb;
+        const bool img = ADJ && xi >= xa && xi < xb;
         mbar_arrive_expect_tx(&bar[s], G::TX_FIELDS + (img ? G::TX_IMAGE : 0));
         tma_load_3d(st_cur(s), &map_cur, &bar[s], z0, y0 - 1, xd);
         tma_load_3d(st_prev(s), &map_prev, &bar[s], z0, y0, xd);
         tma_load_3d(st_c(s), &map_c, &bar[s], z0, y0, xd);
-        if (img) {
-            tma_load_4d(st_sa(s), &map_snap, &bar[s], z0, y0, xi, a.snap_t);
-            tma_load_4d(st_sb(s), &map_snap, &bar[s], z0, y0, xi, a.snap_t - 1);
-            tma_load_3d(st_img(s), &map_img, &bar[s], z0, y0, xi);
-            tma_load_3d(st_ill(s), &map_ill, &bar[s], z0, y0, xi);
+        if constexpr (ADJ) {
+            if (img) {
+                tma_load_4d(st_sa(s), &map_snap, &bar[s], z0, y0, xi, a.snap_t);
+                tma_load_4d(st_sb(s), &map_snap, &bar[s], z0, y0, xi, a.snap_t - 1);
+                tma_load_3d(st_img(s), &map_img, &bar[s], z0, y0, xi);
+                tma_load_3d(st_ill(s), &map_ill, &bar[s], z0, y0, xi);
+            }
         }
     };
     int issued = 0;
@@ -926,19 +947,20 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<SNAP_IN>::MINB))
         for (int i = 0; i < issued; ++i) issue(i);
     }
 
-    const int tcen = (yr + 2) * W + 4 * tz4 + 4;                 // centre in a lambda_t tile
-    const int tyr = (yring - y0 + 2) * W + (zcr - z0) + 4;       // ring row in a lambda_t tile
-    const int tzr = (yz - y0 + 2) * W + (zring - z0 + 4);        // ring point in a lambda_t tile
+    const int tcen = (yr + 2) * W + 4 * tz4 + 4;                 // centre in a current-field tile
+    const int tyr = (yring - y0 + 2) * W + (zcr - z0) + 4;       // ring row in a current-field tile
+    const int tzr = (yz - y0 + 2) * W + (zring - z0 + 4);        // ring point in a current-field tile
     const int rcen = tcen - W, ryr = tyr - W, rzr = tzr - W;     // the same in ring-geometry tiles
     const int ccen = yr * TZ + 4 * tz4;                          // centre in the compact tiles
-    // lambda_t queues (x-1, x, x+1) of the three tasks, lambda' queue of the
-    // centre (planes i-3, i-2, i-1) and c of the centre at plane i-2
+    // current-field queues (x-1, x, x+1) of the three tasks, the u' queue of
+    // the centre (planes i-3, i-2, i-1) and c of the centre at plane i-2
     float um[4] = {0, 0, 0, 0}, u0[4] = {0, 0, 0, 0};
     float rm[4] = {0, 0, 0, 0}, r0[4] = {0, 0, 0, 0};
     float zm_ = 0.0f, z0_ = 0.0f;
     float lm[4] = {0, 0, 0, 0}, l0[4] = {0, 0, 0, 0};
     float cprev[4] = {0, 0, 0, 0};
     int irx_prev = -1;  // receiver column of plane i-2
+    float amax1 = 0.0f, amax2 = 0.0f;
     int fired = 0;
     int timed_out = 0;
 
@@ -959,22 +981,78 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<SNAP_IN>::MINB))
             const int sp = (i - 1) % STAGES;
             const int x = xa - 3 + i;
             const bool xin = x >= 0 && x < a.nx;
+            const bool own = x >= xa && x < xb;  // this chunk's plane: sampling, snapshots, max
             const int dx = min(x, a.nx - 1 - x);
             if (any_rec && xin) irx = rec_line(x, a.rx0, a.rsx, a.rnx);
-            const int irx_a = a.force_row ? irx : -1;  // step t's forcing
+            const int irx_a = (ADJ ? a.force_row : a.seis_row) ? irx : -1;  // step t's receivers
+            const bool inj_a = inj && (a.inj_steps & 1) && x == a.inj_x;
             const float* T = st_cur(sp);
             const float* P = st_prev(sp);
             const float* Cc = st_c(sp);
             float* Lw = lb(i - 1);
-            const bool rc = irx_a >= 0 && iry_c >= 0;
-            step2_a_vec(a, dtab, T, P, Cc, tcen, dx, dyz_c, far_c, xin && cin, um, up, rc ? irx_a * a.rny + iry_c : 0,
-                        rc ? rk : -1, lp, cnow, &fired);
+            // centre
+            ld4(Cc + rcen, cnow);
+            if (xin && cin) {
+                float c0[4], pv[4], ym[4], yp[4], D[4];
+                ld4(T + tcen, c0);
+                ld4(P + rcen, pv);
+                ld4(T + tcen - W, ym);
+                ld4(T + tcen + W, yp);
+                sponge4(a, dtab, dx, dyz_c, far_c, D);
+                const bool rc = irx_a >= 0 && iry_c >= 0;
+                const int q = rc ? irx_a * a.rny + iry_c : 0;
+                adj_update4(a, c0, pv, um, up, ym, yp, T[tcen - 1], T[tcen + 4], cnow, D, a.force_row, q,
+                            ADJ && rc ? rk : -1, lp, &fired);
+                if constexpr (!ADJ) {
+                    if (own && rc) {
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if (k == rk) a.seis_row[q] = lp[k];
+                    }
+                    if (inj_a) {
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if (k == inj_kc) lp[k] += a.inj_val;
+                    }
+                    if constexpr (SNAPS) {
+                        if (own) {
+                            const long long cb = ((long long)x * a.ny + yc) * a.nz + zc;
+                            float qv[4];
+#pragma unroll
+                            for (int k = 0; k < 4; ++k) {
+                                qv[k] = c0[k] * scale_a;
+                                amax1 = fmaxf(amax1, fabsf(lp[k]));
+                            }
+                            snap_store4<SK>(a.snap_out, cb, qv);
+                            if (a.snap_out2) {
+#pragma unroll
+                                for (int k = 0; k < 4; ++k) qv[k] = pv[k] * scale_b;
+                                snap_store4<SK>(a.snap_out2, cb, qv);
+                            }
+                        }
+                    }
+                }
+            }
             st4(Lw + rcen, lp);
             if (has_yr) {
-                float res[4], cv_[4];
-                const bool rr = irx_a >= 0 && iry_r >= 0;
-                step2_a_vec(a, dtab, T, P, Cc, tyr, dx, dyz_r, false, xin && yrin, rm, rp, rr ? irx_a * a.rny + iry_r : 0,
-                            rr ? rkr : -1, res, cv_, &fired);
+                float res[4] = {0, 0, 0, 0};
+                if (xin && yrin) {
+                    float c0[4], pv[4], ym[4], yp[4], cv[4], D[4];
+                    ld4(T + tyr, c0);
+                    ld4(P + ryr, pv);
+                    ld4(Cc + ryr, cv);
+                    ld4(T + tyr - W, ym);
+                    ld4(T + tyr + W, yp);
+                    sponge4(a, dtab, dx, dyz_r, false, D);
+                    const bool rr = ADJ && irx_a >= 0 && iry_r >= 0;
+                    adj_update4(a, c0, pv, rm, rp, ym, yp, T[tyr - 1], T[tyr + 4], cv, D, a.force_row,
+                                rr ? irx_a * a.rny + iry_r : 0, rr ? rkr : -1, res, &fired);
+                    if (!ADJ && inj_a) {
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if (k == inj_kr) res[k] += a.inj_val;
+                    }
+                }
                 st4(Lw + ryr, res);
             }
             if (has_zr) {
@@ -987,14 +1065,15 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<SNAP_IN>::MINB))
                     res = update_fast(u, upd, zm_, zp_, ym, yp, zm, zp, c, a.ax, a.ay, a.az);
                     if (!(fabsf(res) <= a.amp))
                         res = update_guarded(u, upd, zm_, zp_, ym, yp, zm, zp, c, a.ax, a.ay, a.az, a.amp, &fired);
-                    if (irx_a >= 0 && iry_z >= 0) res = fmaf(c, a.force_row[irx_a * a.rny + iry_z], res);
+                    if (ADJ && irx_a >= 0 && iry_z >= 0) res = fmaf(c, a.force_row[irx_a * a.rny + iry_z], res);
                     if (a.stable_sponge) res *= D;
+                    if (!ADJ && inj_a && inj_z) res += a.inj_val;
                 }
                 Lw[rzr] = res;
             }
         }
         if (i >= 4 && cin) {
-            // sub-step B, imaging and stores on plane i-2 (interior x = xa - 4 + i),
+            // sub-step B and the stores on plane i-2 (interior x = xa - 4 + i),
             // from the ring buffer of plane i-2 (complete since the last barrier)
             const int x = xa - 4 + i;
             const float* Lr = lb(i - 2);
@@ -1002,46 +1081,60 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<SNAP_IN>::MINB))
             float ym[4], yp[4], D[4], res[4];
             ld4(Lr + rcen - W, ym);
             ld4(Lr + rcen + W, yp);
-            if (far_c && dx >= a.sw) {
+            sponge4(a, dtab, dx, dyz_c, far_c, D);
+            const float* rows2 = ADJ ? a.force_row2 : a.seis_row2;
+            const bool rc = rows2 && irx_prev >= 0 && iry_c >= 0;
+            const int q = rc ? irx_prev * a.rny + iry_c : 0;
+            adj_update4(a, l0, um, lm, lp, ym, yp, Lr[rcen - 1], Lr[rcen + 4], cprev, D, a.force_row2, q,
+                        ADJ && rc ? rk : -1, res, &fired);
+            if constexpr (!ADJ) {
+                if (rc) {
 #pragma unroll
-                for (int k = 0; k < 4; ++k) D[k] = 1.0f;
-            } else {
+                    for (int k = 0; k < 4; ++k)
+                        if (k == rk) a.seis_row2[q] = res[k];
+                }
+                if (inj && (a.inj_steps & 2) && x == a.inj_x) {
 #pragma unroll
-                for (int k = 0; k < 4; ++k) D[k] = sponge_tab(a, dtab, min(dx, dyz_c[k]));
+                    for (int k = 0; k < 4; ++k)
+                        if (k == inj_kc) res[k] += a.inj_val2;
+                }
+                if constexpr (SNAPS) {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) amax2 = fmaxf(amax2, fabsf(res[k]));
+                }
             }
-            const bool rc = a.force_row2 && irx_prev >= 0 && iry_c >= 0;
-            adj_update4(a, l0, um, lm, lp, ym, yp, Lr[rcen - 1], Lr[rcen + 4], cprev, D, a.force_row2,
-                        rc ? irx_prev * a.rny + iry_c : 0, rc ? rk : -1, res, &fired);
             const long long ob = (long long)(x + 1) * a.plane + (long long)(yc + 1) * a.NZP + zc + Layout::ZOFF;
             st4(a.out + ob, l0);
             st4(a.out2 + ob, res);
-            // imaging: step t pairs lambda_t with the snapshot of t, step t-1
-            // pairs lambda' with the snapshot of t-1, in that order
-            const int sp = (i - 1) % STAGES;
-            float fa[4], fb[4], im[4], il[4];
-            snap_smem4<SNAP_IN>(st_sa(sp), ccen, fa);
-            snap_smem4<SNAP_IN>(st_sb(sp), ccen, fb);
-            ld4(st_img(sp) + ccen, im);
-            ld4(st_ill(sp) + ccen, il);
+            if constexpr (ADJ) {
+                // imaging: step t pairs lambda_t with the snapshot of t, step t-1
+                // pairs lambda' with the snapshot of t-1, in that order
+                const int sp = (i - 1) % STAGES;
+                float fa[4], fb[4], im[4], il[4];
+                snap_smem4<SK>(st_sa(sp), ccen, fa);
+                snap_smem4<SK>(st_sb(sp), ccen, fb);
+                ld4(st_img(sp) + ccen, im);
+                ld4(st_ill(sp) + ccen, il);
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float w = a.stable_sponge ? cprev[k] * D[k] : cprev[k];
-                float f = fa[k] * scale_a;
-                float ad = __fdividef(um[k], w);
-                if (!isfinite(f)) f = 0.0f;
-                if (!isfinite(ad)) ad = 0.0f;
-                im[k] = fmaf(f, ad, im[k]);
-                il[k] = fmaf(f, f, il[k]);
-                f = fb[k] * scale_b;
-                ad = __fdividef(l0[k], w);
-                if (!isfinite(f)) f = 0.0f;
-                if (!isfinite(ad)) ad = 0.0f;
-                im[k] = fmaf(f, ad, im[k]);
-                il[k] = fmaf(f, f, il[k]);
+                for (int k = 0; k < 4; ++k) {
+                    const float w = a.stable_sponge ? cprev[k] * D[k] : cprev[k];
+                    float f = fa[k] * scale_a;
+                    float ad = __fdividef(um[k], w);
+                    if (!isfinite(f)) f = 0.0f;
+                    if (!isfinite(ad)) ad = 0.0f;
+                    im[k] = fmaf(f, ad, im[k]);
+                    il[k] = fmaf(f, f, il[k]);
+                    f = fb[k] * scale_b;
+                    ad = __fdividef(l0[k], w);
+                    if (!isfinite(f)) f = 0.0f;
+                    if (!isfinite(ad)) ad = 0.0f;
+                    im[k] = fmaf(f, ad, im[k]);
+                    il[k] = fmaf(f, f, il[k]);
+                }
+                const long long cb = ((long long)x * a.ny + yc) * a.nz + zc;
+                st4(a.image + cb, im);
+                st4(a.illum + cb, il);
             }
-            const long long cb = ((long long)x * a.ny + yc) * a.nz + zc;
-            st4(a.image + cb, im);
-            st4(a.illum + cb, il);
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -1072,18 +1165,38 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<SNAP_IN>::MINB))
         return;
     }
     if (fired) atomicOr(a.flags, FLAG_GUARD);
+    if constexpr (SNAPS) {
+        for (int o = 16; o > 0; o >>= 1) {
+            amax1 = fmaxf(amax1, __shfl_xor_sync(FULL, amax1, o));
+            amax2 = fmaxf(amax2, __shfl_xor_sync(FULL, amax2, o));
+        }
+        if (lane == 0) {
+            red[warp] = amax1;
+            red[NTHREADS / 32 + warp] = amax2;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            float m1 = red[0], m2 = red[NTHREADS / 32];
+            for (int w = 1; w < NTHREADS / 32; ++w) {
+                m1 = fmaxf(m1, red[w]);
+                m2 = fmaxf(m2, red[NTHREADS / 32 + w]);
+            }
+            atomicMax(a.amax_next, __float_as_uint(m1));
+            atomicMax(a.amax_next2, __float_as_uint(m2));
+        }
+    }
 }
 
-template <int SI>
+template <int MODE, int SK>
 int launch_step2_variant(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
-                         const ImageMaps& im, StepArgs a, cudaStream_t st) {
-    using G = Geo2<SI>;
+                         const ImageMaps* im, StepArgs a, cudaStream_t st) {
+    using G = Geo2<MODE, SK>;
     static bool configured = false;
     static std::mutex mu;
     {
         std::lock_guard<std::mutex> lk(mu);
         if (!configured) {
-            ST_CUDA(cudaFuncSetAttribute(fd_step2_image_kernel<SI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            ST_CUDA(cudaFuncSetAttribute(fd_step2_kernel<MODE, SK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          G::SMEM));
             configured = true;
         }
@@ -1092,8 +1205,11 @@ int launch_step2_variant(const Layout& L, const FieldMaps& mcur, const FieldMaps
     a.x_chunk = (int)((L.nx + chunks - 1) / chunks);
     const int nch = (int)((L.nx + a.x_chunk - 1) / a.x_chunk);
     dim3 grid((unsigned)((L.nz + TZ - 1) / TZ), (unsigned)((L.ny + G::TYV - 1) / G::TYV), (unsigned)nch);
-    fd_step2_image_kernel<SI><<<grid, NTHREADS, G::SMEM, st>>>(mcur.cur2, mprev.cur[0], mc.cur[0], im.snap, im.image,
-                                                              im.illum, a);
+    // the imaging maps are read only by the adjoint mode
+    const CUtensorMap& ms = im ? im->snap : mc.cur[0];
+    const CUtensorMap& mi = im ? im->image : mc.cur[0];
+    const CUtensorMap& ml = im ? im->illum : mc.cur[0];
+    fd_step2_kernel<MODE, SK><<<grid, NTHREADS, G::SMEM, st>>>(mcur.cur2, mprev.cur[0], mc.cur[0], ms, mi, ml, a);
     ::stg::count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
@@ -1239,6 +1355,24 @@ __global__ void sumsq_finite_kernel(const float* __restrict__ f, long long n, do
 }
 
 // Interior copy with non-finite values replaced by 0 (save_snapshot, wave_equation.cpp:463-480).
+// Snapshot of one field, as fd_step_kernel stores the snapshot of its centre
+// field: v * (16384 / |max|) rounded to the store's kind, compact interior.
+template <int K>
+__global__ void snapshot_of_field_kernel(const float* __restrict__ f, Layout L, void* snap,
+                                         const unsigned* amax) {
+    const float m = __uint_as_float(*amax);
+    const float inv = m > 0.0f ? SNAP_QMAX / m : 0.0f;
+    const long long total = L.nx * L.ny * L.nz;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long ix = e / (L.ny * L.nz);
+        const long long r = e - ix * (L.ny * L.nz);
+        const long long iy = r / L.nz;
+        const long long iz = r - iy * L.nz;
+        snap_store<K>(snap, e, f[L.at(ix, iy, iz)] * inv);
+    }
+}
+
 __global__ void interior_copy_kernel(const float* __restrict__ f, Layout L, float* __restrict__ out) {
     const long long total = L.nx * L.ny * L.nz;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
@@ -1388,10 +1522,34 @@ int launch_fd_step2_image(const Layout& L, const FieldMaps& mcur, const FieldMap
     ST_CHECK(!a.zlim && !a.seis_row && !a.snap_out && a.inj_x < 0, ST_ERR_UNSUPPORTED,
              "two-step imaging: adjoint steps only");
     switch (snap_in) {
-        case SNAP_BF16: return launch_step2_variant<SNAP_BF16>(L, mcur, mprev, mc, imaps, a, st);
-        case SNAP_FP16: return launch_step2_variant<SNAP_FP16>(L, mcur, mprev, mc, imaps, a, st);
-        case SNAP_FP32: return launch_step2_variant<SNAP_FP32>(L, mcur, mprev, mc, imaps, a, st);
+        case SNAP_BF16: return launch_step2_variant<MODE_ADJ, SNAP_BF16>(L, mcur, mprev, mc, &imaps, a, st);
+        case SNAP_FP16: return launch_step2_variant<MODE_ADJ, SNAP_FP16>(L, mcur, mprev, mc, &imaps, a, st);
+        case SNAP_FP32: return launch_step2_variant<MODE_ADJ, SNAP_FP32>(L, mcur, mprev, mc, &imaps, a, st);
         default: ST_CHECK(false, ST_ERR_ARG, "imaging step needs a snapshot kind");
+    }
+}
+
+int launch_fd_step2_forward(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
+                            StepArgs a, int snap_out, cudaStream_t st) {
+    a.nx = (int)L.nx;
+    a.ny = (int)L.ny;
+    a.nz = (int)L.nz;
+    a.NZP = (int)L.NZP;
+    a.plane = L.plane;
+    if (a.timeout_ns == 0) a.timeout_ns = 2000000000ull;
+    ST_CHECK(a.out && a.out2, ST_ERR_ARG, "two-step forward: missing outputs");
+    ST_CHECK(!a.zlim && !a.force_row && !a.force_row2 && !a.image && !a.grad, ST_ERR_UNSUPPORTED,
+             "two-step forward: forward steps without terrain only");
+    ST_CHECK(L.nz % 4 == 0, ST_ERR_UNSUPPORTED, "two-step forward needs nz %% 4 == 0");
+    ST_CHECK(snap_out == SNAP_NONE || (a.snap_out && a.amax_cur && a.amax_next && a.amax_next2 &&
+                                       (!a.snap_out2 || a.amax_cur2)),
+             ST_ERR_ARG, "two-step forward: missing snapshot operands");
+    switch (snap_out) {
+        case SNAP_NONE: return launch_step2_variant<MODE_FWD, SNAP_NONE>(L, mcur, mprev, mc, nullptr, a, st);
+        case SNAP_BF16: return launch_step2_variant<MODE_FWD, SNAP_BF16>(L, mcur, mprev, mc, nullptr, a, st);
+        case SNAP_FP16: return launch_step2_variant<MODE_FWD, SNAP_FP16>(L, mcur, mprev, mc, nullptr, a, st);
+        case SNAP_FP32: return launch_step2_variant<MODE_FWD, SNAP_FP32>(L, mcur, mprev, mc, nullptr, a, st);
+        default: ST_CHECK(false, ST_ERR_ARG, "bad snapshot kind %d", snap_out);
     }
 }
 
@@ -1498,6 +1656,20 @@ int launch_count_nonfinite(const float* f, long long n, unsigned long long* out,
 int launch_sumsq_finite(const float* f, long long n, double* out, cudaStream_t st) {
     ST_CUDA(cudaMemsetAsync(out, 0, sizeof(double), st));
     sumsq_finite_kernel<<<grid_for(n), 256, 0, st>>>(f, n, out);
+    ::stg::count_launch();
+    ST_CUDA(cudaGetLastError());
+    return ST_OK;
+}
+
+int launch_snapshot_of_field(const float* f, const Layout& L, void* snap, int kind, const unsigned* amax,
+                             cudaStream_t st) {
+    const int g = grid_for(L.nx * L.ny * L.nz);
+    switch (kind) {
+        case SNAP_BF16: snapshot_of_field_kernel<SNAP_BF16><<<g, 256, 0, st>>>(f, L, snap, amax); break;
+        case SNAP_FP16: snapshot_of_field_kernel<SNAP_FP16><<<g, 256, 0, st>>>(f, L, snap, amax); break;
+        case SNAP_FP32: snapshot_of_field_kernel<SNAP_FP32><<<g, 256, 0, st>>>(f, L, snap, amax); break;
+        default: ST_CHECK(false, ST_ERR_ARG, "bad snapshot kind %d", kind);
+    }
     ::stg::count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;

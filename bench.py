@@ -35,11 +35,20 @@ for _p in (PKG, os.path.join(REPO, "oracle")):
 
 import numpy as np  # noqa: E402
 
-ALG_BYTES_FWD = 18   # read u, prev, c + write out (16) + BF16 snapshot store (2)
-ALG_BYTES_BWD = 34   # 16 + BF16 snapshot read (2) + image and illumination read-modify-write (16)
-# two adjoint steps per launch: read lambda_t, lambda_{t+1}, c (12) + two BF16 snapshots (4) + image and
-# illumination read-modify-write (16) + write both steps' fields (8), per point per launch
-ALG_BYTES_BWD2 = 40
+SNAP_BYTES = {"bf16": 2, "fp16": 2, "fp32": 4}
+
+
+def alg_bytes(snap, paired):
+    """Algorithmic HBM bytes per interior point per launch of the forward and
+    the adjoint+imaging kernels. One step per launch: read u, prev, c + write
+    out (16) + the snapshot store (forward) or read (adjoint) + image and
+    illumination read-modify-write (16, adjoint). Two steps per launch: read
+    u, prev, c (12) + write both steps' fields (8) + two snapshots + the image
+    and illumination read-modify-write once (16, adjoint)."""
+    es = SNAP_BYTES[snap]
+    if paired:
+        return 20 + 2 * es, 36 + 2 * es
+    return 16 + es, 32 + es
 METRIC = "stencil Gpts/s"
 
 
@@ -52,8 +61,8 @@ def parse():
     ap.add_argument("--nt", type=int, default=2000, help="time steps per shot (2000 = the workload)")
     ap.add_argument("--n", type=int, default=256, help="grid edge (256 = the workload)")
     ap.add_argument("--snap", choices=["bf16", "fp16", "fp32"], default="bf16")
-    ap.add_argument("--adjoint-steps", type=int, choices=[1, 2], default=2,
-                    help="adjoint time steps per launch of the imaging pass (results are identical)")
+    ap.add_argument("--fused-steps", type=int, choices=[1, 2], default=2,
+                    help="time steps per launch of the forward and imaging passes (results are identical)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU sample time")
@@ -445,7 +454,7 @@ def run_gpu(args):
     cfg = se.SolverConfig(dt=w.dt, nt=w.nt, sponge_width=w.sponge_width, sponge_damping=w.sponge_damping,
                           sponge_mode=w.sponge_mode)
     s = se.WaveEquationSolver(grid, cfg, device=torch.cuda.current_device())
-    s.set_step_fusion(args.adjoint_steps)
+    s.set_step_fusion(args.fused_steps)
     vel_true = se.workloads.to_reference_layout(w.vel)
     vel_mig = se.workloads.to_reference_layout(w.vel_migration)
     # observed data (input preparation, untimed)
@@ -492,19 +501,23 @@ def run_gpu(args):
     pts_step = 2.0 * w.nt * npts
     value = world * pts_step * args.steps / (el_ms / 1e3) / 1e9
     hbm_peak, peak_kind = measured_peaks()
-    # the imaging pass runs nt / 2 two-step launches (an odd nt adds one single step)
-    paired = args.adjoint_steps == 2 and w.nt % 2 == 0 and w.nz % 8 == 0
+    # both passes run nt / 2 two-step launches (an odd nt adds one single step)
+    paired = args.fused_steps == 2 and w.nt % 2 == 0 and w.nz % 8 == 0
+    fwd_bytes, bwd_bytes = alg_bytes(args.snap, paired)
+    snap = args.snap.upper()
     if paired:
-        bwd_kernel = "fd_step2_image_kernel<BF16> (two adjoint steps + imaging)"
-        bwd_bytes, bwd_launches, traffic_key = ALG_BYTES_BWD2, w.nt // 2, "fd_step2_image_bf16_256"
+        bwd_kernel = f"fd_step2_kernel<adjoint, {snap}> (two adjoint steps + imaging)"
+        fwd_kernel = f"fd_step2_kernel<forward, {snap}> (two forward steps + snapshot stores)"
+        launches_per_pass, traffic_key = w.nt // 2, "fd_step2_image_bf16_256"
     else:
-        bwd_kernel = "fd_step_kernel<SNAP_NONE, BF16, imaging> (adjoint step + imaging)"
-        bwd_bytes, bwd_launches, traffic_key = ALG_BYTES_BWD, w.nt, "fd_step_adjoint_image_bf16_256"
-    bwd_launch_ms = statistics.mean(bwd_ms) / bwd_launches
-    fwd_launch_ms = statistics.mean(fwd_ms) / w.nt
+        bwd_kernel = f"fd_step_kernel<SNAP_NONE, {snap}, imaging> (adjoint step + imaging)"
+        fwd_kernel = f"fd_step_kernel<{snap}, NONE> (forward step + snapshot store)"
+        launches_per_pass, traffic_key = w.nt, "fd_step_adjoint_image_bf16_256"
+    bwd_launch_ms = statistics.mean(bwd_ms) / launches_per_pass
+    fwd_launch_ms = statistics.mean(fwd_ms) / launches_per_pass
     bw_bwd = bwd_bytes * npts / (bwd_launch_ms / 1e3) / 1e9
-    bw_fwd = ALG_BYTES_FWD * npts / (fwd_launch_ms / 1e3) / 1e9
-    alg_total = (ALG_BYTES_FWD * w.nt + bwd_bytes * bwd_launches) * npts * args.steps
+    bw_fwd = fwd_bytes * npts / (fwd_launch_ms / 1e3) / 1e9
+    alg_total = (fwd_bytes + bwd_bytes) * launches_per_pass * npts * args.steps
     traffic = profile_traffic(traffic_key) if args.snap == "bf16" and w.nx == 256 else None
     line = {
         "metric": METRIC, "value": value, "unit": "Gpts/s", "n_gpus": world, "steps": args.steps,
@@ -518,9 +531,10 @@ def run_gpu(args):
                      "peak_kind": f"{peak_kind} copy bandwidth", "traffic": traffic,
                      "alg_bytes_per_launch": bwd_bytes * npts, "launch_ms": bwd_launch_ms,
                      "steps_per_launch": 2 if paired else 1},
-        "roofline_forward": {"bound": "hbm", "kernel": "fd_step_kernel<BF16, NONE> (forward step + snapshot store)",
+        "roofline_forward": {"bound": "hbm", "kernel": fwd_kernel,
                              "achieved": bw_fwd, "peak": hbm_peak, "unit": "GB/s", "frac": bw_fwd / hbm_peak,
-                             "alg_bytes_per_launch": ALG_BYTES_FWD * npts, "launch_ms": fwd_launch_ms},
+                             "alg_bytes_per_launch": fwd_bytes * npts, "launch_ms": fwd_launch_ms,
+                             "steps_per_launch": 2 if paired else 1},
         "phases_ms_per_step": {"forward": statistics.mean(fwd_ms), "backward": statistics.mean(bwd_ms)},
         "gpu_launches": launches,
         "clocks": clk.summary(),

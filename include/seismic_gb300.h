@@ -173,11 +173,13 @@ int st_solver_fault_stats(st_solver* s, st_fault_stats* out);
  * torch views): which = ST_FIELD_*. Valid until the next call that steps the
  * solver (the imaging pass exchanges field buffers). */
 int st_solver_device_field(st_solver* s, int which, float** out);
-/* Adjoint time steps per launch of the RTM imaging pass (st_rtm_shot and its
- * host variant): 2 (default) runs steps t and t-1 in one launch with the
- * imaging of both fused, 1 one step per launch; the image, illumination and
- * fields are bit-identical either way. The imaging pass of
- * RTMEngine::process_shot (rtm/rtm_engine.cpp:59-110), restructured. */
+/* Time steps per launch of the shot-level passes (st_shot_forward, st_rtm_shot
+ * and its host variant, the forward pass of the FWI gradient): 2 (default)
+ * runs two steps in one launch (in the imaging pass with the imaging of both
+ * fused), 1 one step per launch; seismograms, snapshots, images and fields are
+ * bit-identical either way. The time loops of WaveEquationSolver::
+ * forward_propagate (solver/wave_equation.cpp:100-152) and
+ * WaveEquationSolver::run_rtm (solver/wave_equation.cpp:621-688), restructured. */
 int st_solver_set_step_fusion(st_solver* s, int steps);
 /* The CUDA stream the handle orders its work on (a cudaStream_t). */
 int st_solver_stream(st_solver* s, void** out);

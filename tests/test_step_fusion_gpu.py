@@ -1,11 +1,12 @@
-"""The RTM imaging pass with two adjoint steps per launch against one step
-per launch, through the C ABI: image, illumination and the final adjoint
-fields must be bit-identical (each point is updated by the same arithmetic in
-the same order), for odd and even step counts, both sponge rules, every
-snapshot kind, receivers whose forcing lands on the recomputed ring of a
-tile, grids that end inside a tile, and different x-chunkings of the grid.
-The two-step path is also the default one the oracle parity tests of
-test_rtm_gpu.py run."""
+"""Two time steps per launch against one step per launch, through the C ABI.
+RTM imaging pass: image, illumination and the final adjoint fields; forward
+pass: seismograms, snapshot bytes, snapshot scales and the final fields. All
+must be bit-identical (each point is updated by the same arithmetic in the
+same order), for odd and even step counts, both sponge rules, every snapshot
+kind, receivers and sources on the recomputed ring of a tile, grids that end
+inside a tile, and different x-chunkings of the grid. The two-step path is
+also the default one the oracle parity tests of test_rtm_gpu.py and
+test_forward_gpu.py run."""
 import os
 
 import numpy as np
@@ -99,3 +100,63 @@ def test_step_fusion_argument_checked(se):
             s.set_step_fusion(3)
     finally:
         s.close()
+
+
+def run_forward(se, n, nt, sponge, src, rec_z, kind, steps, seed=5):
+    """One forward shot; returns seismograms, snapshot bytes, the scale array
+    and the two final fields."""
+    import torch
+    nx, ny, nz = n
+    rng = np.random.default_rng(seed)
+    vel = 1500.0 + 1500.0 * rng.random((nx, ny, nz))
+    d = 10.0
+    dt = se.workloads.cfl_dt(d, 3000.0)
+    s = se.WaveEquationSolver(se.GridParams(nx, ny, nz, d, d, d),
+                              se.SolverConfig(dt=dt, nt=nt, sponge_width=6, sponge_damping=0.015))
+    try:
+        s.set_sponge_mode(sponge)
+        s.set_velocity_field(se.workloads.to_reference_layout(vel))
+        s.set_step_fusion(steps)
+        rec = se.workloads.ReceiverGrid(0, 3, (nx + 2) // 3, 0, 1, ny, rec_z)
+        seis = torch.zeros((nt, rec.count), device="cuda")
+        wav = se.workloads.ricker(30.0, dt, nt)
+        es = {0: 0, 1: 2, 2: 2, 3: 4}[kind]
+        snaps = torch.zeros(max(nt * nx * ny * nz * es, 1), dtype=torch.uint8, device="cuda")
+        amax = torch.zeros(nt + 1, dtype=torch.int32, device="cuda")
+        if kind:
+            assert se.shot_forward(s, src, wav, nt, rec, seis=seis, snap_kind=kind, snaps=snaps, snap_amax=amax) == 0
+        else:
+            assert se.shot_forward(s, src, wav, nt, rec, seis=seis) == 0
+        torch.cuda.synchronize()
+        return (seis.cpu().numpy(), snaps.cpu().numpy(), amax.cpu().numpy(), s.get_field(0), s.get_field(1))
+    finally:
+        s.close()
+
+
+FWD_CASES = [
+    # (nx, ny, nz), nt, sponge rule, source, receiver plane z, snapshot kind
+    ((28, 24, 32), 41, "reference", (14, 16, 5), 5, 1),    # source on row y0 of tile 1: the ring row of tile 0
+    ((40, 20, 72), 40, "stable", (20, 15, 64), 63, 1),     # source on z0 of tile 1 / ring point of tile 0
+    ((70, 33, 64), 23, "stable", (35, 31, 63), 60, 2),     # source on the last z of tile 0
+    ((9, 17, 40), 12, "stable", (4, 16, 39), 39, 3),       # source in the one-row tile, on the last z
+    ((30, 20, 36), 17, "stable", (15, 10, 18), 18, 0),     # no snapshots; nz % 8 != 0
+]
+
+
+@pytest.mark.parametrize("n,nt,sponge,src,rec_z,kind", FWD_CASES)
+def test_two_forward_steps_per_launch_bit_identical(se, n, nt, sponge, src, rec_z, kind):
+    one = run_forward(se, n, nt, sponge, src, rec_z, kind, steps=1)
+    two = run_forward(se, n, nt, sponge, src, rec_z, kind, steps=2)
+    assert np.abs(one[0]).max() > 0
+    for a, b, what in zip(one, two, ("seismograms", "snapshots", "snapshot scales", "current field",
+                                     "previous field")):
+        assert np.array_equal(a, b), f"{what} differ"
+
+
+@pytest.mark.parametrize("chunks", ["1", "4"])
+def test_two_forward_steps_any_chunking(se, monkeypatch, chunks):
+    base = run_forward(se, (40, 20, 72), 19, "stable", (20, 15, 64), 63, 1, steps=1)
+    monkeypatch.setenv("SEISMIC_GB300_XCHUNKS", chunks)
+    two = run_forward(se, (40, 20, 72), 19, "stable", (20, 15, 64), 63, 1, steps=2)
+    for a, b in zip(base, two):
+        assert np.array_equal(a, b)
