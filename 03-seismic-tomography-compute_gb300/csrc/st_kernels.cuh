@@ -100,7 +100,7 @@ int make_compact_map(CUtensorMap* map, const float* base, const Layout& L, int b
 int launch_fd_step(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
                    StepArgs a, int snap_out, int snap_in, int epi, const CUtensorMap* msnap, cudaStream_t st,
                    const ImageMaps* imaps = nullptr);
-// Launch two adjoint steps with fused imaging (fd_step2_image_kernel): reads
+// Launch two adjoint steps with fused imaging (fd_step2_kernel, adjoint mode): reads
 // cur = lambda_t and prev = lambda_{t+1}, writes a.out = lambda_{t-1}' (the
 // output of step t) and a.out2 = the output of step t-1, from snapshots
 // a.snap_t and a.snap_t - 1 (scales a.amax_in, a.amax_in2) and the receiver
