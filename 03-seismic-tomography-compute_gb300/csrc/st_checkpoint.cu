@@ -224,7 +224,33 @@ int backward(CkptRun& c, int j) {
         c.started = true;
     }
     const int t0 = c.seg_begin(j), t1 = c.seg_end(j);
+    // imaging: pairs of steps inside the segment share one launch (the
+    // solver's own fields and spare; the checkpoint sets are not involved)
+    const bool pairs = c.epi == 1 && c.staged && s->fused_steps == 2;
     for (int t = t1 - 1; t >= t0; --t) {
+        if (pairs && t - 1 >= t0) {
+            StepArgs a = base_args(s, nullptr);
+            if (nrec > 0) {
+                a.rz = (int)R.z;
+                a.rx0 = (int)R.x0;
+                a.rsx = (int)R.sx;
+                a.rnx = (int)R.nx;
+                a.ry0 = (int)R.y0;
+                a.rsy = (int)R.sy;
+                a.rny = (int)R.ny;
+                a.force_row = c.force + (size_t)(t - 1) * nrec;
+                if (t >= 2) a.force_row2 = c.force + (size_t)(t - 2) * nrec;
+            }
+            a.snap_t = t - t0;
+            a.amax_in = c.amax_seg + (t - t0);
+            a.amax_in2 = c.amax_seg + (t - 1 - t0);
+            a.image = c.image;
+            a.illum = c.illum;
+            ST_TRY(fused_step2(s, a, c.kind, c.imaps));
+            c.stats.adjoint_steps += 2;
+            --t;
+            continue;
+        }
         StepArgs a = base_args(s, nullptr);
         if (nrec > 0 && t >= 1) {
             a.rz = (int)R.z;
