@@ -83,6 +83,8 @@ struct CkptRun {
     float* illum = nullptr;
     float* grad_c = nullptr;
     CUtensorMap msnap;
+    CUtensorMap mgrad;     // compact map of grad_c (gradient step pairs)
+    bool grad_pairs = false;
     ImageMaps imaps;
     bool staged = false;
     std::function<int()> before_backward;
@@ -224,9 +226,10 @@ int backward(CkptRun& c, int j) {
         c.started = true;
     }
     const int t0 = c.seg_begin(j), t1 = c.seg_end(j);
-    // imaging: pairs of steps inside the segment share one launch (the
-    // solver's own fields and spare; the checkpoint sets are not involved)
-    const bool pairs = c.epi == 1 && c.staged && s->fused_steps == 2;
+    // imaging and gradient: pairs of steps inside the segment share one
+    // launch (the solver's own fields and spare; the checkpoint sets are not
+    // involved)
+    const bool pairs = (c.epi == 1 && c.staged && s->fused_steps == 2) || (c.epi == 2 && c.grad_pairs);
     for (int t = t1 - 1; t >= t0; --t) {
         if (pairs && t - 1 >= t0) {
             StepArgs a = base_args(s, nullptr);
@@ -244,9 +247,14 @@ int backward(CkptRun& c, int j) {
             a.snap_t = t - t0;
             a.amax_in = c.amax_seg + (t - t0);
             a.amax_in2 = c.amax_seg + (t - 1 - t0);
-            a.image = c.image;
-            a.illum = c.illum;
-            ST_TRY(fused_step2(s, a, c.kind, c.imaps));
+            if (c.epi == 1) {
+                a.image = c.image;
+                a.illum = c.illum;
+                ST_TRY(fused_step2(s, a, c.kind, c.imaps));
+            } else {
+                a.grad = c.grad_c;
+                ST_TRY(fused_step2_grad(s, a, c.kind, c.msnap, c.mgrad));
+            }
             c.stats.adjoint_steps += 2;
             --t;
             continue;
@@ -358,6 +366,8 @@ int checkpointed_adjoint(st_solver* s, const st_shot* shot, int snap_kind, int s
     c.amax_seg = reinterpret_cast<unsigned*>(c.segbuf + sbytes);
     for (int k = 0; k < 3; ++k) ST_TRY(build_field_maps(&c.gm[k], c.g[k], L));
     if (epi == 2) ST_TRY(build_snap_map_grad(&c.msnap, c.segbuf, snap_kind, L, c.seg));
+    c.grad_pairs = epi == 2 && s->fused_steps == 2 && L.nz % 4 == 0;
+    if (c.grad_pairs) ST_TRY(make_compact_map(&c.mgrad, c.grad_c, L, FD_TZ, 16));
     c.staged = epi == 1 && image_maps_supported(snap_kind, L);
     if (c.staged) ST_TRY(build_image_maps(&c.imaps, c.segbuf, snap_kind, c.seg, image, illum, L));
     c.slot_of.assign((size_t)c.nseg, -1);

@@ -115,8 +115,11 @@ int gradient_backward_impl(st_solver* s, const st_shot* shot, const float* adj, 
     const int64_t nrec = R.nx * R.ny;
     const int nt = shot->nt;
     const size_t npts = (size_t)(L.nx * L.ny * L.nz);
-    CUtensorMap msnap;
+    CUtensorMap msnap, mgrad;
     ST_TRY(build_snap_map_grad(&msnap, snaps, snap_kind, L, std::max(nt, 1)));
+    // pairs of steps share one launch (the gradient of both accumulated once)
+    const bool pairs = s->fused_steps == 2 && L.nz % 4 == 0;
+    if (pairs) ST_TRY(make_compact_map(&mgrad, grad_c, L, FD_TZ, 16));
     ST_TRY(zero_fields(s));
     ST_CUDA(cudaMemsetAsync(grad_c, 0, npts * sizeof(float), s->stream));
     if (nt <= 0) return ST_OK;
@@ -124,6 +127,21 @@ int gradient_backward_impl(st_solver* s, const st_shot* shot, const float* adj, 
         ST_TRY(launch_rec_force(s, R, adj + (size_t)(nt - 1) * nrec));
     }
     for (int t = nt - 1; t >= 0; --t) {
+        if (pairs && t >= 1) {
+            StepArgs a = base_args(s, nullptr);
+            if (nrec > 0) {
+                set_receivers_args(a, R);
+                a.force_row = adj + (size_t)(t - 1) * nrec;
+                if (t >= 2) a.force_row2 = adj + (size_t)(t - 2) * nrec;
+            }
+            a.snap_t = t;
+            a.amax_in = amax + t;
+            a.amax_in2 = amax + t - 1;
+            a.grad = grad_c;
+            ST_TRY(fused_step2_grad(s, a, snap_kind, msnap, mgrad));
+            --t;
+            continue;
+        }
         StepArgs a = base_args(s, nullptr);
         if (nrec > 0 && t >= 1) {
             set_receivers_args(a, R);

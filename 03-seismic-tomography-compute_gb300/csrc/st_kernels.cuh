@@ -108,6 +108,13 @@ int launch_fd_step(const Layout& L, const FieldMaps& mcur, const FieldMaps& mpre
 // staged image maps (nz % 4 == 0).
 int launch_fd_step2_image(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
                           StepArgs a, int snap_in, const ImageMaps& imaps, cudaStream_t st);
+// Launch two adjoint steps with the gradient epilogue (fd_step2_kernel,
+// gradient mode): as launch_fd_step2_image, but a.grad (compact interior)
+// accumulates (lambda / c) * L(snapshot) for both steps; msnap is the store's
+// halo map (build_snap_map_grad), mgrad a compact map of a.grad (box {64, 16}).
+int launch_fd_step2_grad(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
+                         StepArgs a, int snap_in, const CUtensorMap& msnap, const CUtensorMap& mgrad,
+                         cudaStream_t st);
 // Launch two forward steps t, t+1 (fd_step2_kernel, forward mode): reads
 // cur = u_t, prev = u_{t-1}; writes a.out = u_{t+1}, a.out2 = u_{t+2};
 // samples a.seis_row / a.seis_row2; injects per a.inj_steps; with snapshots

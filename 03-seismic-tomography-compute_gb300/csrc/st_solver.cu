@@ -299,6 +299,16 @@ int fused_step2(st_solver* s, StepArgs a, int snap_in, const ImageMaps& imaps) {
     return ST_OK;
 }
 
+int fused_step2_grad(st_solver* s, StepArgs a, int snap_in, const CUtensorMap& msnap, const CUtensorMap& mgrad) {
+    ST_TRY(ensure_spare(s));
+    a.out = s->f[s->in];
+    a.out2 = s->f4;
+    ST_TRY(launch_fd_step2_grad(s->L, s->maps[s->ic], s->maps[s->ip], s->map_c, a, snap_in, msnap, mgrad,
+                                s->stream));
+    rotate_after_pair(s);
+    return ST_OK;
+}
+
 int fused_step2_forward(st_solver* s, StepArgs a, int snap_out) {
     ST_TRY(ensure_spare(s));
     a.out = s->f[s->in];

@@ -119,6 +119,8 @@ int fused_step2(st_solver* s, StepArgs a, int snap_in, const ImageMaps& imaps);
 // Two forward steps t, t+1 in one launch (launch_fd_step2_forward):
 // afterwards cur = u_{t+2} and prev = u_{t+1}.
 int fused_step2_forward(st_solver* s, StepArgs a, int snap_out);
+// Two adjoint steps with the gradient epilogue in one launch (launch_fd_step2_grad).
+int fused_step2_grad(st_solver* s, StepArgs a, int snap_in, const CUtensorMap& msnap, const CUtensorMap& mgrad);
 int zero_fields(st_solver* s);
 long long dev_index(const st_solver* s, int64_t ix, int64_t iy, int64_t iz);
 bool finite_sample(const double* w, int64_t len, int64_t t, float* out);

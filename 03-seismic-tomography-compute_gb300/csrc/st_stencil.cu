@@ -715,11 +715,16 @@ int launch_variant(const Layout& L, const FieldMaps& mcur, const FieldMaps& mpre
 // y0+16) and, for imaging, one plane behind, the two snapshot, image and
 // illumination tiles of interior x = xa - 3 + i. Iteration i runs sub-step A
 // on plane i-1 and sub-step B (with the stores) on plane i-2.
-enum Step2Mode : int { MODE_ADJ = 0, MODE_FWD = 1 };
+enum Step2Mode : int { MODE_ADJ = 0, MODE_FWD = 1, MODE_GRAD = 2 };
 
 template <int MODE, int SK>
 struct Geo2 {
     static constexpr bool IMG = MODE == MODE_ADJ;
+    static constexpr bool GRD = MODE == MODE_GRAD;
+    // gradient: snapshot tiles with a one-cell y/z halo (box from z0 - GSOFF,
+    // rows y0-1 .. y0+16), as the one-step gradient kernel stages them
+    static constexpr int GSW = snap_bytes(SK) == 2 ? TZ + 16 : TZ + 8;
+    static constexpr int GSOFF = snap_bytes(SK) == 2 ? 8 : 4;
     static constexpr int TYV = 16;
     static constexpr int W = TZ + 8;            // z from z0 - 4
     static constexpr int CUR_H = TYV + 4;       // rows y0 - 2 .. y0 + 17
@@ -727,18 +732,19 @@ struct Geo2 {
     static constexpr int CUR_BYTES = W * CUR_H * 4;
     static constexpr int RING_BYTES = W * RING_H * 4;
     static constexpr int RING_PAD = ((RING_BYTES + 127) / 128) * 128;
-    static constexpr int SNAP_TILE = IMG ? TZ * TYV * snap_bytes(SK) : 0;
+    static constexpr int SNAP_TILE = IMG ? TZ * TYV * snap_bytes(SK) : (GRD ? GSW * RING_H * snap_bytes(SK) : 0);
     static constexpr int SNAP_PAD = ((SNAP_TILE + 127) / 128) * 128;
-    static constexpr int CTR = IMG ? TZ * TYV * 4 : 0;
+    static constexpr int CTR = (IMG || GRD) ? TZ * TYV * 4 : 0;
     static constexpr int OFF_PREV = ((CUR_BYTES + 127) / 128) * 128;
     static constexpr int OFF_C = OFF_PREV + RING_PAD;
     static constexpr int OFF_SA = OFF_C + RING_PAD;
     static constexpr int OFF_SB = OFF_SA + SNAP_PAD;
     static constexpr int OFF_IMG = OFF_SB + SNAP_PAD;
     static constexpr int OFF_ILL = OFF_IMG + CTR;
-    static constexpr int STAGE_BYTES = OFF_ILL + CTR;
+    static constexpr int STAGE_BYTES = OFF_ILL + (IMG ? CTR : 0);
     static constexpr int TX_FIELDS = CUR_BYTES + 2 * RING_BYTES;
-    static constexpr int TX_IMAGE = 2 * SNAP_TILE + 2 * CTR;
+    static constexpr int TX_SNAPS = 2 * SNAP_TILE;         // the two snapshot tiles
+    static constexpr int TX_ACC = (IMG ? 2 : 1) * CTR;     // image + illumination, or gradient
     static constexpr int STAGES = 3;
     static constexpr int SMEM = STAGES * STAGE_BYTES + 2 * RING_PAD + EXTRA_BYTES;
     static constexpr int FIT = SM_SMEM / (SMEM + 1024);
@@ -816,6 +822,27 @@ __device__ __forceinline__ void sponge4(const StepArgs& a, const float* dtab, in
     }
 }
 
+// Laplacian of a snapshot at the four z of a centre group, scaled, with the
+// one-step gradient kernel's expression: S / Sn are the halo tiles (width SW)
+// of planes x / x+1 and srow the group's offset there, sm the group's values
+// at plane x-1.
+template <int K, int SW>
+__device__ __forceinline__ void snap_lap4(const unsigned char* S, const unsigned char* Sn, int srow,
+                                          const float sm[4], const StepArgs& a, float scale, float out[4]) {
+    float s0[4], spn[4], sym[4], syp[4];
+    snap_smem4<K>(S, srow, s0);
+    snap_smem4<K>(Sn, srow, spn);
+    snap_smem4<K>(S, srow - SW, sym);
+    snap_smem4<K>(S, srow + SW, syp);
+    const float zm0 = snap_smem1<K>(S, srow - 1), zp3 = snap_smem1<K>(S, srow + 4);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float zm_ = k == 0 ? zm0 : s0[k - 1], zp_ = k == 3 ? zp3 : s0[k + 1];
+        out[k] = scale * (fmaf(-2.0f, s0[k], spn[k] + sm[k]) * a.ax + fmaf(-2.0f, s0[k], syp[k] + sym[k]) * a.ay +
+                          fmaf(-2.0f, s0[k], zp_ + zm_) * a.az);
+    }
+}
+
 template <int MODE, int SK>
 __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     fd_step2_kernel(const __grid_constant__ CUtensorMap map_cur, const __grid_constant__ CUtensorMap map_prev,
@@ -823,8 +850,11 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                     const __grid_constant__ CUtensorMap map_img, const __grid_constant__ CUtensorMap map_ill,
                     const StepArgs a) {
     using G = Geo2<MODE, SK>;
-    constexpr bool ADJ = MODE == MODE_ADJ;
-    constexpr bool SNAPS = !ADJ && SK != SNAP_NONE;
+    constexpr bool ADJ = MODE == MODE_ADJ;     // adjoint steps with imaging
+    constexpr bool GRD = MODE == MODE_GRAD;    // adjoint steps with the gradient
+    constexpr bool FWD = MODE == MODE_FWD;
+    constexpr bool BACK = !FWD;                // receiver forcing, snapshots read
+    constexpr bool SNAPS = FWD && SK != SNAP_NONE;
     constexpr int W = G::W;
     constexpr int STAGES = G::STAGES;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -873,16 +903,16 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     // receivers: forcing (adjoint) at every task, sampling (forward) at the
     // centre only; rk / rkr: the receiver plane's point in the centre /
     // ring-row group
-    const bool recs = ADJ ? (a.force_row || a.force_row2) : (a.seis_row || a.seis_row2);
+    const bool recs = BACK ? (a.force_row || a.force_row2) : (a.seis_row || a.seis_row2);
     const int rk = (recs && a.rz >= zc && a.rz < zc + 4) ? a.rz - zc : -1;
-    const int rkr = (ADJ && recs && has_yr && a.rz >= zcr && a.rz < zcr + 4) ? a.rz - zcr : -1;
+    const int rkr = (BACK && recs && has_yr && a.rz >= zcr && a.rz < zcr + 4) ? a.rz - zcr : -1;
     const int iry_c = rk >= 0 ? rec_line(yc, a.ry0, a.rsy, a.rny) : -1;
     const int iry_r = rkr >= 0 ? rec_line(yring, a.ry0, a.rsy, a.rny) : -1;
-    const int iry_z = ADJ && recs && has_zr && zring == a.rz ? rec_line(yz, a.ry0, a.rsy, a.rny) : -1;
+    const int iry_z = BACK && recs && has_zr && zring == a.rz ? rec_line(yz, a.ry0, a.rsy, a.rny) : -1;
     const bool any_rec = iry_c >= 0 || iry_r >= 0 || iry_z >= 0;
     // forward source injection (a.inj_steps bit 0: sub-step A, bit 1: B) at
     // point inj_kc / inj_kr of the centre / ring-row group, or the ring point
-    const bool inj = !ADJ && a.inj_x >= 0;
+    const bool inj = FWD && a.inj_x >= 0;
     const int inj_kc = (inj && a.inj_y == yc && a.inj_z >= zc && a.inj_z < zc + 4) ? a.inj_z - zc : -1;
     const int inj_kr = (inj && has_yr && a.inj_y == yring && a.inj_z >= zcr && a.inj_z < zcr + 4) ? a.inj_z - zcr
                                                                                                   : -1;
@@ -895,7 +925,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     // imaging: snapshot scales of steps t and t-1; forward: inverse scales of
     // the two stored snapshots (u_t and u_{t-1})
     float scale_a = 0.0f, scale_b = 0.0f;
-    if constexpr (ADJ) {
+    if constexpr (BACK) {
         scale_a = __uint_as_float(*a.amax_in) / SNAP_QMAX;
         scale_b = __uint_as_float(*a.amax_in2) / SNAP_QMAX;
     }
@@ -926,19 +956,30 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     auto issue = [&](int i) {
         const int s = i % STAGES;
         const int xd = xa - 1 + i;  // device x of interior plane xa - 2 + i
-        const int xi = xa - 3 + i;  // interior plane of the imaging operands
-        const bool img = ADJ && xi >= xa && xi < xb;
-        mbar_arrive_expect_tx(&bar[s], G::TX_FIELDS + (img ? G::TX_IMAGE : 0));
+        const int xi = xa - 3 + i;  // interior plane of the imaging / gradient operands
+        const bool acc = (ADJ || GRD) && xi >= xa && xi < xb;
+        // the gradient's snapshot Laplacian also reads the planes either side
+        const bool snp = ADJ ? acc : (GRD && xi >= xa - 1 && xi <= xb);
+        mbar_arrive_expect_tx(&bar[s], G::TX_FIELDS + (snp ? G::TX_SNAPS : 0) + (acc ? G::TX_ACC : 0));
         tma_load_3d(st_cur(s), &map_cur, &bar[s], z0, y0 - 1, xd);
         tma_load_3d(st_prev(s), &map_prev, &bar[s], z0, y0, xd);
         tma_load_3d(st_c(s), &map_c, &bar[s], z0, y0, xd);
         if constexpr (ADJ) {
-            if (img) {
+            if (acc) {
                 tma_load_4d(st_sa(s), &map_snap, &bar[s], z0, y0, xi, a.snap_t);
                 tma_load_4d(st_sb(s), &map_snap, &bar[s], z0, y0, xi, a.snap_t - 1);
                 tma_load_3d(st_img(s), &map_img, &bar[s], z0, y0, xi);
                 tma_load_3d(st_ill(s), &map_ill, &bar[s], z0, y0, xi);
             }
+        }
+        if constexpr (GRD) {
+            // x = z0 - GSOFF is 16 bytes left of the tile (negative at z0 = 0:
+            // a load, zero-filled there, as the rows beyond the grid)
+            if (snp) {
+                tma_load_4d(st_sa(s), &map_snap, &bar[s], z0 - G::GSOFF, y0 - 1, xi, a.snap_t);
+                tma_load_4d(st_sb(s), &map_snap, &bar[s], z0 - G::GSOFF, y0 - 1, xi, a.snap_t - 1);
+            }
+            if (acc) tma_load_3d(st_img(s), &map_img, &bar[s], z0, y0, xi);
         }
     };
     int issued = 0;
@@ -952,6 +993,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     const int tzr = (yz - y0 + 2) * W + (zring - z0 + 4);        // ring point in a current-field tile
     const int rcen = tcen - W, ryr = tyr - W, rzr = tzr - W;     // the same in ring-geometry tiles
     const int ccen = yr * TZ + 4 * tz4;                          // centre in the compact tiles
+    const int gsrow = (yr + 1) * G::GSW + 4 * tz4 + G::GSOFF;    // centre in the gradient's snapshot tiles
     // current-field queues (x-1, x, x+1) of the three tasks, the u' queue of
     // the centre (planes i-3, i-2, i-1) and c of the centre at plane i-2
     float um[4] = {0, 0, 0, 0}, u0[4] = {0, 0, 0, 0};
@@ -959,6 +1001,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     float zm_ = 0.0f, z0_ = 0.0f;
     float lm[4] = {0, 0, 0, 0}, l0[4] = {0, 0, 0, 0};
     float cprev[4] = {0, 0, 0, 0};
+    float sm_a[4] = {0, 0, 0, 0}, sm_b[4] = {0, 0, 0, 0};  // gradient: snapshot centres at plane i-3
     int irx_prev = -1;  // receiver column of plane i-2
     float amax1 = 0.0f, amax2 = 0.0f;
     int fired = 0;
@@ -984,7 +1027,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
             const bool own = x >= xa && x < xb;  // this chunk's plane: sampling, snapshots, max
             const int dx = min(x, a.nx - 1 - x);
             if (any_rec && xin) irx = rec_line(x, a.rx0, a.rsx, a.rnx);
-            const int irx_a = (ADJ ? a.force_row : a.seis_row) ? irx : -1;  // step t's receivers
+            const int irx_a = (BACK ? a.force_row : a.seis_row) ? irx : -1;  // step t's receivers
             const bool inj_a = inj && (a.inj_steps & 1) && x == a.inj_x;
             const float* T = st_cur(sp);
             const float* P = st_prev(sp);
@@ -1002,8 +1045,8 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                 const bool rc = irx_a >= 0 && iry_c >= 0;
                 const int q = rc ? irx_a * a.rny + iry_c : 0;
                 adj_update4(a, c0, pv, um, up, ym, yp, T[tcen - 1], T[tcen + 4], cnow, D, a.force_row, q,
-                            ADJ && rc ? rk : -1, lp, &fired);
-                if constexpr (!ADJ) {
+                            BACK && rc ? rk : -1, lp, &fired);
+                if constexpr (FWD) {
                     if (own && rc) {
 #pragma unroll
                         for (int k = 0; k < 4; ++k)
@@ -1044,10 +1087,10 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                     ld4(T + tyr - W, ym);
                     ld4(T + tyr + W, yp);
                     sponge4(a, dtab, dx, dyz_r, false, D);
-                    const bool rr = ADJ && irx_a >= 0 && iry_r >= 0;
+                    const bool rr = BACK && irx_a >= 0 && iry_r >= 0;
                     adj_update4(a, c0, pv, rm, rp, ym, yp, T[tyr - 1], T[tyr + 4], cv, D, a.force_row,
                                 rr ? irx_a * a.rny + iry_r : 0, rr ? rkr : -1, res, &fired);
-                    if (!ADJ && inj_a) {
+                    if (FWD && inj_a) {
 #pragma unroll
                         for (int k = 0; k < 4; ++k)
                             if (k == inj_kr) res[k] += a.inj_val;
@@ -1065,9 +1108,9 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                     res = update_fast(u, upd, zm_, zp_, ym, yp, zm, zp, c, a.ax, a.ay, a.az);
                     if (!(fabsf(res) <= a.amp))
                         res = update_guarded(u, upd, zm_, zp_, ym, yp, zm, zp, c, a.ax, a.ay, a.az, a.amp, &fired);
-                    if (ADJ && irx_a >= 0 && iry_z >= 0) res = fmaf(c, a.force_row[irx_a * a.rny + iry_z], res);
+                    if (BACK && irx_a >= 0 && iry_z >= 0) res = fmaf(c, a.force_row[irx_a * a.rny + iry_z], res);
                     if (a.stable_sponge) res *= D;
-                    if (!ADJ && inj_a && inj_z) res += a.inj_val;
+                    if (FWD && inj_a && inj_z) res += a.inj_val;
                 }
                 Lw[rzr] = res;
             }
@@ -1082,12 +1125,12 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
             ld4(Lr + rcen - W, ym);
             ld4(Lr + rcen + W, yp);
             sponge4(a, dtab, dx, dyz_c, far_c, D);
-            const float* rows2 = ADJ ? a.force_row2 : a.seis_row2;
+            const float* rows2 = BACK ? a.force_row2 : a.seis_row2;
             const bool rc = rows2 && irx_prev >= 0 && iry_c >= 0;
             const int q = rc ? irx_prev * a.rny + iry_c : 0;
             adj_update4(a, l0, um, lm, lp, ym, yp, Lr[rcen - 1], Lr[rcen + 4], cprev, D, a.force_row2, q,
-                        ADJ && rc ? rk : -1, res, &fired);
-            if constexpr (!ADJ) {
+                        BACK && rc ? rk : -1, res, &fired);
+            if constexpr (FWD) {
                 if (rc) {
 #pragma unroll
                     for (int k = 0; k < 4; ++k)
@@ -1134,6 +1177,29 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                 const long long cb = ((long long)x * a.ny + yc) * a.nz + zc;
                 st4(a.image + cb, im);
                 st4(a.illum + cb, il);
+            }
+            if constexpr (GRD) {
+                // gradient: step t pairs lambda_t with L(snapshot of t), step t-1
+                // pairs lambda' with L(snapshot of t-1), in that order
+                const int sp = (i - 1) % STAGES;
+                float fa[4], fb[4], g[4];
+                snap_lap4<SK, G::GSW>(st_sa(sp), st_sa(s), gsrow, sm_a, a, scale_a, fa);
+                snap_lap4<SK, G::GSW>(st_sb(sp), st_sb(s), gsrow, sm_b, a, scale_b, fb);
+                ld4(st_img(sp) + ccen, g);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    g[k] = fmaf(um[k] / cprev[k], fa[k], g[k]);
+                    g[k] = fmaf(l0[k] / cprev[k], fb[k], g[k]);
+                }
+                st4(a.grad + ((long long)x * a.ny + yc) * a.nz + zc, g);
+            }
+        }
+        if constexpr (GRD) {
+            // the snapshot centres of plane i-2 are the next plane's x-1 values
+            if (i >= 3) {
+                const int sp = (i - 1) % STAGES;
+                snap_smem4<SK>(st_sa(sp), gsrow, sm_a);
+                snap_smem4<SK>(st_sb(sp), gsrow, sm_b);
             }
         }
 #pragma unroll
@@ -1526,6 +1592,32 @@ int launch_fd_step2_image(const Layout& L, const FieldMaps& mcur, const FieldMap
         case SNAP_FP16: return launch_step2_variant<MODE_ADJ, SNAP_FP16>(L, mcur, mprev, mc, &imaps, a, st);
         case SNAP_FP32: return launch_step2_variant<MODE_ADJ, SNAP_FP32>(L, mcur, mprev, mc, &imaps, a, st);
         default: ST_CHECK(false, ST_ERR_ARG, "imaging step needs a snapshot kind");
+    }
+}
+
+int launch_fd_step2_grad(const Layout& L, const FieldMaps& mcur, const FieldMaps& mprev, const FieldMaps& mc,
+                         StepArgs a, int snap_in, const CUtensorMap& msnap, const CUtensorMap& mgrad,
+                         cudaStream_t st) {
+    a.nx = (int)L.nx;
+    a.ny = (int)L.ny;
+    a.nz = (int)L.nz;
+    a.NZP = (int)L.NZP;
+    a.plane = L.plane;
+    if (a.timeout_ns == 0) a.timeout_ns = 2000000000ull;
+    ST_CHECK(L.nz % 4 == 0, ST_ERR_UNSUPPORTED, "two-step gradient needs nz %% 4 == 0");
+    ST_CHECK(a.out && a.out2 && a.grad && a.amax_in && a.amax_in2 && a.snap_t >= 1, ST_ERR_ARG,
+             "two-step gradient: missing operands");
+    ST_CHECK(!a.zlim && !a.seis_row && !a.snap_out && a.inj_x < 0 && !a.image, ST_ERR_UNSUPPORTED,
+             "two-step gradient: adjoint steps only");
+    ImageMaps m;
+    m.snap = msnap;
+    m.image = mgrad;
+    m.illum = mgrad;
+    switch (snap_in) {
+        case SNAP_BF16: return launch_step2_variant<MODE_GRAD, SNAP_BF16>(L, mcur, mprev, mc, &m, a, st);
+        case SNAP_FP16: return launch_step2_variant<MODE_GRAD, SNAP_FP16>(L, mcur, mprev, mc, &m, a, st);
+        case SNAP_FP32: return launch_step2_variant<MODE_GRAD, SNAP_FP32>(L, mcur, mprev, mc, &m, a, st);
+        default: ST_CHECK(false, ST_ERR_ARG, "gradient step needs a snapshot kind");
     }
 }
 

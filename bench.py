@@ -707,6 +707,7 @@ def run_large(args):
     cfg = se.SolverConfig(dt=w.dt, nt=nt, sponge_width=w.sponge_width, sponge_damping=w.sponge_damping,
                           sponge_mode=w.sponge_mode)
     s = se.WaveEquationSolver(se.GridParams(n, n, n, w.d, w.d, w.d), cfg)
+    s.set_step_fusion(args.fused_steps)
     v_true = torch.from_numpy(w.vel.astype(np.float32)).cuda()
     v0 = torch.from_numpy(se.workloads.smooth(w.vel, 6.0).astype(np.float32)).cuda()
     fwi.set_velocity_device(s, v_true)

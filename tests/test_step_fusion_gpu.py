@@ -5,8 +5,9 @@ must be bit-identical (each point is updated by the same arithmetic in the
 same order), for odd and even step counts, both sponge rules, every snapshot
 kind, receivers and sources on the recomputed ring of a tile, grids that end
 inside a tile, and different x-chunkings of the grid. The two-step path is
-also the default one the oracle parity tests of test_rtm_gpu.py and
-test_forward_gpu.py run."""
+also the default one the oracle parity tests of test_rtm_gpu.py,
+test_forward_gpu.py and test_fwi_gpu.py run. Velocity gradients (FWI
+gradient epilogue) are compared the same way, stored and checkpointed."""
 import os
 
 import numpy as np
@@ -25,6 +26,7 @@ def se():
     spec.loader.exec_module(mod)
     mod.build()
     import seismic_engine
+    import seismic_engine.fwi  # noqa: F401
     return seismic_engine
 
 
@@ -160,3 +162,55 @@ def test_two_forward_steps_any_chunking(se, monkeypatch, chunks):
     two = run_forward(se, (40, 20, 72), 19, "stable", (20, 15, 64), 63, 1, steps=2)
     for a, b in zip(base, two):
         assert np.array_equal(a, b)
+
+
+def run_gradient(se, n, nt, sponge, src, rec_z, kind, steps, checkpoint=None, seed=9):
+    """Velocity gradient of one shot for a seeded adjoint source; returns the
+    gradient and the two final fields."""
+    import torch
+    nx, ny, nz = n
+    rng = np.random.default_rng(seed)
+    vel = 1500.0 + 1500.0 * rng.random((nx, ny, nz))
+    d = 10.0
+    dt = se.workloads.cfl_dt(d, 3000.0)
+    s = se.WaveEquationSolver(se.GridParams(nx, ny, nz, d, d, d),
+                              se.SolverConfig(dt=dt, nt=nt, sponge_width=6, sponge_damping=0.015))
+    try:
+        s.set_sponge_mode(sponge)
+        s.set_velocity_field(se.workloads.to_reference_layout(vel))
+        s.set_step_fusion(steps)
+        rec = se.workloads.ReceiverGrid(1, 2, (nx - 2) // 2, 0, 1, ny, rec_z)
+        adj = torch.from_numpy((rng.standard_normal((nt, rec.count)) * 1e-3).astype(np.float32)).cuda()
+        wav = se.workloads.ricker(30.0, dt, nt)
+        gv = torch.zeros(nx * ny * nz, device="cuda")
+        r = se.fwi.shot_gradient(s, src, wav, nt, rec, adj, gv, kind, checkpoint=checkpoint)
+        assert (r == 0) if checkpoint is None else isinstance(r, dict)
+        torch.cuda.synchronize()
+        return (gv.cpu().numpy(), s.get_field(0), s.get_field(1))
+    finally:
+        s.close()
+
+
+GRAD_CASES = [
+    # (nx, ny, nz), nt, sponge rule, source, receiver plane z, snapshot kind
+    ((28, 24, 32), 41, "reference", (14, 16, 5), 8, 1),
+    ((40, 20, 72), 40, "stable", (20, 15, 64), 61, 3),     # second z tile; receivers by the tile seam
+    ((9, 17, 40), 13, "stable", (4, 16, 36), 39, 2),
+]
+
+
+@pytest.mark.parametrize("n,nt,sponge,src,rec_z,kind", GRAD_CASES)
+def test_two_gradient_steps_per_launch_bit_identical(se, n, nt, sponge, src, rec_z, kind):
+    one = run_gradient(se, n, nt, sponge, src, rec_z, kind, steps=1)
+    two = run_gradient(se, n, nt, sponge, src, rec_z, kind, steps=2)
+    assert np.abs(one[0]).max() > 0
+    for a, b, what in zip(one, two, ("gradient", "current field", "previous field")):
+        assert np.array_equal(a, b), f"{what} differ"
+
+
+def test_two_gradient_steps_checkpointed(se):
+    """Pairs inside checkpoint segments of odd and even length against one step per launch."""
+    base = run_gradient(se, (28, 24, 32), 41, "stable", (14, 16, 5), 8, 1, steps=1)
+    for seg, slots in [(10, 2), (7, 3)]:
+        two = run_gradient(se, (28, 24, 32), 41, "stable", (14, 16, 5), 8, 1, steps=2, checkpoint=(seg, slots))
+        assert np.array_equal(base[0], two[0]), (seg, slots)
