@@ -421,6 +421,11 @@ def run_sampled_rays(args):
                             vp_max=8500.0)
     t_obs = rays.forward_model(vp * 1.02).cpu().numpy()
     obs = SimpleNamespace(picks=[])
+    # one untimed iteration first: the first use of each torch operation in a process loads its kernels
+    warm_model = SimpleNamespace(**{**vars(model), "vp": model.vp.copy()})  # the driver updates model.vp
+    warm = AdjointStateInversion(warm_model, obs, None, max_iterations=1, step_length=10.0, smoothing_sigma=2.0,
+                                 misfit_type="l2", rays=rays, observed=t_obs, weights=ps.weight)
+    warm.run()
     inv = AdjointStateInversion(model, obs, None, max_iterations=3, step_length=10.0, smoothing_sigma=2.0,
                                 misfit_type="l2", rays=rays, observed=t_obs, weights=ps.weight)
     torch.cuda.synchronize()
