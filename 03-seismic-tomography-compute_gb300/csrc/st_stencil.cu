@@ -708,13 +708,20 @@ int launch_variant(const Layout& L, const FieldMaps& mcur, const FieldMaps& mpre
 // which reads it as its previous field. |u'| and |u''| are max-reduced into
 // the scales of steps t+1 and t+2. 24 bytes per point per launch with 16-bit
 // snapshots instead of 2 x 18.
+// MODE_GRAD (the FWI gradient pass; SK = the snapshot kind read): adjoint
+// steps t and t-1 with the receiver forcing of each, and grad += (lambda / c)
+// * L(snapshot) of both steps in one read-modify-write: 32 bytes per point
+// per launch with 16-bit snapshots instead of 2 x 26.
 //
 // Planes i = 0 .. n+3 of a CTA's chunk [xa, xb) (n = xb - xa) are interior
 // x = xa - 2 + i. Stage i of the TMA ring carries the current field of plane
 // i (rows y0-2 .. y0+17), the previous field and c of plane i (rows y0-1 ..
-// y0+16) and, for imaging, one plane behind, the two snapshot, image and
-// illumination tiles of interior x = xa - 3 + i. Iteration i runs sub-step A
-// on plane i-1 and sub-step B (with the stores) on plane i-2.
+// y0+16) and, one plane behind, the operands of the adjoint modes at interior
+// x = xa - 3 + i: for imaging the two snapshot tiles and the image and
+// illumination tiles, for the gradient the two snapshot tiles with a one-cell
+// y/z halo (also for the planes either side of the chunk) and the gradient
+// tile. Iteration i runs sub-step A on plane i-1 and sub-step B (with the
+// stores) on plane i-2.
 enum Step2Mode : int { MODE_ADJ = 0, MODE_FWD = 1, MODE_GRAD = 2 };
 
 template <int MODE, int SK>
