@@ -214,3 +214,18 @@ def test_two_gradient_steps_checkpointed(se):
     for seg, slots in [(10, 2), (7, 3)]:
         two = run_gradient(se, (28, 24, 32), 41, "stable", (14, 16, 5), 8, 1, steps=2, checkpoint=(seg, slots))
         assert np.array_equal(base[0], two[0]), (seg, slots)
+
+
+@pytest.mark.parametrize("n,nt", [((4, 5, 8), 9), ((5, 17, 16), 6), ((6, 3, 72), 5)])
+def test_two_steps_per_launch_small_grids(se, n, nt):
+    """Grids thinner than a tile along every axis, with few steps."""
+    nx, ny, nz = n
+    rz = nz - 2
+    src = (nx // 2, ny // 2, rz - 1)
+    for run, args in ((run_rtm, (n, nt, "stable", rz, 1)),
+                      (run_forward, (n, nt, "stable", src, rz, 1)),
+                      (run_gradient, (n, nt, "stable", src, rz, 1))):
+        one = run(se, *args, steps=1)
+        two = run(se, *args, steps=2)
+        for a, b in zip(one, two):
+            assert np.array_equal(a, b), run.__name__
