@@ -69,6 +69,8 @@ struct CkptRun {
     float* g[3] = {nullptr, nullptr, nullptr};
     FieldMaps gm[3];
     int gc = 0, gp = 1, gn = 2;
+    float* g4 = nullptr;  // the set's spare field for two-step launches (swapped with the handle's spare)
+    FieldMaps gm4;
     int work_at = -1;  // segment whose start state the working set holds
     float* slots = nullptr;
     std::vector<int> slot_of;  // segment -> slot, -1 when none
@@ -108,6 +110,8 @@ void swap_sets(CkptRun& c) {
     std::swap(s->ic, c.gc);
     std::swap(s->ip, c.gp);
     std::swap(s->in, c.gn);
+    std::swap(s->f4, c.g4);
+    std::swap(s->map4, c.gm4);
 }
 
 struct ForwardSet {
@@ -160,7 +164,56 @@ int forward_steps(CkptRun& c, int t0, int t1, bool store) {
     const int64_t nrec = R.nx * R.ny;
     const size_t per = c.per();
     ForwardSet fs(c);
+    // pairs of steps inside [t0, t1) share one launch; a pair leaves the
+    // snapshot of its first output pending, stored by the next pair from its
+    // previous field, or here before a single step and at the end
+    const bool pairs = s->fused_steps == 2 && s->L.nz % 4 == 0;
+    bool pending = false;
+    auto store_pending = [&](int t) -> int {
+        if (!pending) return ST_OK;
+        pending = false;
+        return launch_snapshot_of_field(s->f[s->ip], s->L, c.segbuf + (size_t)(t - 1 - t0) * per, c.kind,
+                                        c.amax_seg + (t - 1 - t0), s->stream);
+    };
     for (int t = t0; t < t1; ++t) {
+        if (pairs && t + 1 < t1) {
+            StepArgs a = base_args(s, nullptr);
+            float w1 = 0.0f, w2 = 0.0f;
+            const bool i1 = finite_sample(shot->wavelet, shot->wavelet_len, t + 1, &w1);
+            const bool i2 = t + 2 < shot->nt && finite_sample(shot->wavelet, shot->wavelet_len, t + 2, &w2);
+            if (i1 || i2) {
+                set_injection(a, shot->src_ix, shot->src_iy, shot->src_iz, w1);
+                a.inj_val2 = w2;
+                a.inj_steps = (i1 ? 1 : 0) | (i2 ? 2 : 0);
+            }
+            if (nrec > 0 && c.seis) {
+                a.rz = (int)R.z;
+                a.rx0 = (int)R.x0;
+                a.rsx = (int)R.sx;
+                a.rnx = (int)R.nx;
+                a.ry0 = (int)R.y0;
+                a.rsy = (int)R.sy;
+                a.rny = (int)R.ny;
+                a.seis_row = c.seis + (size_t)t * (size_t)nrec;
+                a.seis_row2 = c.seis + (size_t)(t + 1) * (size_t)nrec;
+            }
+            if (store) {
+                a.snap_out = c.segbuf + (size_t)(t - t0) * per;
+                a.amax_cur = c.amax_seg + (t - t0);
+                if (pending) {
+                    a.snap_out2 = c.segbuf + (size_t)(t - 1 - t0) * per;
+                    a.amax_cur2 = c.amax_seg + (t - 1 - t0);
+                }
+                a.amax_next = c.amax_seg + (t - t0) + 1;
+                a.amax_next2 = c.amax_seg + (t - t0) + 2;
+                pending = true;
+            }
+            ST_TRY(fused_step2_forward(s, a, store ? c.kind : SNAP_NONE));
+            c.stats.forward_steps += 2;
+            ++t;
+            continue;
+        }
+        if (store) ST_TRY(store_pending(t));
         StepArgs a = base_args(s, nullptr);
         float wn = 0.0f;
         if (t + 1 < shot->nt && finite_sample(shot->wavelet, shot->wavelet_len, t + 1, &wn))
@@ -183,6 +236,7 @@ int forward_steps(CkptRun& c, int t0, int t1, bool store) {
         ST_TRY(fused_step(s, a, store ? c.kind : SNAP_NONE, SNAP_NONE, 0, nullptr));
         c.stats.forward_steps += 1;
     }
+    if (store) ST_TRY(store_pending(t1));
     return ST_OK;
 }
 
@@ -351,20 +405,24 @@ int checkpointed_adjoint(st_solver* s, const st_shot* shot, int snap_kind, int s
     c.stats.segments = c.nseg;
     c.stats.segment_steps = c.seg;
 
-    // device memory: 3 working fields | slots x 2 fields | K snapshots | K+1 scales
+    // device memory: 4 working fields | slots x 2 fields | K snapshots | K+1 scales
     auto al = [](size_t b) { return ((b + 255) / 256) * 256; };
     const size_t fbytes = al((size_t)L.elems * sizeof(float));
     const size_t sbytes = al(c.per() * (size_t)c.seg);
     const size_t abytes = al(sizeof(unsigned) * (size_t)(c.seg + 1));
-    const size_t total = fbytes * (3 + 2 * (size_t)c.nslots) + sbytes + abytes;
+    const size_t total = fbytes * (4 + 2 * (size_t)c.nslots) + sbytes + abytes;
     ST_TRY(ensure_buffer(s, &s->ckpt_buf, &s->ckpt_cap, total));
     c.stats.device_bytes = (int64_t)total;
     char* p = static_cast<char*>(s->ckpt_buf);
     for (int k = 0; k < 3; ++k) c.g[k] = reinterpret_cast<float*>(p + (size_t)k * fbytes);
     c.slots = reinterpret_cast<float*>(p + 3 * fbytes);
-    c.segbuf = p + fbytes * (3 + 2 * (size_t)c.nslots);
+    c.g4 = reinterpret_cast<float*>(p + fbytes * (3 + 2 * (size_t)c.nslots));
+    c.segbuf = p + fbytes * (4 + 2 * (size_t)c.nslots);
     c.amax_seg = reinterpret_cast<unsigned*>(c.segbuf + sbytes);
     for (int k = 0; k < 3; ++k) ST_TRY(build_field_maps(&c.gm[k], c.g[k], L));
+    // the set's spare: zero once, its halo stays zero (two-step launches write interiors only)
+    ST_CUDA(cudaMemsetAsync(c.g4, 0, (size_t)L.elems * sizeof(float), s->stream));
+    ST_TRY(build_field_maps(&c.gm4, c.g4, L));
     if (epi == 2) ST_TRY(build_snap_map_grad(&c.msnap, c.segbuf, snap_kind, L, c.seg));
     c.grad_pairs = epi == 2 && s->fused_steps == 2 && L.nz % 4 == 0;
     if (c.grad_pairs) ST_TRY(make_compact_map(&c.mgrad, c.grad_c, L, FD_TZ, 16));
