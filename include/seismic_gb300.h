@@ -174,8 +174,8 @@ int st_solver_fault_stats(st_solver* s, st_fault_stats* out);
  * solver (the imaging pass exchanges field buffers). */
 int st_solver_device_field(st_solver* s, int which, float** out);
 /* Time steps per launch of the shot-level passes (st_shot_forward, st_rtm_shot
- * and its host variant, the forward and adjoint passes of the FWI gradient,
- * the adjoint passes of the checkpointed entry points): 2 (default) runs two
+ * and its host variant, the forward and adjoint passes of the FWI gradient
+ * and of the checkpointed entry points): 2 (default) runs two
  * steps in one launch (with the imaging or gradient terms of both fused), 1
  * one step per launch; seismograms, snapshots, images, gradients and fields
  * are bit-identical either way. The time loops of WaveEquationSolver::
