@@ -40,6 +40,7 @@
 #include "st_kernels.cuh"
 
 #include <algorithm>
+#include <cfloat>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -1014,10 +1015,18 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     int fired = 0;
     int timed_out = 0;
 
+    // stage of plane i (s), of plane i-1 (sp) and the phase parity of stage s,
+    // kept by increment; 64-bit offsets of plane i-2's centre group in the
+    // device-layout fields (ob) and in the compact volumes (cb), advanced by a
+    // plane per iteration once sub-step B runs
+    int s = 0, sp = STAGES - 1;
+    unsigned parity = 0;
+    long long ob = (long long)(xa + 1) * a.plane + (long long)(yc + 1) * a.NZP + zc + Layout::ZOFF;
+    long long cb = ((long long)xa * a.ny + yc) * a.nz + zc;
+    const long long cplane = (long long)a.ny * a.nz;
     int i = 0;
     for (; i < nplanes; ++i) {
-        const int s = i % STAGES;
-        if (!mbar_wait_bounded(&bar[s], (i / STAGES) & 1, a.timeout_ns)) timed_out = 1;
+        if (!mbar_wait_bounded(&bar[s], parity, a.timeout_ns)) timed_out = 1;
         float up[4], rp[4] = {0, 0, 0, 0}, zp_ = 0.0f;
         ld4(st_cur(s) + tcen, up);
         if (has_yr) ld4(st_cur(s) + tyr, rp);
@@ -1028,7 +1037,6 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
             // sub-step A on plane i-1 (interior x = xa - 3 + i); it writes the
             // ring buffer of plane i-1, which no thread reads before the
             // barrier that ends this iteration
-            const int sp = (i - 1) % STAGES;
             const int x = xa - 3 + i;
             const bool xin = x >= 0 && x < a.nx;
             const bool own = x >= xa && x < xb;  // this chunk's plane: sampling, snapshots, max
@@ -1153,13 +1161,11 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                     for (int k = 0; k < 4; ++k) amax2 = fmaxf(amax2, fabsf(res[k]));
                 }
             }
-            const long long ob = (long long)(x + 1) * a.plane + (long long)(yc + 1) * a.NZP + zc + Layout::ZOFF;
             st4(a.out + ob, l0);
             st4(a.out2 + ob, res);
             if constexpr (ADJ) {
                 // imaging: step t pairs lambda_t with the snapshot of t, step t-1
                 // pairs lambda' with the snapshot of t-1, in that order
-                const int sp = (i - 1) % STAGES;
                 float fa[4], fb[4], im[4], il[4];
                 snap_smem4<SK>(st_sa(sp), ccen, fa);
                 snap_smem4<SK>(st_sb(sp), ccen, fb);
@@ -1170,25 +1176,23 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                     const float w = a.stable_sponge ? cprev[k] * D[k] : cprev[k];
                     float f = fa[k] * scale_a;
                     float ad = __fdividef(um[k], w);
-                    if (!isfinite(f)) f = 0.0f;
-                    if (!isfinite(ad)) ad = 0.0f;
+                    if (!(fabsf(f) <= FLT_MAX)) f = 0.0f;  // not finite
+                    if (!(fabsf(ad) <= FLT_MAX)) ad = 0.0f;
                     im[k] = fmaf(f, ad, im[k]);
                     il[k] = fmaf(f, f, il[k]);
                     f = fb[k] * scale_b;
                     ad = __fdividef(l0[k], w);
-                    if (!isfinite(f)) f = 0.0f;
-                    if (!isfinite(ad)) ad = 0.0f;
+                    if (!(fabsf(f) <= FLT_MAX)) f = 0.0f;  // not finite
+                    if (!(fabsf(ad) <= FLT_MAX)) ad = 0.0f;
                     im[k] = fmaf(f, ad, im[k]);
                     il[k] = fmaf(f, f, il[k]);
                 }
-                const long long cb = ((long long)x * a.ny + yc) * a.nz + zc;
                 st4(a.image + cb, im);
                 st4(a.illum + cb, il);
             }
             if constexpr (GRD) {
                 // gradient: step t pairs lambda_t with L(snapshot of t), step t-1
                 // pairs lambda' with L(snapshot of t-1), in that order
-                const int sp = (i - 1) % STAGES;
                 float fa[4], fb[4], g[4];
                 snap_lap4<SK, G::GSW>(st_sa(sp), st_sa(s), gsrow, sm_a, a, scale_a, fa);
                 snap_lap4<SK, G::GSW>(st_sb(sp), st_sb(s), gsrow, sm_b, a, scale_b, fb);
@@ -1198,13 +1202,12 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                     g[k] = fmaf(um[k] / cprev[k], fa[k], g[k]);
                     g[k] = fmaf(l0[k] / cprev[k], fb[k], g[k]);
                 }
-                st4(a.grad + ((long long)x * a.ny + yc) * a.nz + zc, g);
+                st4(a.grad + cb, g);
             }
         }
         if constexpr (GRD) {
             // the snapshot centres of plane i-2 are the next plane's x-1 values
             if (i >= 3) {
-                const int sp = (i - 1) % STAGES;
                 snap_smem4<SK>(st_sa(sp), gsrow, sm_a);
                 snap_smem4<SK>(st_sb(sp), gsrow, sm_b);
             }
@@ -1222,6 +1225,15 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
         zm_ = z0_;
         z0_ = zp_;
         irx_prev = irx;
+        sp = s;
+        if (++s == STAGES) {
+            s = 0;
+            parity ^= 1u;
+        }
+        if (i >= 4) {
+            ob += a.plane;
+            cb += cplane;
+        }
         // every thread is done with the slot of plane i-1 and the ring buffer
         // of plane i-2: refill the one, let the next iteration overwrite the other
         if (__syncthreads_or(timed_out)) break;
