@@ -522,16 +522,19 @@ def run_gpu(args):
         bwd_kernel = f"fd_step2_kernel<adjoint, {snap}> (two adjoint steps + imaging)"
         fwd_kernel = f"fd_step2_kernel<forward, {snap}> (two forward steps + snapshot stores)"
         launches_per_pass, traffic_key = w.nt // 2, "fd_step2_image_bf16_256"
+        traffic_key_fwd = "fd_step2_forward_bf16_256"
     else:
         bwd_kernel = f"fd_step_kernel<SNAP_NONE, {snap}, imaging> (adjoint step + imaging)"
         fwd_kernel = f"fd_step_kernel<{snap}, NONE> (forward step + snapshot store)"
         launches_per_pass, traffic_key = w.nt, "fd_step_adjoint_image_bf16_256"
+        traffic_key_fwd = "fd_step_forward_bf16_256"
     bwd_launch_ms = statistics.mean(bwd_ms) / launches_per_pass
     fwd_launch_ms = statistics.mean(fwd_ms) / launches_per_pass
     bw_bwd = bwd_bytes * npts / (bwd_launch_ms / 1e3) / 1e9
     bw_fwd = fwd_bytes * npts / (fwd_launch_ms / 1e3) / 1e9
     alg_total = (fwd_bytes + bwd_bytes) * launches_per_pass * npts * args.steps
     traffic = profile_traffic(traffic_key) if args.snap == "bf16" and w.nx == 256 else None
+    traffic_fwd = profile_traffic(traffic_key_fwd) if args.snap == "bf16" and w.nx == 256 else None
     line = {
         "metric": METRIC, "value": value, "unit": "Gpts/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": el_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -546,7 +549,7 @@ def run_gpu(args):
                      "steps_per_launch": 2 if paired else 1},
         "roofline_forward": {"bound": "hbm", "kernel": fwd_kernel,
                              "achieved": bw_fwd, "peak": hbm_peak, "unit": "GB/s", "frac": bw_fwd / hbm_peak,
-                             "alg_bytes_per_launch": fwd_bytes * npts, "launch_ms": fwd_launch_ms,
+                             "traffic": traffic_fwd, "alg_bytes_per_launch": fwd_bytes * npts, "launch_ms": fwd_launch_ms,
                              "steps_per_launch": 2 if paired else 1},
         "phases_ms_per_step": {"forward": statistics.mean(fwd_ms), "backward": statistics.mean(bwd_ms)},
         "gpu_launches": launches,
