@@ -229,3 +229,17 @@ def test_two_steps_per_launch_small_grids(se, n, nt):
         two = run(se, *args, steps=2)
         for a, b in zip(one, two):
             assert np.array_equal(a, b), run.__name__
+
+
+def test_two_steps_per_launch_mid_size_partial_tiles(se):
+    """301 x 203 x 136: several x-chunks, a last y tile of 11 rows and a last
+    z tile of 8 points, in all three modes."""
+    n, nt, rz = (301, 203, 136), 14, 100
+    src = (150, 101, 97)
+    for run, args in ((run_rtm, (n, nt, "stable", rz, 1)),
+                      (run_forward, (n, nt, "stable", src, rz, 1)),
+                      (run_gradient, (n, nt, "stable", src, rz, 1))):
+        one = run(se, *args, steps=1)
+        two = run(se, *args, steps=2)
+        for a, b in zip(one, two):
+            assert np.array_equal(a, b), run.__name__
