@@ -1,13 +1,28 @@
 #!/usr/bin/env bash
-# Builds oracle/_ref/libseismic_ref.so from the reference's own C++ sources, in
-# place (they are read, never copied), plus oracle/ref_harness.cpp, a
-# single-rank MPI stub header (oracle/mpi_stub/mpi.h) and stubs for the two
-# off-path RTM streaming classes whose shipped sources do not compile
-# (oracle/ref_stubs.cpp). Flags are the reference's own (CMakeLists.txt:24-35)
-# plus -fno-finite-math-only: under plain -ffast-math GCC folds std::isfinite
-# to true, which deletes the reference's NaN/Inf guards
-# (wave_equation.cpp:345-397, rtm_engine.cpp:45-48, fault_tolerance.cpp:72-157);
-# the fixtures pin the guards as written in the source.
+# Builds oracle/_ref/libseismic_ref.so from the reference's own C++ sources
+# plus oracle/ref_harness.cpp, a single-rank MPI stub header
+# (oracle/mpi_stub/mpi.h) and stubs for the two off-path RTM streaming classes
+# whose shipped sources do not compile (oracle/ref_stubs.cpp). Flags are the
+# reference's own (CMakeLists.txt:24-35) plus -fno-finite-math-only: under
+# plain -ffast-math GCC folds std::isfinite to true, which deletes the
+# reference's NaN/Inf guards (wave_equation.cpp:345-397, rtm_engine.cpp:45-48,
+# fault_tolerance.cpp:72-157); the fixtures pin the guards as written.
+#
+# core/, solver/ and rtm/ compile where they lie (read, never copied). The
+# sparse module does not compile as shipped, so its five files are copied at
+# build time into the git-ignored oracle/_ref/patched/sparse/ and receive the
+# three minimal fixes below (sed; each is checked to have applied). Every
+# sparse source and the harness compile against that copy, so all translation
+# units see one AlignedVector.
+#   1. aligned_alloc.h:38: a copy constructor (element-wise copy) in place of
+#      the deleted one, which sparse_ops.cpp:17-18,75,78,207 use.
+#   2. aligned_alloc.h:71-75: resize() fills new elements with `value` always;
+#      as shipped it skips the fill when value == T(), which leaves CG's
+#      x0 = 0 (sparse_ops.cpp:15,59) and spmv_transpose's accumulator
+#      (csr_matrix.cpp:153) uninitialised.
+#   3. csr_matrix.cpp:233-234: pad_to_alignment allocates nnz + 8 * rows
+#      entries (an upper bound of the padded total) instead of a size that is
+#      too small whenever padding fires (heap overflow).
 # x86-64 only (the reference includes <x86intrin.h>/<immintrin.h>); the GPU
 # box has no reference sources, so this runs only where they are present.
 set -euo pipefail
@@ -24,11 +39,24 @@ case "$(uname -m)" in
   *) echo "reference sources need x86 intrinsics; skipping oracle/_ref on $(uname -m)" >&2; exit 0 ;;
 esac
 mkdir -p "$OUT"
+PS="$OUT/patched/sparse"
+rm -rf "$OUT/patched"
+mkdir -p "$PS"
+for f in aligned_alloc.h csr_matrix.h csr_matrix.cpp sparse_ops.h sparse_ops.cpp; do
+  cp "$SRC/sparse/$f" "$PS/$f"
+  chmod u+w "$PS/$f"
+done
+sed -i 's|AlignedVector(const AlignedVector&) = delete;|AlignedVector(const AlignedVector\& o) : data_(nullptr), size_(0), capacity_(0) { resize(o.size_); for (size_t i = 0; i < o.size_; ++i) data_[i] = o.data_[i]; }|' "$PS/aligned_alloc.h"
+sed -i 's|if (value != T()) {|{|' "$PS/aligned_alloc.h"
+sed -i 's|(nnz_ + new_nnz - current_nnz)|(nnz_ + 8 * rows_)|g' "$PS/csr_matrix.cpp"
+grep -q 'AlignedVector(const AlignedVector& o)' "$PS/aligned_alloc.h" || { echo "patch 1 did not apply" >&2; exit 1; }
+! grep -q 'value != T()' "$PS/aligned_alloc.h" || { echo "patch 2 did not apply" >&2; exit 1; }
+[ "$(grep -c '(nnz_ + 8 \* rows_)' "$PS/csr_matrix.cpp")" = 2 ] || { echo "patch 3 did not apply" >&2; exit 1; }
 g++ -std=c++17 -O3 -ffast-math -fno-finite-math-only $ARCHFLAGS -fPIC -shared -w \
-  -include functional -I"$HERE/mpi_stub" -I"$SRC" \
+  -include functional -I"$HERE/mpi_stub" -I"$OUT/patched" -I"$SRC" \
   "$SRC/core/grid.cpp" "$SRC/core/mpi_context.cpp" "$SRC/core/config.cpp" \
   "$SRC/core/fault_tolerance.cpp" "$SRC/solver/wave_equation.cpp" "$SRC/solver/boundary.cpp" \
-  "$SRC/rtm/rtm_engine.cpp" "$SRC/rtm/mmap_writer.cpp" "$SRC/sparse/csr_matrix.cpp" \
+  "$SRC/rtm/rtm_engine.cpp" "$SRC/rtm/mmap_writer.cpp" "$PS/csr_matrix.cpp" "$PS/sparse_ops.cpp" \
   "$HERE/ref_stubs.cpp" "$HERE/ref_harness.cpp" \
   -o "$OUT/libseismic_ref.so.tmp" -Wl,--no-undefined -lpthread
 mv "$OUT/libseismic_ref.so.tmp" "$OUT/libseismic_ref.so"

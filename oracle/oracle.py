@@ -387,6 +387,15 @@ class Reference:
                                                                         C.c_double])
         L.ref_mmap_count_frames.argtypes = [C.c_char_p]
         L.ref_mmap_count_frames.restype = C.c_int64
+        L.ref_csr_fd_stencil.argtypes = [C.c_int64] * 3 + [_d] + [C.c_double] * 4
+        L.ref_csr_fd_stencil.restype = C.c_int64
+        L.ref_csr_spmv_t.argtypes = [_d, C.c_int64, _d]
+        L.ref_hessian_approx.argtypes = [C.c_double]
+        L.ref_hessian_approx.restype = C.c_int64
+        L.ref_cg.argtypes = [C.c_int, _d, C.c_int64, C.c_int, C.c_double, _d]
+        L.ref_dot.argtypes = [_d, _d, C.c_int64]
+        L.ref_dot.restype = C.c_double
+        L.ref_smooth_gradient.argtypes = [_d, C.c_int64, C.c_int64, C.c_int64, C.c_double, _d]
 
     def extract_slices(self, nx, ny, nz, specs, fwd, adj, ic, timestep=0):
         """RTMEngine::extract_slices with a collecting callback: a list of
@@ -503,6 +512,49 @@ class Reference:
         y = np.zeros(rows)
         self.lib.ref_csr_spmv(_p(x, _d), x.size, _p(y, _d))
         return y
+
+    def _csr_get(self, rows, nnz):
+        rp = np.zeros(rows + 1, np.int64)
+        col = np.zeros(max(nnz, 1), np.int64)
+        val = np.zeros(max(nnz, 1))
+        self.lib.ref_csr_get(_p(rp, _i64), _p(col, _i64), _p(val, _d))
+        return rp, col[:nnz], val[:nnz]
+
+    def csr_fd_stencil(self, nx, ny, nz, vel, dx, dy, dz, dt):
+        """CSRMatrix::build_fd_stencil_7point; becomes the current matrix."""
+        v = np.ascontiguousarray(vel, np.float64)
+        nnz = self.lib.ref_csr_fd_stencil(nx, ny, nz, _p(v, _d), dx, dy, dz, dt)
+        return self._csr_get(nx * ny * nz, nnz)
+
+    def csr_spmv_t(self, x, cols):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(cols)
+        self.lib.ref_csr_spmv_t(_p(x, _d), x.size, _p(y, _d))
+        return y
+
+    def hessian_approx(self, reg, rows):
+        """SparseOps::build_hessian_approx of the current matrix (replaces it)."""
+        nnz = self.lib.ref_hessian_approx(reg)
+        return self._csr_get(rows, nnz)
+
+    def cg(self, b, max_iter, tol, jacobi=False):
+        """SparseOps::conjugate_gradient / jacobi_preconditioned_cg on the
+        current matrix (square)."""
+        b = np.ascontiguousarray(b, np.float64)
+        x = np.zeros(b.size)
+        self.lib.ref_cg(int(jacobi), _p(b, _d), b.size, int(max_iter), float(tol), _p(x, _d))
+        return x
+
+    def dot(self, a, b):
+        a = np.ascontiguousarray(a, np.float64)
+        b = np.ascontiguousarray(b, np.float64)
+        return self.lib.ref_dot(_p(a, _d), _p(b, _d), min(a.size, b.size))
+
+    def smooth_gradient(self, g, nx, ny, nz, sigma):
+        g = np.ascontiguousarray(g, np.float64)
+        out = np.zeros(nx * ny * nz)
+        self.lib.ref_smooth_gradient(_p(g, _d), nx, ny, nz, float(sigma), _p(out, _d))
+        return out
 
     def repair_field_nan(self, data, nx, ny, nz, hw=1, repl=0.0):
         d = np.array(data, np.float64, copy=True)

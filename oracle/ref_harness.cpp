@@ -327,3 +327,72 @@ int ref_terrain(int64_t nx, int64_t ny, int64_t nz, double dx, double dy, double
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- sparse ops
+// Built against the patched scratch copy of sparse/ (oracle/build_ref.sh lists
+// the three fixes); every call below runs the reference's own code on it.
+#include "sparse/sparse_ops.h"
+
+namespace {
+seismic::AlignedVector<double> to_aligned(const double* p, int64_t n) {
+    seismic::AlignedVector<double> v(n);
+    for (int64_t i = 0; i < n; ++i) v[i] = p[i];
+    return v;
+}
+}  // namespace
+
+extern "C" {
+
+// CSRMatrix::build_fd_stencil_7point (sparse/csr_matrix.cpp:74-116) into the
+// current matrix (its build_from_triplets pads every row to a multiple of 8,
+// the fixed pad_to_alignment). Returns nnz.
+int64_t ref_csr_fd_stencil(int64_t nx, int64_t ny, int64_t nz, const double* vel, double dx, double dy, double dz,
+                           double dt) {
+    g_csr = std::make_unique<seismic::CSRMatrix>();
+    g_csr->build_fd_stencil_7point(nx, ny, nz, vel, dx, dy, dz, dt);
+    return g_csr->nnz();
+}
+
+// CSRMatrix::spmv_transpose (sparse/csr_matrix.cpp:151-166) on the current
+// matrix; with the zero-fill fix its accumulator starts at 0.
+int ref_csr_spmv_t(const double* x, int64_t nxv, double* y) {
+    if (!g_csr) return -1;
+    auto yv = g_csr->spmv_transpose(to_aligned(x, nxv));
+    for (int64_t j = 0; j < g_csr->cols(); ++j) y[j] = yv[j];
+    return 0;
+}
+
+// SparseOps::build_hessian_approx (sparse/sparse_ops.cpp:204-210): the current
+// matrix is replaced by the returned copy with reg added to its diagonal.
+int64_t ref_hessian_approx(double reg) {
+    if (!g_csr) return -1;
+    auto h = std::make_unique<seismic::CSRMatrix>(seismic::SparseOps::build_hessian_approx(*g_csr, reg));
+    g_csr = std::move(h);
+    return g_csr->nnz();
+}
+
+// SparseOps::conjugate_gradient (jacobi == 0) or jacobi_preconditioned_cg
+// (jacobi != 0) (sparse/sparse_ops.cpp:8-113) on the current matrix.
+int ref_cg(int jacobi, const double* b, int64_t n, int max_iter, double tol, double* x) {
+    if (!g_csr) return -1;
+    auto bv = to_aligned(b, n);
+    auto xv = jacobi ? seismic::SparseOps::jacobi_preconditioned_cg(*g_csr, bv, max_iter, tol)
+                     : seismic::SparseOps::conjugate_gradient(*g_csr, bv, max_iter, tol);
+    for (int64_t i = 0; i < g_csr->rows(); ++i) x[i] = xv[i];
+    return 0;
+}
+
+// SparseOps::dot_product (sparse/sparse_ops.cpp:172-187).
+double ref_dot(const double* a, const double* b, int64_t n) {
+    return seismic::SparseOps::dot_product(to_aligned(a, n), to_aligned(b, n));
+}
+
+// SparseOps::smooth_gradient (sparse/sparse_ops.cpp:115-158).
+int ref_smooth_gradient(const double* g, int64_t nx, int64_t ny, int64_t nz, double sigma, double* out) {
+    std::vector<double> gv(g, g + nx * ny * nz);
+    auto r = seismic::SparseOps::smooth_gradient(gv, nx, ny, nz, sigma);
+    std::memcpy(out, r.data(), r.size() * sizeof(double));
+    return 0;
+}
+
+}  // extern "C"

@@ -9,14 +9,15 @@
  * legs of bench.py load this library, and only as the checker or the timed CPU
  * baseline. The product (the CUDA library) never links or calls it.
  *
- * Pinning: the propagator, RTM imaging, CSR build and SpMV here are checked
- * against the reference's own C++ (built by oracle/build_ref.sh) in
- * tests/test_oracle_pins.py and through the committed fixtures in
- * tests/golden/ (generated by tests/golden/make_golden.py). The CG / PCG loops
- * and the Gaussian smoothing restate sparse/sparse_ops.cpp, which does not
- * compile as shipped (AlignedVector has a deleted copy constructor), so they
- * are pinned only through their building blocks (spmv, dot order) and by
- * known properties (exact solves of small SPD systems).
+ * Pinning: the propagator, RTM imaging, CSR build (with and without the
+ * padding rule), SpMV / SpMV^T, the CG / Jacobi-PCG loops, dot_product and
+ * the Gaussian smoothing here are checked against the reference's own C++
+ * (built by oracle/build_ref.sh; sparse/ from a scratch copy with the three
+ * minimal fixes listed there) through the committed fixtures in tests/golden/
+ * (tests/golden/make_golden.py, make_golden_sparse.py) in
+ * tests/test_oracle_golden.py. The exact adjoint and the normal-equation
+ * operator have no reference counterpart: they are pinned by properties
+ * (dot-product and Taylor tests).
  */
 #include <math.h>
 #include <stdint.h>

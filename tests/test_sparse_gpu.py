@@ -222,3 +222,57 @@ def test_regularised_update_with_given_rhs(se):
     it, rel, true_rel = se.normal_cg_device(L, None, 1.0, x, 2000, 1e-7, True, rhs=rhs)
     assert true_rel < 5e-6  # FP32 vectors: the attainable true residual of this operator is about 1e-6
     assert np.linalg.norm(x.cpu().numpy() - xs) <= 1e-5 * np.linalg.norm(xs)
+
+
+def _unpadded(rp, col, val):
+    rows = np.repeat(np.arange(rp.size - 1), np.diff(rp))
+    keep = ~((col == rows) & (val == 0.0))
+    return rows[keep], col[keep], val[keep]
+
+
+def test_sparse_ops_match_reference_fixture(se, golden_dir):
+    """The GPU sparse path against the reference's own sparse module
+    (sparse_small.npz, from sparse/csr_matrix.cpp + sparse/sparse_ops.cpp
+    built with the three fixes oracle/build_ref.sh lists): the padded FD
+    stencil build, SpMV / SpMV^T, CG and Jacobi-PCG at tol 1e-6 (iterations
+    within 1, solutions within 1e-5 relative: FP32 vectors, FP64 scalars),
+    dot_product, smooth_gradient and build_hessian_approx."""
+    g = np.load(os.path.join(golden_dir, "sparse_small.npz"))
+    nx, ny, nz = (int(v) for v in g["fd_n"])
+    dx, dy, dz, dt = (float(v) for v in g["fd_d"])
+    n = nx * ny * nz
+    fd = se.CSRMatrix().build_fd_stencil_7point(nx, ny, nz, g["fd_vel"], dx, dy, dz, dt, pad=True)
+    np.testing.assert_array_equal(fd.row_ptr(), g["fd_row_ptr"])
+    np.testing.assert_array_equal(fd.col_ind(), g["fd_col"])
+    np.testing.assert_allclose(fd.values(), f32(g["fd_val"]), rtol=2.0 ** -23, atol=0)
+    for got, ref in ((fd.spmv(g["fd_x"]), g["fd_y"]), (fd.spmv_transpose(g["fd_xt"]), g["fd_yt"])):
+        assert np.linalg.norm(got - ref) <= 1e-6 * np.linalg.norm(ref)
+    sr, sc, sv = _unpadded(g["spd_row_ptr"], g["spd_col"], g["spd_val"])
+    spd = se.CSRMatrix().build_from_triplets(200, 200, sr, sc, sv, pad=True)
+    np.testing.assert_array_equal(spd.row_ptr(), g["spd_row_ptr"])
+    np.testing.assert_array_equal(spd.col_ind(), g["spd_col"])
+    np.testing.assert_array_equal(spd.values(), f32(g["spd_val"]))
+    assert np.linalg.norm(spd.spmv(g["spd_x"]) - g["spd_y"]) <= 1e-6 * np.linalg.norm(g["spd_y"])
+    for name, m in (("fd", fd), ("spd", spd)):
+        for jac, fn in ((0, se.SparseOps.conjugate_gradient), (1, se.SparseOps.jacobi_preconditioned_cg)):
+            key = f"cg_{name}_{jac}_6"
+            x = fn(m, g[f"{name}_b"], 10000, 1e-6)
+            assert abs(se.SparseOps.last_iterations - int(g[key + "_iters"])) <= 1, (key, se.SparseOps.last_iterations)
+            assert np.linalg.norm(x - g[key + "_x"]) <= 1e-5 * np.linalg.norm(g[key + "_x"])
+    assert np.array_equal(se.SparseOps.conjugate_gradient(fd, np.zeros(n), 100, 1e-6), g["cg_fd_zero_x"])
+    offs = np.concatenate([[0], np.cumsum(g["dot_lens"])])
+    for i in range(g["dot_lens"].size):
+        a, b = g["dot_a"][offs[i]:offs[i + 1]], g["dot_b"][offs[i]:offs[i + 1]]
+        assert abs(se.SparseOps.dot_product(a, b) - g["dot_out"][i]) <= 1e-14 * np.abs(a * b).sum()
+    sn = tuple(int(v) for v in g["smooth_n"])
+    for s, ref in zip(g["smooth_sigma"], g["smooth_out"]):
+        np.testing.assert_allclose(se.SparseOps.smooth_gradient(g["smooth_g"], *sn, float(s)), ref,
+                                   rtol=1e-12, atol=1e-13)
+    H = se.SparseOps.build_hessian_approx(fd, 0.37)
+    np.testing.assert_array_equal(H.row_ptr(), g["fd_row_ptr"])
+    np.testing.assert_allclose(H.values(), f32(g["hess_fd_val"]), rtol=2.0 ** -23, atol=0)
+    R = se.CSRMatrix().build_from_triplets(40, 30, g["hess_rand_r"], g["hess_rand_c"], g["hess_rand_v"])
+    HR = se.SparseOps.build_hessian_approx(R, 0.37)
+    np.testing.assert_array_equal(HR.row_ptr(), g["hess_rand_row_ptr"])
+    np.testing.assert_array_equal(HR.col_ind(), g["hess_rand_col"])
+    np.testing.assert_array_equal(HR.values(), f32(g["hess_rand_val"]))
