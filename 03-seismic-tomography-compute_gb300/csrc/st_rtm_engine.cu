@@ -30,6 +30,31 @@ __global__ void image_kernel(const double* __restrict__ fwd, const double* __res
     }
 }
 
+// The same condition on two FP32 fields of the solver's device layout
+// (apply_rtm_step, wave_equation.cpp:598-619): values widened to FP64.
+__global__ void image_device_kernel(const float* __restrict__ fwd, const float* __restrict__ adj, stg::Layout L,
+                                    double* __restrict__ image, double* __restrict__ illum) {
+    const long long n = L.nx * L.ny * L.nz;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const long long ix = k / (L.ny * L.nz), r = k % (L.ny * L.nz), iy = r / L.nz, iz = r % L.nz;
+        const long long i = L.at(ix, iy, iz);
+        const double f0 = fwd[i], a0 = adj[i];
+        const double f = isfinite(f0) ? f0 : 0.0;
+        const double a = isfinite(a0) ? a0 : 0.0;
+        image[k] = __dadd_rn(image[k], __dmul_rn(f, a));
+        illum[k] = __dadd_rn(illum[k], __dmul_rn(f, f));
+    }
+}
+
+// Loads FP32 image / illumination accumulators into the FP64 ones.
+__global__ void load_fp32_kernel(const float* __restrict__ image32, const float* __restrict__ illum32,
+                                 double* __restrict__ image, double* __restrict__ illum, long long n) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        image[k] = image32[k];
+        illum[k] = illum32[k];
+    }
+}
+
 // RTMEngine::finalize_image (rtm_engine.cpp:170-182).
 __global__ void finalize_kernel(const double* __restrict__ image, const double* __restrict__ illum,
                                 double* __restrict__ refl, long long n) {
@@ -55,6 +80,7 @@ struct st_rtm_engine {
     double* fwd = nullptr;  // staging of one padded field each
     double* adj = nullptr;
     size_t stage_cap = 0;
+    bool own_stream = true;  // false: the stream of the solver that owns the engine
 };
 
 using namespace stg;
@@ -95,7 +121,7 @@ int st_rtm_engine_destroy(st_rtm_engine* e) {
     cudaFree(e->refl);
     cudaFree(e->fwd);
     cudaFree(e->adj);
-    if (e->stream) cudaStreamDestroy(e->stream);
+    if (e->stream && e->own_stream) cudaStreamDestroy(e->stream);
     delete e;
     return ST_OK;
 }
@@ -168,3 +194,38 @@ int st_rtm_engine_result(st_rtm_engine* e, double* image, double* illumination, 
 }
 
 }  // extern "C"
+
+namespace stg {
+
+// The engine of a solver's RTM driver: it runs on the solver's stream, so
+// its work is ordered with the solver's steps.
+int rtm_engine_create_on_stream(int64_t nx, int64_t ny, int64_t nz, double dx, double dy, double dz, int device,
+                                cudaStream_t stream, st_rtm_engine** out) {
+    ST_TRY(st_rtm_engine_create(nx, ny, nz, dx, dy, dz, 1, device, out));
+    st_rtm_engine* e = *out;
+    cudaStreamDestroy(e->stream);
+    e->stream = stream;
+    e->own_stream = false;
+    return ST_OK;
+}
+
+int rtm_engine_image_fields(st_rtm_engine* e, const float* fwd, const float* adj, const Layout& L) {
+    ST_CHECK(e && fwd && adj && L.nx == e->nx && L.ny == e->ny && L.nz == e->nz, ST_ERR_ARG,
+             "engine and field extents differ");
+    image_device_kernel<<<blocks(e->nx * e->ny * e->nz), 256, 0, e->stream>>>(fwd, adj, L, e->image, e->illum);
+    count_launch();
+    ST_CUDA(cudaGetLastError());
+    return ST_OK;
+}
+
+int rtm_engine_load_fp32(st_rtm_engine* e, const float* image, const float* illum) {
+    const long long n = e->nx * e->ny * e->nz;
+    load_fp32_kernel<<<blocks(n), 256, 0, e->stream>>>(image, illum, e->image, e->illum, n);
+    count_launch();
+    ST_CUDA(cudaGetLastError());
+    return ST_OK;
+}
+
+const double* rtm_engine_image(const st_rtm_engine* e) { return e->image; }
+
+}  // namespace stg

@@ -349,11 +349,11 @@ int health_check(st_solver* s, int timestep, int* result) {
     ::stg::count_launch();
         repair_nan_kernel<<<1, 1024, 0, s->stream>>>(s->f[s->ip], s->L, s->dtab, s->sw, 1, 0.0f, s->counter);
     ::stg::count_launch();
-        clamp_view_kernel<<<256, 256, 0, s->stream>>>(s->f[s->ic], s->L, s->dtab, s->sw, 0, (float)-s->amp_limit,
-                                                      (float)s->amp_limit);
+        clamp_view_kernel<<<256, 256, 0, s->stream>>>(s->f[s->ic], s->L, s->dtab, s->sw, 0,
+                                                      (float)-s->ft_amp_limit, (float)s->ft_amp_limit);
     ::stg::count_launch();
-        clamp_view_kernel<<<256, 256, 0, s->stream>>>(s->f[s->ip], s->L, s->dtab, s->sw, 1, (float)-s->amp_limit,
-                                                      (float)s->amp_limit);
+        clamp_view_kernel<<<256, 256, 0, s->stream>>>(s->f[s->ip], s->L, s->dtab, s->sw, 1,
+                                                      (float)-s->ft_amp_limit, (float)s->ft_amp_limit);
     ::stg::count_launch();
         ST_CUDA(cudaGetLastError());
         unsigned long long post = 0;
@@ -509,6 +509,8 @@ int st_solver_create(const st_grid_params* grid, const st_solver_config* cfg, in
 int st_solver_destroy(st_solver* s) {
     if (!s) return ST_OK;
     cudaSetDevice(s->device);
+    rtm_release(s);
+    cudaFree(s->rtm_fwd);
     clear_snaps(s);
     for (int k = 0; k < 3; ++k) cudaFree(s->f[k]);
     cudaFree(s->f4);
@@ -733,6 +735,7 @@ int st_solver_verify_cfl(st_solver* s, int* ok) {
 int st_solver_set_amplitude_limit(st_solver* s, double limit) {
     ST_CHECK(s, ST_ERR_ARG, "null solver");
     s->amp_limit = std::max(1.0, limit);
+    s->ft_amp_limit = s->amp_limit;
     return ST_OK;
 }
 
@@ -796,6 +799,34 @@ int st_solver_get_snapshots(st_solver* s, double* out, int64_t count) {
 int st_solver_fault_stats(st_solver* s, st_fault_stats* out) {
     ST_CHECK(s && out, ST_ERR_ARG, "null argument");
     *out = s->stats;
+    return ST_OK;
+}
+
+int st_solver_reset_fault_stats(st_solver* s) {
+    ST_CHECK(s, ST_ERR_ARG, "null solver");
+    s->stats = st_fault_stats{};
+    return ST_OK;
+}
+
+int st_solver_set_fault_param(st_solver* s, int which, double value) {
+    ST_CHECK(s && std::isfinite(value), ST_ERR_ARG, "bad argument");
+    switch (which) {
+        case ST_FT_MAX_REPAIR_ATTEMPTS: s->max_repair_attempts = (int)std::max(1.0, std::min(value, 1e9)); break;
+        case ST_FT_AMPLITUDE_LIMIT: s->ft_amp_limit = std::max(1.0, value); break;
+        case ST_FT_CFL_SAFETY_FACTOR: s->cfl_safety = std::max(0.01, std::min(value, 0.99)); break;
+        default: ST_CHECK(false, ST_ERR_ARG, "unknown fault-tolerance parameter %d", which);
+    }
+    return ST_OK;
+}
+
+int st_solver_fault_param(st_solver* s, int which, double* out) {
+    ST_CHECK(s && out, ST_ERR_ARG, "null argument");
+    switch (which) {
+        case ST_FT_MAX_REPAIR_ATTEMPTS: *out = s->max_repair_attempts; break;
+        case ST_FT_AMPLITUDE_LIMIT: *out = s->ft_amp_limit; break;
+        case ST_FT_CFL_SAFETY_FACTOR: *out = s->cfl_safety; break;
+        default: ST_CHECK(false, ST_ERR_ARG, "unknown fault-tolerance parameter %d", which);
+    }
     return ST_OK;
 }
 

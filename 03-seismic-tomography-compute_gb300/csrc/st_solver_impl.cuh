@@ -58,7 +58,8 @@ struct st_solver {
     stg::Layout L{};
     st_grid_params grid{};
     st_solver_config cfg{};
-    double amp_limit = 1e10;
+    double amp_limit = 1e10;     // the stencil's amplitude clamp (the solver's amplitude_limit_)
+    double ft_amp_limit = 1e10;  // the repair clamp (its FaultTolerance's amplitude_limit_)
     double cfl_safety = 0.49;
     int max_repair_attempts = 3;
     stg::PinnedVec vel_host;  // reference layout; authoritative unless vel_host_valid is false
@@ -95,6 +96,20 @@ struct st_solver {
     int* zlim = nullptr;                // terrain: per-column z limits (st_solver_set_terrain), or null
     st_slice_stream* slices = nullptr;  // RTM slice stream (configure_rtm), borrowed
     int slice_interval = 0;             // capture every slice_interval steps
+    // RTM driver of the solver face (st_solver_configure_rtm, st_rtm_driver.cu)
+    int rtm_enabled = 0;
+    st_rtm_engine* rtm_engine = nullptr;    // owned; runs on `stream`
+    st_slice_stream* rtm_stream = nullptr;  // owned (configure_rtm with the mmap writer)
+    float* rtm_fwd = nullptr;               // store_forward_wavefield_for_rtm's copy of the current field
+    bool rtm_fwd_valid = false;
+    st_receiver_grid rtm_rec{};
+    int rtm_snap_kind = ST_SNAP_BF16;
+    int rtm_segment = 0;
+    int rtm_interval = 50;
+    int rtm_slices_per_capture = 3;          // non-VOLUME slice specs
+    int64_t rtm_ring_cap = 1024, rtm_attempts = 0, rtm_captured = 0, rtm_dropped = 0;
+    void* rtm_buf = nullptr;                // run_rtm: amax | image | illum | residuals (FP32)
+    size_t rtm_cap = 0;
     // phase boundaries of the last shot-level call, recorded on `stream`:
     // [0] start, [1] forward done, [2] backward done
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
@@ -141,6 +156,16 @@ int launch_rec_force(st_solver* s, const st_receiver_grid& R, const float* row);
 int checkpointed_adjoint(st_solver* s, const st_shot* shot, int snap_kind, int segment_steps, int max_slots, int epi,
                          const float* force, float* image, float* illum, float* grad_c, float* seis,
                          const std::function<int()>& before_backward, st_checkpoint_stats* stats);
+// Helpers of the engine a solver's RTM driver owns (st_rtm_engine.cu).
+int rtm_engine_create_on_stream(int64_t nx, int64_t ny, int64_t nz, double dx, double dy, double dz, int device,
+                                cudaStream_t stream, st_rtm_engine** out);
+// image += fwd * adj, illum += fwd^2 (FP64) over the interior of two device-layout fields.
+int rtm_engine_image_fields(st_rtm_engine* e, const float* fwd, const float* adj, const Layout& L);
+// Overwrites the engine's FP64 image / illumination with FP32 accumulators.
+int rtm_engine_load_fp32(st_rtm_engine* e, const float* image, const float* illum);
+const double* rtm_engine_image(const st_rtm_engine* e);
+// Releases the RTM driver's resources (st_rtm_driver.cu); used by destroy.
+void rtm_release(st_solver* s);
 // The exact-adjoint entry points transpose the unmasked step, so they refuse
 // while a terrain (st_solver_set_terrain) is attached.
 inline int require_no_terrain(const st_solver* s) {

@@ -8,7 +8,7 @@ All compute runs in libseismic_gb300.so (CUDA, sm_103a) through its C ABI
 """
 from ._lib import SeismicError, load as load_library, lib_path  # noqa: F401
 from .wave import (  # noqa: F401
-    FaultStats, GridParams, HealthStatus, PropagationResult, SolverConfig, StepResult, WaveEquationSolver,
+    FaultStats, FaultTolerance, GridParams, HealthStatus, PropagationResult, SolverConfig, StepResult, WaveEquationSolver,
     WaveField, field_layout, rtm_shot, rtm_shot_checkpointed, rtm_shot_host, shot_adjoint, shot_forward,
     shot_forward_host,
 )

@@ -27,6 +27,7 @@ ST_FIELD_CURRENT, ST_FIELD_PREVIOUS, ST_FIELD_NEXT, ST_FIELD_VELOCITY = 0, 1, 2,
 ST_SNAP_NONE, ST_SNAP_BF16, ST_SNAP_FP16, ST_SNAP_FP32 = 0, 1, 2, 3
 ST_SPONGE_REFERENCE, ST_SPONGE_STABLE = 0, 1
 ST_TERRAIN_FREE_SURFACE, ST_TERRAIN_SEAFLOOR = 1, 2
+ST_FT_MAX_REPAIR_ATTEMPTS, ST_FT_AMPLITUDE_LIMIT, ST_FT_CFL_SAFETY_FACTOR = 0, 1, 2
 
 
 class SeismicError(RuntimeError):
@@ -79,6 +80,14 @@ class SliceSpecC(C.Structure):
     _fields_ = [("axis", C.c_int32), ("index", C.c_int64), ("stride", C.c_int64)]
 
 
+class RtmConfigC(C.Structure):
+    _fields_ = [("enable_rtm", C.c_int), ("enable_snapshots", C.c_int), ("snapshot_interval", C.c_int),
+                ("enable_mmap_writer", C.c_int), ("mmap_filename", C.c_char_p), ("mmap_max_bytes", C.c_int64),
+                ("ring_buffer_capacity", C.c_int64), ("slice_specs", C.POINTER(SliceSpecC)),
+                ("n_slice_specs", C.c_int), ("receivers", ReceiverGridC), ("snap_kind", C.c_int),
+                ("checkpoint_segment", C.c_int)]
+
+
 class BathymetryPointC(C.Structure):
     _fields_ = [("x", C.c_double), ("y", C.c_double), ("depth", C.c_double)]
 
@@ -124,6 +133,17 @@ SIGNATURES = {
     "st_solver_snapshot_values": [_vp, _i64],
     "st_solver_get_snapshots": [_vp, _d, C.c_int64],
     "st_solver_fault_stats": [_vp, C.POINTER(FaultStatsC)],
+    "st_solver_reset_fault_stats": [_vp],
+    "st_solver_set_fault_param": [_vp, C.c_int, C.c_double],
+    "st_solver_fault_param": [_vp, C.c_int, _d],
+    "st_solver_configure_rtm": [_vp, C.POINTER(RtmConfigC)],
+    "st_solver_rtm_engine": [_vp, C.POINTER(_vp)],
+    "st_solver_rtm_slice_stream": [_vp, C.POINTER(_vp)],
+    "st_solver_rtm_snapshot_counts": [_vp, _i64, _i64],
+    "st_solver_store_forward_wavefield_for_rtm": [_vp, C.c_int],
+    "st_solver_apply_rtm_step": [_vp, C.c_int, C.c_int],
+    "st_solver_run_rtm": [_vp, _d, C.c_int64, _d, C.c_int64, C.POINTER(PropagationResultC)],
+    "st_solver_apply_sponge_layer": [_vp],
     "st_solver_device_field": [_vp, C.c_int, C.POINTER(_vp)],
     "st_solver_set_step_fusion": [_vp, C.c_int],
     "st_solver_stream": [_vp, C.POINTER(_vp)],

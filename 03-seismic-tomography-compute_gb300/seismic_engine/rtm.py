@@ -36,7 +36,13 @@ class SliceSpec:
 
 @dataclass
 class RTMConfig:
-    """seismic::RTMConfig (wave_equation.h:39-48)."""
+    """seismic::RTMConfig (wave_equation.h:39-48), plus the inputs of the true
+    RTM that WaveEquationSolver.run_rtm performs here (no reference
+    counterpart): `receivers` (a workloads.ReceiverGrid or an object with x0,
+    sx, nx, y0, sy, ny, z; None = every interior cell of the plane z = 0),
+    `snap_kind` (forward snapshot storage, ST_SNAP_*; 0 = BF16 with a
+    per-snapshot scale) and `checkpoint_segment` (binomial checkpointing with
+    segments of that many steps; 0 = store every step)."""
     enable_rtm: bool = False
     enable_snapshots: bool = False
     snapshot_interval: int = 50
@@ -45,6 +51,9 @@ class RTMConfig:
     mmap_max_bytes: int = 2 * 1024 * 1024 * 1024
     ring_buffer_capacity: int = 1024
     slice_specs: list = field(default_factory=list)
+    receivers: object = None
+    snap_kind: int = 0
+    checkpoint_segment: int = 0
 
 
 @dataclass
@@ -64,10 +73,23 @@ class RTMEngine:
         self._h = h
         self._n = (nx, ny, nz)
         self._specs = []
+        self._owner = None
+
+    @classmethod
+    def _borrow(cls, handle, n, owner):
+        """The engine a solver owns (WaveEquationSolver.rtm_engine()); it
+        stays valid while `owner` keeps its RTM configuration."""
+        e = cls.__new__(cls)
+        e._h = handle
+        e._n = n
+        e._specs = []
+        e._owner = owner
+        return e
 
     def close(self):
         if getattr(self, "_h", None):
-            _lib.load().st_rtm_engine_destroy(self._h)
+            if self._owner is None:
+                _lib.load().st_rtm_engine_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -251,6 +251,18 @@ class SliceStream:
         self.shape = (nx, ny, nz)
         self.specs = specs
 
+    @classmethod
+    def _borrow(cls, handle, filename, shape, specs):
+        """A view of a stream another object owns (the solver's configure_rtm);
+        close() leaves it open."""
+        ss = cls.__new__(cls)
+        ss._h = handle
+        ss._borrowed = True
+        ss.filename = filename
+        ss.shape = shape
+        ss.specs = specs
+        return ss
+
     @property
     def handle(self):
         return self._h
@@ -274,7 +286,8 @@ class SliceStream:
 
     def close(self):
         if getattr(self, "_h", None) is not None:
-            call("st_slice_stream_destroy", self._h)
+            if not getattr(self, "_borrowed", False):
+                call("st_slice_stream_destroy", self._h)
             self._h = None
 
     def __del__(self):

@@ -273,35 +273,119 @@ class WaveEquationSolver:
         call("st_solver_set_terrain", self._h, terrain.handle if terrain is not None else None,
              flags if terrain is not None else 0)
 
-    # ---- RTM slice streaming (wave_equation.cpp:510-575)
+    # ---- FaultTolerance of the solver (wave_equation.h:84-85, 94)
+    def fault_tolerance(self) -> "FaultTolerance":
+        """The solver's FaultTolerance (core/fault_tolerance.h:31-97)."""
+        return FaultTolerance(self)
+
+    # ---- RTM driver (wave_equation.h:96-110, wave_equation.cpp:508-688)
     def configure_rtm(self, cfg):
-        """WaveEquationSolver::configure_rtm: with enable_rtm and
-        enable_mmap_writer, a GPU slice stream on cfg.mmap_filename (ring of
-        cfg.mmap_max_bytes) captures cfg.slice_specs (default: the middle Z, Y
-        and X planes) every cfg.snapshot_interval steps of shot_forward and of
-        the imaging pass of rtm_shot (forward snapshot, adjoint field, image)."""
-        from .slices import SliceStream
-        self.shutdown_rtm_resources()
+        """WaveEquationSolver::configure_rtm: releases the previous RTM
+        resources; with enable_rtm or enable_snapshots, creates the solver's
+        RTMEngine and, with enable_mmap_writer, a GPU slice stream on
+        cfg.mmap_filename that captures cfg.slice_specs (default: the middle
+        Z, Y and X planes) every cfg.snapshot_interval steps of shot_forward,
+        rtm_shot and run_rtm, and at apply_rtm_step(t, True)."""
+        from .slices import _specs_c
+        specs = list(cfg.slice_specs or [])
+        arr, n = _specs_c(specs)
+        r = cfg.receivers
+        rc = _lib.ReceiverGridC(r.x0, r.sx, r.nx, r.y0, r.sy, r.ny, r.z) if r is not None \
+            else _lib.ReceiverGridC(0, 1, 0, 0, 1, 0, 0)
+        fname = cfg.mmap_filename.encode() if cfg.mmap_filename else None
+        c = _lib.RtmConfigC(int(bool(cfg.enable_rtm)), int(bool(cfg.enable_snapshots)), int(cfg.snapshot_interval),
+                            int(bool(cfg.enable_mmap_writer)), fname, int(cfg.mmap_max_bytes),
+                            int(cfg.ring_buffer_capacity), arr if n else None, n, rc, int(cfg.snap_kind),
+                            int(cfg.checkpoint_segment))
+        self._rtm_engine = None
+        self._slices = None
+        call("st_solver_configure_rtm", self._h, C.byref(c))
         self._rtm_cfg = cfg
-        if cfg.enable_rtm and cfg.enable_mmap_writer and cfg.mmap_filename:
-            ss = SliceStream(cfg.mmap_filename, self.nx, self.ny, self.nz, specs=cfg.slice_specs,
-                             max_bytes=cfg.mmap_max_bytes, capacity=cfg.ring_buffer_capacity)
-            call("st_solver_set_slice_stream", self._h, ss.handle, max(int(cfg.snapshot_interval), 1))
-            self._slices = ss
+
+    def rtm_config(self):
+        """The RTMConfig of the last configure_rtm (a default one before)."""
+        from .rtm import RTMConfig
+        return getattr(self, "_rtm_cfg", None) or RTMConfig()
+
+    def rtm_engine(self):
+        """The solver's RTMEngine (image, illumination, reflectivity of
+        run_rtm / apply_rtm_step), or None while RTM is disabled."""
+        from .rtm import RTMEngine
+        h = C.c_void_p()
+        call("st_solver_rtm_engine", self._h, C.byref(h))
+        if not h.value:
+            return None
+        eng = getattr(self, "_rtm_engine", None)
+        if eng is None or eng._h is None or eng._h.value != h.value:
+            eng = RTMEngine._borrow(h, (self.nx, self.ny, self.nz), self)
+            eng.set_slice_specs(self.rtm_config().slice_specs)
+            self._rtm_engine = eng
+        return eng
 
     def slice_stream(self):
-        """The attached SliceStream (the reference's snapshot_buffer() /
-        mmap_writer() pair), or None."""
-        return getattr(self, "_slices", None)
+        """The slice stream configure_rtm created (the reference's
+        snapshot_buffer() / mmap_writer() pair), or None."""
+        from .slices import SliceStream, default_slice_specs
+        h = C.c_void_p()
+        call("st_solver_rtm_slice_stream", self._h, C.byref(h))
+        if not h.value:
+            return None
+        ss = getattr(self, "_slices", None)
+        if ss is None or ss.handle is None or ss.handle.value != h.value:
+            cfg = self.rtm_config()
+            ss = SliceStream._borrow(h, cfg.mmap_filename, (self.nx, self.ny, self.nz),
+                                     list(cfg.slice_specs) or default_slice_specs())
+            self._slices = ss
+        return ss
+
+    snapshot_buffer = slice_stream
+    mmap_writer = slice_stream
+
+    def snapshots_captured(self) -> int:
+        c = C.c_int64()
+        call("st_solver_rtm_snapshot_counts", self._h, C.byref(c), None)
+        return c.value
+
+    def snapshots_dropped(self) -> int:
+        d = C.c_int64()
+        call("st_solver_rtm_snapshot_counts", self._h, None, C.byref(d))
+        return d.value
+
+    def store_forward_wavefield_for_rtm(self, timestep: int):
+        call("st_solver_store_forward_wavefield_for_rtm", self._h, int(timestep))
+
+    def apply_rtm_step(self, timestep: int, with_snapshot: bool):
+        call("st_solver_apply_rtm_step", self._h, int(timestep), int(bool(with_snapshot)))
+
+    def run_rtm(self, source_wavelet, receiver_residuals) -> PropagationResult:
+        """WaveEquationSolver::run_rtm as true reverse-time migration: the
+        source wavelet at the domain centre, receiver_residuals FP64
+        [nt][nrec] (time-major; the receivers of rtm_config().receivers, by
+        default every interior cell of the plane z = 0). Afterwards
+        rtm_engine().result() holds the image. Without enable_rtm /
+        enable_snapshots it does nothing and reports success, as the
+        reference."""
+        w = np.ascontiguousarray(source_wavelet, dtype=np.float64).reshape(-1)
+        r = np.ascontiguousarray(receiver_residuals, dtype=np.float64).reshape(-1)
+        nul = C.cast(None, C.POINTER(C.c_double))
+        res = _lib.PropagationResultC()
+        call("st_solver_run_rtm", self._h, _dptr(w) if w.size else nul, w.size, _dptr(r) if r.size else nul,
+             r.size, C.byref(res))
+        return PropagationResult(StepResult(res.status), res.total_nan_encountered, res.total_cells_repaired,
+                                 res.timesteps_completed, bool(res.completed_successfully))
+
+    def apply_sponge_layer(self):
+        """WaveEquationSolver::apply_sponge_layer: current and previous times
+        the sponge factor over the sponge band."""
+        call("st_solver_apply_sponge_layer", self._h)
 
     def shutdown_rtm_resources(self):
-        """Detaches and closes the slice stream (wave_equation.cpp:562-575),
-        after every captured frame is in the file."""
-        ss = getattr(self, "_slices", None)
-        if ss is not None:
-            call("st_solver_set_slice_stream", self._h, None, 0)
-            ss.close()
+        """Releases the RTM resources (wave_equation.cpp:562-575); the slice
+        stream's file holds every captured frame afterwards."""
+        if getattr(self, "_h", None):
+            self._rtm_engine = None
             self._slices = None
+            call("st_solver_configure_rtm", self._h, None)
 
     # ---- GB300 additions
     def set_step_fusion(self, steps: int):
@@ -318,6 +402,82 @@ class WaveEquationSolver:
         p = C.c_void_p()
         call("st_solver_stream", self._h, C.byref(p))
         return p.value or 0
+
+
+class FaultTolerance:
+    """seismic::FaultTolerance (core/fault_tolerance.h:31-97) of a solver:
+    its statistics and settings live in the solver handle; the field helpers
+    run on the GPU in FP64. One rank: the global checks are the local ones."""
+
+    def __init__(self, solver: WaveEquationSolver):
+        self._s = solver
+
+    def stats(self) -> FaultStats:
+        return self._s.fault_stats()
+
+    def reset_stats(self):
+        call("st_solver_reset_fault_stats", self._s.handle)
+
+    def _get(self, which):
+        v = C.c_double()
+        call("st_solver_fault_param", self._s.handle, which, C.byref(v))
+        return v.value
+
+    def set_max_repair_attempts(self, n: int):
+        call("st_solver_set_fault_param", self._s.handle, _lib.ST_FT_MAX_REPAIR_ATTEMPTS, float(n))
+
+    def max_repair_attempts(self) -> int:
+        return int(self._get(_lib.ST_FT_MAX_REPAIR_ATTEMPTS))
+
+    def set_amplitude_limit(self, limit: float):
+        call("st_solver_set_fault_param", self._s.handle, _lib.ST_FT_AMPLITUDE_LIMIT, float(limit))
+
+    def amplitude_limit(self) -> float:
+        return self._get(_lib.ST_FT_AMPLITUDE_LIMIT)
+
+    def set_cfl_safety_factor(self, factor: float):
+        call("st_solver_set_fault_param", self._s.handle, _lib.ST_FT_CFL_SAFETY_FACTOR, float(factor))
+
+    def cfl_safety_factor(self) -> float:
+        return self._get(_lib.ST_FT_CFL_SAFETY_FACTOR)
+
+    def verify_cfl_condition(self, velocity, count, dx, dy, dz, dt, cfl_limit=0.5) -> bool:
+        """fault_tolerance.cpp:49-70: max finite velocity * dt / d <= cfl_limit on every axis."""
+        v = np.asarray(velocity, np.float64).reshape(-1)[:int(count)]
+        v = v[np.isfinite(v)]
+        vmax = max(0.0, float(v.max())) if v.size else 0.0
+        return max(vmax * dt / dx, vmax * dt / dy, vmax * dt / dz) <= cfl_limit
+
+    def global_health_check(self, local_status) -> int:
+        return int(local_status)
+
+    def global_health_check_field(self, data, count=None) -> int:
+        from .fields import check_field_health
+        a = np.asarray(data, np.float64).reshape(-1)
+        return 1 if check_field_health(a if count is None else a[:int(count)]) > 0 else 0
+
+    @staticmethod
+    def count_nan_inf(data, count=None) -> int:
+        from .fields import check_field_health
+        a = np.asarray(data, np.float64).reshape(-1)
+        return check_field_health(a if count is None else a[:int(count)])
+
+    @staticmethod
+    def is_valid_double(v) -> bool:
+        return bool(np.isfinite(v))
+
+    @staticmethod
+    def safe_clamp(v, lo, hi) -> float:
+        return 0.0 if not np.isfinite(v) else float(max(lo, min(v, hi)))
+
+    @staticmethod
+    def clamp_field(data, lo, hi):
+        from .fields import clamp_field_safe
+        return clamp_field_safe(data, lo, hi)
+
+    def repair_field_nan(self, data, nx, ny, nz, halo_width=1, replace_value=0.0):
+        from .fields import repair_field_nan
+        return repair_field_nan(data, nx, ny, nz, halo_width, replace_value)
 
 
 def _shot_c(src, wavelet: np.ndarray, nt: int, rec):

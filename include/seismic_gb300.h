@@ -167,6 +167,15 @@ int st_solver_snapshot_values(st_solver* s, int64_t* count);
 int st_solver_get_snapshots(st_solver* s, double* out, int64_t count);
 /* Replaces fault_stats (wave_equation.h:94). */
 int st_solver_fault_stats(st_solver* s, st_fault_stats* out);
+/* The solver's FaultTolerance (fault_tolerance(), wave_equation.h:84-85):
+ * reset_stats (core/fault_tolerance.cpp:183-186) and its settings with the
+ * reference's clamps (:188-198): max_repair_attempts >= 1, amplitude_limit
+ * >= 1 (the repair clamp only; the solver's set_amplitude_limit sets both,
+ * wave_equation.cpp:453-456), cfl_safety_factor in [0.01, 0.99]. */
+enum st_fault_param { ST_FT_MAX_REPAIR_ATTEMPTS = 0, ST_FT_AMPLITUDE_LIMIT = 1, ST_FT_CFL_SAFETY_FACTOR = 2 };
+int st_solver_reset_fault_stats(st_solver* s);
+int st_solver_set_fault_param(st_solver* s, int which, double value);
+int st_solver_fault_param(st_solver* s, int which, double* out);
 
 /* ----------------------------------------------------- GB300 shot entry points */
 /* Device pointers to the solver's fields in the device layout (for zero-copy
@@ -387,6 +396,75 @@ int st_slice_stream_destroy(st_slice_stream* ss);
  * imaging pass of st_rtm_shot captures (the stored forward snapshot V_t,
  * the adjoint field, the image so far). ss = NULL or interval <= 0 detaches. */
 int st_solver_set_slice_stream(st_solver* s, st_slice_stream* ss, int interval);
+
+/* ------------------------------------------------ RTM driver of the solver */
+/* RTMConfig (solver/wave_equation.h:39-48) plus the inputs of the true RTM
+ * that run_rtm performs here. A zeroed struct is valid: every GB300 field
+ * has its default at 0. */
+typedef struct st_rtm_config {
+    int enable_rtm;
+    int enable_snapshots;
+    int snapshot_interval;         /* slice capture every N steps (<= 0: 50) */
+    int enable_mmap_writer;
+    const char* mmap_filename;     /* NULL or "" disables the writer */
+    int64_t mmap_max_bytes;        /* <= 0: 2 GiB */
+    int64_t ring_buffer_capacity;  /* <= 0: 1024 */
+    const st_slice_spec* slice_specs; /* NULL / 0: the middle Z, Y and X planes */
+    int n_slice_specs;
+    /* GB300 additions for run_rtm: receivers of the residual traces
+     * (nx*ny == 0: every interior cell of the plane z = 0), the forward
+     * snapshot storage (ST_SNAP_NONE = BF16 with a per-snapshot scale) and
+     * binomial checkpointing (segment length in steps; 0 = store every step). */
+    st_receiver_grid receivers;
+    int snap_kind;
+    int checkpoint_segment;
+} st_rtm_config;
+/* Replaces configure_rtm / init_rtm_resources / shutdown_rtm_resources
+ * (wave_equation.cpp:508-575): drops the previous RTM resources, then, when
+ * enable_rtm or enable_snapshots is set, creates the solver's RTMEngine
+ * (FP64 image accumulators on the device) and, with enable_mmap_writer and a
+ * file name, a slice stream on that file attached to the solver (the ring
+ * buffer and mmap writer pair). cfg = NULL disables RTM. */
+int st_solver_configure_rtm(st_solver* s, const st_rtm_config* cfg);
+/* rtm_engine() (wave_equation.h:99): the solver's engine (borrowed; valid
+ * until the next configure_rtm or destroy), NULL while RTM is disabled. */
+int st_solver_rtm_engine(st_solver* s, st_rtm_engine** out);
+/* snapshot_buffer() / mmap_writer() (wave_equation.h:100-101): the slice
+ * stream configure_rtm created (borrowed), NULL when there is none. */
+int st_solver_rtm_slice_stream(st_solver* s, st_slice_stream** out);
+/* snapshots_captured() / snapshots_dropped() (wave_equation.h:106-107):
+ * slices handed to the ring buffer. Without a slice stream the ring is the
+ * reference's never-drained one (capacity rounded up to a power of two;
+ * once full, every other capture is dropped, snapshot_buffer.cpp:28-56). */
+int st_solver_rtm_snapshot_counts(st_solver* s, int64_t* captured, int64_t* dropped);
+/* store_forward_wavefield_for_rtm (wave_equation.cpp:577-596): copies the
+ * current field into the solver's forward-wavefield buffer (no-op while RTM
+ * is disabled). */
+int st_solver_store_forward_wavefield_for_rtm(st_solver* s, int timestep);
+/* apply_rtm_step (wave_equation.cpp:598-619): the engine's imaging condition
+ * on (the stored forward wavefield, or the current field when none was
+ * stored; the current field), and with with_snapshot the slices of (that
+ * forward field, the current field, the image) to the ring. No-op while RTM
+ * is disabled. */
+int st_solver_apply_rtm_step(st_solver* s, int timestep, int with_snapshot);
+/* run_rtm (wave_equation.cpp:621-688) as true reverse-time migration: while
+ * RTM is disabled it returns OK with completed_successfully set and does
+ * nothing, as the reference. Otherwise a forward pass of config.nt steps
+ * from zero fields with the source wavelet injected at the domain centre
+ * (nx/2, ny/2, nz/2) for t < n_src (non-finite samples skipped), the exact
+ * adjoint pass forced by receiver_residuals (FP64 [nt][nrec], time-major,
+ * receiver q = irx*ny + iry of the configured receiver grid; exactly
+ * nt*nrec values), the zero-lag imaging condition fused into it, and
+ * finalize_image: the solver's engine then holds image, illumination and
+ * reflectivity. Slices are captured every snapshot_interval steps of both
+ * passes when a slice stream exists. The reference instead correlates the
+ * forward field with itself and reads the residuals as a halo-padded field. */
+int st_solver_run_rtm(st_solver* s, const double* source_wavelet, int64_t n_src, const double* receiver_residuals,
+                      int64_t n_res, st_propagation_result* out);
+/* apply_sponge_layer (wave_equation.cpp:262-297) as a standalone call:
+ * field().current and field().previous are multiplied by the sponge factor D
+ * over the sponge band, exactly as the reference's call does. */
+int st_solver_apply_sponge_layer(st_solver* s);
 
 /* ------------------------------------------------------ FWI gradients */
 /* Sets the model from a device FP32 interior velocity (nx*ny*nz, x slowest);

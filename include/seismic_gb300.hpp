@@ -200,6 +200,156 @@ inline TomographyConfig load_config(const std::string& yaml_path) {
     return cfg;
 }
 
+// ---------------------------------------------------------------- rtm/rtm_engine.h:12-23
+enum class SliceAxis { X = 0, Y = 1, Z = 2, VOLUME = 3 };
+// index < 0 = the middle plane of that axis.
+struct SliceSpec {
+    SliceAxis axis;
+    int64_t index;
+    int64_t stride;
+};
+
+// ---------------------------------------------------------------- rtm/rtm_engine.h:25-96
+struct RTMImageCondition {
+    std::vector<double> image, illumination, reflectivity;
+};
+
+class RTMEngine {
+   public:
+    RTMEngine(int64_t nx, int64_t ny, int64_t nz, double dx, double dy, double dz, int halo_width, int device = 0)
+        : nx_(nx), ny_(ny), nz_(nz) {
+        check(st_rtm_engine_create(nx, ny, nz, dx, dy, dz, halo_width, device, &h_));
+    }
+    ~RTMEngine() {
+        if (owned_) st_rtm_engine_destroy(h_);
+    }
+    RTMEngine(const RTMEngine&) = delete;
+    RTMEngine& operator=(const RTMEngine&) = delete;
+    void apply_image_condition(const double* fwd, const double* adj, int64_t ny, int64_t nz, int64_t step) {
+        check(st_rtm_engine_apply_image_condition(h_, fwd, adj, ny, nz, step));
+    }
+    void finalize_image() { check(st_rtm_engine_finalize_image(h_)); }
+    void reset_image() { check(st_rtm_engine_reset_image(h_)); }
+    const RTMImageCondition& result() const {
+        auto& r = const_cast<RTMImageCondition&>(res_);
+        const size_t n = (size_t)total_cells();
+        r.image.resize(n);
+        r.illumination.resize(n);
+        r.reflectivity.resize(n);
+        check(st_rtm_engine_result(h_, r.image.data(), r.illumination.data(), r.reflectivity.data()));
+        return res_;
+    }
+    int64_t nx() const { return nx_; }
+    int64_t ny() const { return ny_; }
+    int64_t nz() const { return nz_; }
+    int64_t total_cells() const { return nx_ * ny_ * nz_; }
+    void set_slice_specs(const std::vector<SliceSpec>& specs) { specs_ = specs; }
+    const std::vector<SliceSpec>& slice_specs() const { return specs_; }
+
+   private:
+    friend class WaveEquationSolver;
+    // The engine a solver owns (WaveEquationSolver::rtm_engine()).
+    RTMEngine(st_rtm_engine* borrowed, int64_t nx, int64_t ny, int64_t nz)
+        : h_(borrowed), nx_(nx), ny_(ny), nz_(nz), owned_(false) {}
+    st_rtm_engine* h_ = nullptr;
+    int64_t nx_, ny_, nz_;
+    bool owned_ = true;
+    RTMImageCondition res_;
+    std::vector<SliceSpec> specs_;
+};
+
+// ---------------------------------------------------------------- core/fault_tolerance.h:13-97
+enum class HealthStatus : int {
+    HEALTHY = 0,
+    NAN_DETECTED = 1,
+    INF_DETECTED = 2,
+    CFL_VIOLATION = 3,
+    DIVERGENCE = 4,
+    COMM_FAILURE = 5
+};
+
+// One rank: the global checks are the local ones. The object a solver's
+// fault_tolerance() returns reads and sets the statistics and settings the
+// solver's steps use; a standalone object keeps its own settings. The field
+// helpers run on the GPU in FP64 on host arrays.
+class FaultTolerance {
+   public:
+    struct FaultStats {
+        int64_t total_nan_count;
+        int64_t total_inf_count;
+        int64_t cells_repaired;
+        int64_t timesteps_recovered;
+        int global_abort_count;
+    };
+    explicit FaultTolerance(int comm = 0, int rank = 0, int size = 1) { (void)comm, (void)rank, (void)size; }
+
+    int global_health_check(HealthStatus local_status) const { return static_cast<int>(local_status); }
+    int global_health_check_field(const double* data, int64_t count) const {
+        return count_nan_inf(data, count) > 0 ? 1 : 0;
+    }
+    int broadcast_error(int local_error) const { return local_error; }
+    // fault_tolerance.cpp:49-70
+    bool verify_cfl_condition(const double* velocity, int64_t count, double dx, double dy, double dz, double dt,
+                              double cfl_limit = 0.5) const {
+        double vmax = 0.0;
+        for (int64_t i = 0; i < count; ++i)
+            if (std::isfinite(velocity[i]) && velocity[i] > vmax) vmax = velocity[i];
+        return std::max({vmax * dt / dx, vmax * dt / dy, vmax * dt / dz}) <= cfl_limit;
+    }
+    static int64_t count_nan_inf(const double* data, int64_t count) {
+        int64_t n = 0;
+        check(st_field_count_nonfinite(data, count, 0, &n));
+        return n;
+    }
+    static bool is_valid_double(double v) { return std::isfinite(v); }
+    static double safe_clamp(double v, double lo, double hi) {
+        return std::isfinite(v) ? std::max(lo, std::min(v, hi)) : 0.0;
+    }
+    static void clamp_field(double* data, int64_t count, double lo, double hi) {
+        check(st_field_clamp(data, count, lo, hi, 0));
+    }
+    void repair_field_nan(double* data, int64_t count, int64_t nx, int64_t ny, int64_t nz, int halo_width,
+                          double replace_value = 0.0) const {
+        check(st_field_repair_nan(data, count, nx, ny, nz, halo_width, replace_value, 0));
+    }
+    const FaultStats& stats() const {
+        if (h_) {
+            st_fault_stats st{};
+            check(st_solver_fault_stats(h_, &st));
+            stats_ = FaultStats{st.total_nan_count, st.total_inf_count, st.cells_repaired, st.timesteps_recovered,
+                                st.global_abort_count};
+        }
+        return stats_;
+    }
+    void reset_stats() {
+        stats_ = FaultStats{};
+        if (h_) check(st_solver_reset_fault_stats(h_));
+    }
+    void set_max_repair_attempts(int n) { set(ST_FT_MAX_REPAIR_ATTEMPTS, n, max_repair_, 1.0, 1e9); }
+    int max_repair_attempts() const { return (int)get(ST_FT_MAX_REPAIR_ATTEMPTS, max_repair_); }
+    void set_amplitude_limit(double v) { set(ST_FT_AMPLITUDE_LIMIT, v, amp_, 1.0, HUGE_VAL); }
+    double amplitude_limit() const { return get(ST_FT_AMPLITUDE_LIMIT, amp_); }
+    void set_cfl_safety_factor(double v) { set(ST_FT_CFL_SAFETY_FACTOR, v, cfl_, 0.01, 0.99); }
+    double cfl_safety_factor() const { return get(ST_FT_CFL_SAFETY_FACTOR, cfl_); }
+
+   private:
+    friend class WaveEquationSolver;
+    void set(int which, double v, double& local, double lo, double hi) {
+        if (h_) check(st_solver_set_fault_param(h_, which, v));
+        else local = (int)which == ST_FT_MAX_REPAIR_ATTEMPTS ? std::floor(std::max(lo, std::min(v, hi)))
+                                                             : std::max(lo, std::min(v, hi));
+    }
+    double get(int which, double local) const {
+        if (!h_) return local;
+        double v = 0.0;
+        check(st_solver_fault_param(h_, which, &v));
+        return v;
+    }
+    st_solver* h_ = nullptr;
+    double max_repair_ = 3, amp_ = 1e10, cfl_ = 0.49;
+    mutable FaultStats stats_{};
+};
+
 // ---------------------------------------------------------------- solver/wave_equation.h:16-144
 struct WaveField {
     std::vector<double> current, previous, next, velocity, snapshots;
@@ -215,6 +365,25 @@ struct PropagationResult {
     bool completed_successfully;
 };
 
+// RTMConfig (wave_equation.h:39-48), plus the inputs of the true RTM that
+// run_rtm performs here (no reference counterpart): receivers of the residual
+// traces (nx*ny == 0: every interior cell of the plane z = 0), the forward
+// snapshot storage (ST_SNAP_NONE = BF16 with a per-snapshot scale) and
+// binomial checkpointing (segment length in steps; 0 = store every step).
+struct RTMConfig {
+    bool enable_rtm = false;
+    bool enable_snapshots = false;
+    int snapshot_interval = 50;
+    bool enable_mmap_writer = false;
+    std::string mmap_filename = "rtm_snapshots.dat";
+    int64_t mmap_max_bytes = 2LL * 1024LL * 1024LL * 1024LL;
+    size_t ring_buffer_capacity = 1024;
+    std::vector<SliceSpec> slice_specs;
+    st_receiver_grid receivers{0, 1, 0, 0, 1, 0, 0};
+    int snap_kind = ST_SNAP_NONE;
+    int checkpoint_segment = 0;
+};
+
 class WaveEquationSolver {
    public:
     WaveEquationSolver(const MpiContext& mpi, const CartesianGrid& grid, const SolverConfig& config, int device = 0)
@@ -225,8 +394,12 @@ class WaveEquationSolver {
         st_solver_config sc{config.frequency, config.dt, config.nt, config.water_depth, config.seafloor_gradient,
                             config.sponge_width, config.sponge_damping, config.snapshot_interval};
         check(st_solver_create(&gp, &sc, device, &h_));
+        ft_.h_ = h_;
     }
-    ~WaveEquationSolver() { st_solver_destroy(h_); }
+    ~WaveEquationSolver() {
+        engine_.reset();
+        st_solver_destroy(h_);
+    }
     WaveEquationSolver(const WaveEquationSolver&) = delete;
     WaveEquationSolver& operator=(const WaveEquationSolver&) = delete;
 
@@ -245,6 +418,11 @@ class WaveEquationSolver {
         return prop(st_solver_adjoint_propagate, r);
     }
     void exchange_halo(WaveField&) {}  // one domain: the halo ring stays zero
+    // current and previous times the sponge factor over the sponge band (wave_equation.cpp:262-297)
+    void apply_sponge_layer() {
+        sync();
+        check(st_solver_apply_sponge_layer(h_));
+    }
     const WaveField& field() const {
         const_cast<WaveEquationSolver*>(this)->download();
         return field_;
@@ -280,6 +458,79 @@ class WaveEquationSolver {
         int64_t n = 0;
         check(st_solver_nan_count_current(h_, &n));
         return n;
+    }
+    FaultTolerance& fault_tolerance() { return ft_; }
+    const FaultTolerance& fault_tolerance() const { return ft_; }
+    const FaultTolerance::FaultStats& fault_stats() const { return ft_.stats(); }
+
+    // ---- RTM driver (wave_equation.h:96-110, wave_equation.cpp:508-688)
+    void configure_rtm(const RTMConfig& cfg) {
+        sync();
+        std::vector<st_slice_spec> specs;
+        for (const auto& sp : cfg.slice_specs) specs.push_back({(int32_t)sp.axis, sp.index, sp.stride});
+        st_rtm_config c{};
+        c.enable_rtm = cfg.enable_rtm;
+        c.enable_snapshots = cfg.enable_snapshots;
+        c.snapshot_interval = cfg.snapshot_interval;
+        c.enable_mmap_writer = cfg.enable_mmap_writer;
+        c.mmap_filename = cfg.mmap_filename.c_str();
+        c.mmap_max_bytes = cfg.mmap_max_bytes;
+        c.ring_buffer_capacity = (int64_t)cfg.ring_buffer_capacity;
+        c.slice_specs = specs.empty() ? nullptr : specs.data();
+        c.n_slice_specs = (int)specs.size();
+        c.receivers = cfg.receivers;
+        c.snap_kind = cfg.snap_kind;
+        c.checkpoint_segment = cfg.checkpoint_segment;
+        engine_.reset();
+        check(st_solver_configure_rtm(h_, &c));
+        rtm_cfg_ = cfg;
+        st_rtm_engine* e = nullptr;
+        check(st_solver_rtm_engine(h_, &e));
+        if (e) {
+            const LocalGrid& l = grid_.local();
+            engine_.reset(new RTMEngine(e, l.nx_local, l.ny_local, l.nz_local));
+            engine_->set_slice_specs(cfg.slice_specs);
+        }
+    }
+    const RTMConfig& rtm_config() const { return rtm_cfg_; }
+    // nullptr while RTM is disabled; owned by the solver
+    RTMEngine* rtm_engine() { return engine_.get(); }
+    // The GPU slice stream plays both the ring buffer and the mmap writer
+    // (nullptr without enable_mmap_writer); use st_slice_stream_* on it.
+    st_slice_stream* snapshot_buffer() {
+        st_slice_stream* p = nullptr;
+        check(st_solver_rtm_slice_stream(h_, &p));
+        return p;
+    }
+    st_slice_stream* mmap_writer() { return snapshot_buffer(); }
+    // True RTM: source at the domain centre; receiver_residuals [nt][nrec]
+    // time-major on rtm_config().receivers. rtm_engine()->result() holds the
+    // image afterwards.
+    PropagationResult run_rtm(const std::vector<double>& source_wavelet, const std::vector<double>& receiver_residuals) {
+        sync();
+        st_propagation_result r{};
+        check(st_solver_run_rtm(h_, source_wavelet.data(), (int64_t)source_wavelet.size(), receiver_residuals.data(),
+                                (int64_t)receiver_residuals.size(), &r));
+        return PropagationResult{StepResult(r.status), r.total_nan_encountered, r.total_cells_repaired,
+                                 r.timesteps_completed, r.completed_successfully != 0};
+    }
+    int64_t snapshots_captured() const {
+        int64_t c = 0;
+        check(st_solver_rtm_snapshot_counts(h_, &c, nullptr));
+        return c;
+    }
+    int64_t snapshots_dropped() const {
+        int64_t d = 0;
+        check(st_solver_rtm_snapshot_counts(h_, nullptr, &d));
+        return d;
+    }
+    void store_forward_wavefield_for_rtm(int timestep) {
+        sync();
+        check(st_solver_store_forward_wavefield_for_rtm(h_, timestep));
+    }
+    void apply_rtm_step(int timestep, bool with_snapshot) {
+        sync();
+        check(st_solver_apply_rtm_step(h_, timestep, with_snapshot ? 1 : 0));
     }
     st_solver* handle() { return h_; }
 
@@ -319,45 +570,9 @@ class WaveEquationSolver {
     st_solver* h_ = nullptr;
     WaveField field_;
     bool dirty_ = false;
-};
-
-// ---------------------------------------------------------------- rtm/rtm_engine.h:25-96
-struct RTMImageCondition {
-    std::vector<double> image, illumination, reflectivity;
-};
-
-class RTMEngine {
-   public:
-    RTMEngine(int64_t nx, int64_t ny, int64_t nz, double dx, double dy, double dz, int halo_width, int device = 0)
-        : nx_(nx), ny_(ny), nz_(nz) {
-        check(st_rtm_engine_create(nx, ny, nz, dx, dy, dz, halo_width, device, &h_));
-    }
-    ~RTMEngine() { st_rtm_engine_destroy(h_); }
-    RTMEngine(const RTMEngine&) = delete;
-    RTMEngine& operator=(const RTMEngine&) = delete;
-    void apply_image_condition(const double* fwd, const double* adj, int64_t ny, int64_t nz, int64_t step) {
-        check(st_rtm_engine_apply_image_condition(h_, fwd, adj, ny, nz, step));
-    }
-    void finalize_image() { check(st_rtm_engine_finalize_image(h_)); }
-    void reset_image() { check(st_rtm_engine_reset_image(h_)); }
-    const RTMImageCondition& result() const {
-        auto& r = const_cast<RTMImageCondition&>(res_);
-        const size_t n = (size_t)total_cells();
-        r.image.resize(n);
-        r.illumination.resize(n);
-        r.reflectivity.resize(n);
-        check(st_rtm_engine_result(h_, r.image.data(), r.illumination.data(), r.reflectivity.data()));
-        return res_;
-    }
-    int64_t nx() const { return nx_; }
-    int64_t ny() const { return ny_; }
-    int64_t nz() const { return nz_; }
-    int64_t total_cells() const { return nx_ * ny_ * nz_; }
-
-   private:
-    st_rtm_engine* h_ = nullptr;
-    int64_t nx_, ny_, nz_;
-    RTMImageCondition res_;
+    FaultTolerance ft_;
+    RTMConfig rtm_cfg_;
+    std::unique_ptr<RTMEngine> engine_;
 };
 
 // ---------------------------------------------------------------- solver/boundary.h:9-52

@@ -396,6 +396,12 @@ class Reference:
         L.ref_dot.argtypes = [_d, _d, C.c_int64]
         L.ref_dot.restype = C.c_double
         L.ref_smooth_gradient.argtypes = [_d, C.c_int64, C.c_int64, C.c_int64, C.c_double, _d]
+        L.ref_adjoint_propagate.argtypes = ([C.c_int64] * 3 + [C.c_double] * 4 + [C.c_int, C.c_int, C.c_double, _d, _d,
+                                                                                   C.c_int64, _d, C.c_int64, _d, _d,
+                                                                                   _i64])
+        L.ref_rtm_building_blocks.argtypes = ([C.c_int64] * 3 + [C.c_double] * 4 + [C.c_int, C.c_double, _d, _d,
+                                                                                     C.c_int, _i32, C.c_int64, _d, _d,
+                                                                                     _d, _d, _d, _i64])
 
     def extract_slices(self, nx, ny, nz, specs, fwd, adj, ic, timestep=0):
         """RTMEngine::extract_slices with a collecting callback: a list of
@@ -555,6 +561,36 @@ class Reference:
         out = np.zeros(nx * ny * nz)
         self.lib.ref_smooth_gradient(_p(g, _d), nx, ny, nz, float(sigma), _p(out, _d))
         return out
+
+    def adjoint_propagate(self, nx, ny, nz, dx, dy, dz, dt, nt, sw, damp, vel, residual, fwd_wavelet=None):
+        """WaveEquationSolver::adjoint_propagate on a fresh solver, after
+        forward_propagate(fwd_wavelet) on it when given."""
+        v = np.ascontiguousarray(vel, np.float64)
+        r = np.ascontiguousarray(residual, np.float64)
+        fw = np.ascontiguousarray(fwd_wavelet if fwd_wavelet is not None else np.zeros(1), np.float64)
+        nfw = 0 if fwd_wavelet is None else fw.size
+        n = (nx + 2) * (ny + 2) * (nz + 2)
+        cur, prev, res = np.zeros(n), np.zeros(n), np.zeros(5, np.int64)
+        self.lib.ref_adjoint_propagate(nx, ny, nz, dx, dy, dz, dt, nt, sw, damp, _p(v, _d), _p(fw, _d), nfw,
+                                       _p(r, _d), r.size, _p(cur, _d), _p(prev, _d), _p(res, _i64))
+        return dict(cur=cur, prev=prev, status=int(res[0]), nan=int(res[1]), repaired=int(res[2]),
+                    steps=int(res[3]), ok=bool(res[4]))
+
+    def rtm_building_blocks(self, nx, ny, nz, dx, dy, dz, dt, sw, damp, vel, wavelet, ops, ring_capacity):
+        """configure_rtm + inject / step_forward / store_forward_wavefield_for_rtm /
+        apply_rtm_step / apply_sponge_layer as ops[t] says (bits 1, 2, 4, 8)."""
+        v = np.ascontiguousarray(vel, np.float64)
+        w = np.ascontiguousarray(wavelet, np.float64)
+        o = np.ascontiguousarray(ops, np.int32)
+        n = (nx + 2) * (ny + 2) * (nz + 2)
+        m = nx * ny * nz
+        img, ill, refl, cur, prev = np.zeros(m), np.zeros(m), np.zeros(m), np.zeros(n), np.zeros(n)
+        counts = np.zeros(2, np.int64)
+        self.lib.ref_rtm_building_blocks(nx, ny, nz, dx, dy, dz, dt, sw, damp, _p(v, _d), _p(w, _d), o.size,
+                                         _p(o, _i32), int(ring_capacity), _p(img, _d), _p(ill, _d), _p(refl, _d),
+                                         _p(cur, _d), _p(prev, _d), _p(counts, _i64))
+        return dict(image=img, illum=ill, refl=refl, cur=cur, prev=prev, captured=int(counts[0]),
+                    dropped=int(counts[1]))
 
     def repair_field_nan(self, data, nx, ny, nz, hw=1, repl=0.0):
         d = np.array(data, np.float64, copy=True)

@@ -396,3 +396,77 @@ int ref_smooth_gradient(const double* g, int64_t nx, int64_t ny, int64_t nz, dou
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- solver RTM driver, sponge, adjoint_propagate
+extern "C" {
+
+// The reference's adjoint_propagate (wave_equation.cpp:154-194) on a fresh
+// solver, after forward_propagate(fwd_wavelet) on the same solver when
+// n_fwd > 0 (adjoint_propagate does not reset the fields). result[0..4] =
+// status, total_nan_encountered, total_cells_repaired, timesteps_completed,
+// completed_successfully.
+int ref_adjoint_propagate(int64_t nx, int64_t ny, int64_t nz, double dx, double dy, double dz, double dt, int nt,
+                          int sponge_width, double sponge_damping, const double* vel_padded, const double* fwd_wavelet,
+                          int64_t n_fwd, const double* residual, int64_t n_res, double* out_current,
+                          double* out_previous, int64_t* result) {
+    auto& w = world();
+    int coords[3] = {0, 0, 0};
+    int dims[3] = {1, 1, 1};
+    seismic::CartesianGrid grid(make_params(nx, ny, nz, dx, dy, dz), coords, dims);
+    seismic::WaveEquationSolver solver(*w.mpi, grid, make_config(dt, nt, sponge_width, sponge_damping, 100000));
+    const int64_t n = grid.local().total_cells_with_halo;
+    solver.set_velocity_field(vel_padded, n);
+    if (n_fwd > 0) solver.forward_propagate(std::vector<double>(fwd_wavelet, fwd_wavelet + n_fwd));
+    seismic::PropagationResult pr = solver.adjoint_propagate(std::vector<double>(residual, residual + n_res));
+    result[0] = static_cast<int64_t>(pr.status);
+    result[1] = pr.total_nan_encountered;
+    result[2] = pr.total_cells_repaired;
+    result[3] = pr.timesteps_completed;
+    result[4] = pr.completed_successfully ? 1 : 0;
+    std::memcpy(out_current, solver.field().current.data(), n * sizeof(double));
+    std::memcpy(out_previous, solver.field().previous.data(), n * sizeof(double));
+    return 0;
+}
+
+// The RTM building blocks of the solver (wave_equation.cpp:508-619) and a
+// standalone apply_sponge_layer (:262-297). configure_rtm(enable_rtm, default
+// slice specs, ring_capacity); then for t < nsteps: inject_source(centre,
+// {w[t]}); step_forward(t); when ops[t] & 1 store_forward_wavefield_for_rtm(t);
+// when ops[t] & 2 apply_rtm_step(t, ops[t] & 4); when ops[t] & 8
+// apply_sponge_layer(). Afterwards finalize_image(): image / illum / refl
+// (interior), the fields, counts[0..1] = snapshots_captured / dropped.
+int ref_rtm_building_blocks(int64_t nx, int64_t ny, int64_t nz, double dx, double dy, double dz, double dt,
+                            int sponge_width, double sponge_damping, const double* vel_padded, const double* w,
+                            int nsteps, const int* ops, int64_t ring_capacity, double* image, double* illum,
+                            double* refl, double* out_current, double* out_previous, int64_t* counts) {
+    auto& wd = world();
+    int coords[3] = {0, 0, 0};
+    int dims[3] = {1, 1, 1};
+    seismic::CartesianGrid grid(make_params(nx, ny, nz, dx, dy, dz), coords, dims);
+    seismic::WaveEquationSolver solver(*wd.mpi, grid, make_config(dt, nsteps, sponge_width, sponge_damping, 100000));
+    const int64_t n = grid.local().total_cells_with_halo;
+    solver.set_velocity_field(vel_padded, n);
+    seismic::RTMConfig rc;
+    rc.enable_rtm = true;
+    rc.ring_buffer_capacity = static_cast<size_t>(ring_capacity);
+    solver.configure_rtm(rc);
+    for (int t = 0; t < nsteps; ++t) {
+        solver.inject_source(nx / 2, ny / 2, nz / 2, {w[t]});
+        solver.step_forward(t);
+        if (ops[t] & 1) solver.store_forward_wavefield_for_rtm(t);
+        if (ops[t] & 2) solver.apply_rtm_step(t, (ops[t] & 4) != 0);
+        if (ops[t] & 8) solver.apply_sponge_layer();
+    }
+    solver.rtm_engine()->finalize_image();
+    const auto& r = solver.rtm_engine()->result();
+    std::memcpy(image, r.image.data(), r.image.size() * sizeof(double));
+    std::memcpy(illum, r.illumination.data(), r.illumination.size() * sizeof(double));
+    std::memcpy(refl, r.reflectivity.data(), r.reflectivity.size() * sizeof(double));
+    std::memcpy(out_current, solver.field().current.data(), n * sizeof(double));
+    std::memcpy(out_previous, solver.field().previous.data(), n * sizeof(double));
+    counts[0] = solver.snapshots_captured();
+    counts[1] = solver.snapshots_dropped();
+    return 0;
+}
+
+}  // extern "C"

@@ -75,5 +75,47 @@ int main(int argc, char** argv) {
     const bool rd = seismic::MmapSnapshotWriter::read_frame(ring, 1, back);
     std::printf("ring %d %lld %d %lld\n", ok ? 1 : 0, (long long)seismic::MmapSnapshotWriter::count_frames(ring),
                 rd ? 1 : 0, (long long)back.size());
+
+    // the RTM driver and the rest of the solver face
+    seismic::RTMConfig rc;
+    rc.enable_rtm = true;
+    rc.receivers = st_receiver_grid{0, 2, 10, 0, 2, 9, 0};
+    rc.snap_kind = ST_SNAP_FP32;
+    seismic::CartesianGrid grid2(gp, coords, dims);
+    seismic::SolverConfig sc2 = cfg.solver;
+    sc2.nt = 24;
+    seismic::WaveEquationSolver rtm_solver(mpi, grid2, sc2);
+    rtm_solver.initialize_velocity(2500.0);
+    const seismic::PropagationResult off = rtm_solver.run_rtm({1.0}, {});
+    rtm_solver.configure_rtm(rc);
+    std::vector<double> wav(24), res(24 * 90);
+    for (int t = 0; t < 24; ++t) wav[t] = std::sin(0.4 * t);
+    for (size_t k = 0; k < res.size(); ++k) res[k] = 1e-3 * std::cos(0.1 * (double)k);
+    const seismic::PropagationResult pr = rtm_solver.run_rtm(wav, res);
+    double rimg = 0.0;
+    for (double v : rtm_solver.rtm_engine()->result().image) rimg += v;
+    std::printf("run_rtm %d %d %d %.17g\n", off.completed_successfully ? 1 : 0, (int)pr.status,
+                pr.timesteps_completed, rimg);
+    rtm_solver.reset_field();
+    rtm_solver.rtm_engine()->reset_image();
+    for (int t = 0; t < 10; ++t) {
+        rtm_solver.inject_source(10, 9, 11, {wav[t]});
+        rtm_solver.step_forward(t);
+        if (t == 4) rtm_solver.store_forward_wavefield_for_rtm(t);
+        rtm_solver.apply_rtm_step(t, t % 3 == 0);
+    }
+    rtm_solver.apply_sponge_layer();
+    rtm_solver.rtm_engine()->finalize_image();
+    double bimg = 0.0;
+    for (double v : rtm_solver.rtm_engine()->result().image) bimg += v;
+    std::printf("blocks %.17g %.17g %lld %lld\n", bimg, rtm_solver.compute_energy(),
+                (long long)rtm_solver.snapshots_captured(), (long long)rtm_solver.snapshots_dropped());
+    seismic::FaultTolerance& ft = rtm_solver.fault_tolerance();
+    ft.set_cfl_safety_factor(2.0);
+    ft.reset_stats();
+    std::printf("fault %g %d %lld\n", ft.cfl_safety_factor(), ft.max_repair_attempts(),
+                (long long)rtm_solver.fault_stats().cells_repaired);
+    const seismic::PropagationResult ap = rtm_solver.adjoint_propagate({0.5, -0.25, 0.125});
+    std::printf("adjoint %d %d %.17g\n", (int)ap.status, ap.timesteps_completed, rtm_solver.compute_energy());
     return 0;
 }

@@ -74,3 +74,34 @@ def test_cpp_face_matches_python_face(tmp_path):
     # the ring file: two frames written, frame 1 read back (500 bytes)
     assert vals["ring"] == [1.0, 2.0, 1.0, 500.0]
     assert se.MmapSnapshotWriter.read_frame(ring, 0) == bytes([7]) * 300
+    # the RTM driver, sponge, fault-tolerance and adjoint_propagate methods of the C++ class
+    s2 = se.WaveEquationSolver(se.GridParams(20, 18, 22, 10.0, 10.0, 10.0),
+                               se.SolverConfig(dt=0.001, nt=24, sponge_width=4, sponge_damping=0.015))
+    s2.initialize_velocity(2500.0)
+    off = s2.run_rtm([1.0], [])
+    rec = se.workloads.ReceiverGrid(0, 2, 10, 0, 2, 9, 0)
+    s2.configure_rtm(se.RTMConfig(enable_rtm=True, receivers=rec, snap_kind=se._lib.ST_SNAP_FP32))
+    wav = np.sin(0.4 * np.arange(24))
+    res = 1e-3 * np.cos(0.1 * np.arange(24 * 90))
+    pr = s2.run_rtm(wav, res)
+    rimg = float(np.sum(s2.rtm_engine().result().image))
+    assert vals["run_rtm"][:3] == [1.0, 0.0, 24.0] and off.completed_successfully and pr.timesteps_completed == 24
+    assert vals["run_rtm"][3] == pytest.approx(rimg, rel=1e-12)
+    s2.reset_field()
+    s2.rtm_engine().reset_image()
+    for t in range(10):
+        s2.inject_source(10, 9, 11, [wav[t]])
+        s2.step_forward(t)
+        if t == 4:
+            s2.store_forward_wavefield_for_rtm(t)
+        s2.apply_rtm_step(t, t % 3 == 0)
+    s2.apply_sponge_layer()
+    s2.rtm_engine().finalize_image()
+    bimg = float(np.sum(s2.rtm_engine().result().image))
+    assert vals["blocks"][0] == pytest.approx(bimg, rel=1e-12)
+    assert vals["blocks"][1] == pytest.approx(s2.compute_energy(), rel=1e-12)
+    assert vals["blocks"][2:] == [12.0, 0.0] == [s2.snapshots_captured(), s2.snapshots_dropped()]
+    assert vals["fault"] == [0.99, 3.0, 0.0]
+    ap = s2.adjoint_propagate([0.5, -0.25, 0.125])
+    assert vals["adjoint"][:2] == [0.0, 24.0] and ap.timesteps_completed == 24
+    assert vals["adjoint"][2] == pytest.approx(s2.compute_energy(), rel=1e-12)

@@ -219,3 +219,24 @@ def test_hessian_approx_rule_matches_reference(golden_dir):
     rows = np.repeat(np.arange(40), np.diff(g["hess_rand_row_ptr"]))
     missing = [i for i in range(30) if not np.any((rows == i) & (g["hess_rand_col"] == i))]
     assert missing, "the fixture has rows without a diagonal entry"
+
+
+def test_adjoint_propagate_matches_reference(oracle, golden_dir):
+    """adjoint_propagate (wave_equation.cpp:154-194) on a fresh solver: the
+    residual injected at the centre before each step, in reverse time order,
+    for t < len and finite values only."""
+    g = load(golden_dir, "solver_api_small.npz")
+    nx, ny, nz = (int(v) for v in g["n"])
+    nt = int(g["adj_nt"])
+    grid = oracle.grid(nx, ny, nz, float(g["d"]), float(g["d"]), float(g["d"]), float(g["dt"]),
+                       int(g["sw"]), float(g["damp"]))
+    resid = g["adj_resid"]
+    w = np.zeros(nt)
+    for k in range(nt):
+        t = nt - 1 - k
+        if t < resid.size and np.isfinite(resid[t]):
+            w[k] = resid[t]
+    r = oracle.run(grid, g["vel"], nt, np.array([[nx // 2, ny // 2, nz // 2]]), w[:, None], np.zeros((0, 3)))
+    assert np.abs(r["cur"] - g["adj_cur"]).max() <= 1e-12 * np.abs(g["adj_cur"]).max()
+    assert np.abs(r["prev"] - g["adj_prev"]).max() <= 1e-12 * np.abs(g["adj_prev"]).max()
+    assert list(g["adj_result"]) == [0, 0, 0, nt, 1]
