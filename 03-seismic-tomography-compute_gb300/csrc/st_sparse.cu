@@ -159,14 +159,20 @@ __global__ void __launch_bounds__(256) spmv_kernel(const long long* __restrict__
     const int lane = threadIdx.x % G;
     const long long gid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / G;
     const long long stride = ((long long)gridDim.x * blockDim.x) / G;
+    // the warp's first group: every lane of a warp runs the same number of
+    // iterations (groups past the last row idle through them), so the
+    // full-warp shuffles below always see all 32 lanes
+    const long long gfirst = (blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31u)) / G;
     double local = 0.0;
     constexpr long long PF = 2;  // rows ahead (measured: 1 -> 1.67 ms, 2 -> 1.57, 3 -> 1.61 for A x + A^T y)
-    for (long long row = gid; row < rows; row += stride) {
-        const long long a = rp[row], b = rp[row + 1];
+    for (long long it = 0; gfirst + it * stride < rows; ++it) {
+        const long long row = gid + it * stride;
+        const bool active = row < rows;
+        const long long a = active ? rp[row] : 0, b = active ? rp[row + 1] : 0;
         // the group's row after next: pull its columns and values into L2 now, so
         // its loads wait on L2 rather than DRAM (one 128-byte line per lane);
         // short rows (small G) are left to the caches
-        if (G >= 8 && row + PF * stride < rows) {
+        if (G >= 8 && active && row + PF * stride < rows) {
             const long long na = rp[row + PF * stride], nb = rp[row + PF * stride + 1];
             const long long l0 = na >> 5, l1 = (nb + 31) >> 5;  // 32 four-byte entries per line
             for (long long l = l0 + lane; l < l1; l += G) {
@@ -192,7 +198,7 @@ __global__ void __launch_bounds__(256) spmv_kernel(const long long* __restrict__
         float sum = (s0 + s1) + (s2 + s3);
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(FULL, sum, o, G);
-        if (lane == 0) {
+        if (lane == 0 && active) {
             if (add) sum = fmaf(add_scale, add[row], sum);
             y[row] = sum;
             if (pdot) local += (double)pdot[row] * (double)sum;
