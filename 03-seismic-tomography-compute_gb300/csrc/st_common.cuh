@@ -131,6 +131,11 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity
     }
 }
 
+// Limit of the waits that drain a kernel's copies in flight after another
+// wait gave up: always the full default, whatever limit the pipeline ran with,
+// so that no copy can land in shared memory after the CTA has exited.
+constexpr uint64_t WAIT_DRAIN_NS = 2000000000ull;
+
 // 3-D tiled TMA load of one box into shared memory, completing on `bar`.
 // c0 is the innermost (z) coordinate and must be a multiple of 4 elements
 // (16 bytes) for FP32 data; the launchers guarantee it.

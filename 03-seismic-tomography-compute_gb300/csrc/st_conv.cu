@@ -233,7 +233,8 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
             }
             // drain: every issued window has landed before the CTA may exit
             for (int f = (g > NSLOT ? g - NSLOT : 0); f < g; ++f)
-                if (!mbar_wait_bounded(&cs->full[f % NSLOT], (f / NSLOT) & 1, lim)) atomicOr(a.flags, CONV_FLAG_TIMEOUT);
+                if (!mbar_wait_bounded(&cs->full[f % NSLOT], (f / NSLOT) & 1, lim > WAIT_DRAIN_NS ? lim : WAIT_DRAIN_NS))
+                    atomicOr(a.flags, CONV_FLAG_TIMEOUT);
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -294,7 +295,7 @@ __global__ void __launch_bounds__(CONV_THREADS, 1)
             // drain: the last commit tracks every MMA this thread issued
             if (committed > 0) {
                 const int last = committed - 1;
-                if (!mbar_wait_bounded(&cs->tfull[last & 1], (last >> 1) & 1, lim))
+                if (!mbar_wait_bounded(&cs->tfull[last & 1], (last >> 1) & 1, lim > WAIT_DRAIN_NS ? lim : WAIT_DRAIN_NS))
                     atomicOr(a.flags, CONV_FLAG_TIMEOUT);
             }
         }

@@ -31,7 +31,9 @@ struct StepArgs {
     float* grad;             // gradient: grad += (centre / c) * L(snapshot)   (compact interior)
     int snap_t;              // gradient: time index of the snapshot in the store
     unsigned* flags;         // FLAG_GUARD / FLAG_TIMEOUT
-    unsigned long long timeout_ns;
+    unsigned long long timeout_ns;  // limit of every bounded wait (0: the launcher's default, 2 s)
+    int withhold;            // fault-path test hook: plane withhold - 1 of every CTA's march is never
+                             // copied, so its waits run out (0: none)
     int stable_sponge;       // 1: out = D * (update + forcing) (damped new field), 0: the reference rule
     const int* zlim;         // terrain: per (x, y) column (x * ny + y), points with z < zlim are set to 0
                              // after the update (free surface / seafloor masks), or null

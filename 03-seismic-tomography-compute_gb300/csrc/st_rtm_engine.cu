@@ -228,4 +228,8 @@ int rtm_engine_load_fp32(st_rtm_engine* e, const float* image, const float* illu
 
 const double* rtm_engine_image(const st_rtm_engine* e) { return e->image; }
 
+void rtm_engine_set_stream(st_rtm_engine* e, cudaStream_t stream) {
+    if (!e->own_stream) e->stream = stream;
+}
+
 }  // namespace stg

@@ -254,6 +254,9 @@ StepArgs base_args(st_solver* s, float* out) {
     a.rsx = a.rsy = 1;
     a.stable_sponge = s->sponge_mode == ST_SPONGE_STABLE;
     a.zlim = s->zlim;
+    a.timeout_ns = s->wait_limit_ns;
+    a.withhold = s->withhold;  // the test hook applies to one launch
+    s->withhold = 0;
     return a;
 }
 
@@ -477,7 +480,8 @@ int st_solver_create(const st_grid_params* grid, const st_solver_config* cfg, in
     s->cfg = *cfg;
     s->L = make_layout(grid->nx_global, grid->ny_global, grid->nz_global);
     s->vel_host.assign((size_t)ref_elems(s.get()), 0.0);
-    ST_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    ST_CUDA(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking));
+    s->stream = s->own_stream;
     for (int k = 0; k < 3; ++k) ST_CUDA(cudaEventCreate(&s->ev[k]));
     const size_t fb = (size_t)s->L.elems * sizeof(float);
     for (int k = 0; k < 3; ++k) ST_CUDA(cudaMalloc(&s->f[k], fb));
@@ -528,7 +532,8 @@ int st_solver_destroy(st_solver* s) {
     cudaFree(s->vel_dev);
     for (int k = 0; k < 3; ++k)
         if (s->ev[k]) cudaEventDestroy(s->ev[k]);
-    if (s->stream) cudaStreamDestroy(s->stream);
+    if (s->stream != s->own_stream) cudaStreamSynchronize(s->stream);
+    if (s->own_stream) cudaStreamDestroy(s->own_stream);
     delete s;
     return ST_OK;
 }
@@ -799,6 +804,30 @@ int st_solver_get_snapshots(st_solver* s, double* out, int64_t count) {
 int st_solver_fault_stats(st_solver* s, st_fault_stats* out) {
     ST_CHECK(s && out, ST_ERR_ARG, "null argument");
     *out = s->stats;
+    return ST_OK;
+}
+
+int st_solver_set_stream(st_solver* s, void* stream) {
+    ST_CHECK(s, ST_ERR_ARG, "null solver");
+    ST_CUDA(cudaSetDevice(s->device));
+    cudaStream_t next = stream ? static_cast<cudaStream_t>(stream) : s->own_stream;
+    if (next == s->stream) return ST_OK;
+    // work queued so far stays ordered before everything issued on the new stream
+    cudaEvent_t ev = nullptr;
+    ST_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    const cudaError_t e1 = cudaEventRecord(ev, s->stream);
+    const cudaError_t e2 = e1 == cudaSuccess ? cudaStreamWaitEvent(next, ev, 0) : e1;
+    cudaEventDestroy(ev);
+    ST_CUDA(e2);
+    s->stream = next;
+    if (s->rtm_engine) rtm_engine_set_stream(s->rtm_engine, next);
+    return ST_OK;
+}
+
+int st_solver_set_wait_test(st_solver* s, unsigned long long limit_ns, int withhold_plane) {
+    ST_CHECK(s && withhold_plane >= -1, ST_ERR_ARG, "bad argument");
+    s->wait_limit_ns = limit_ns;
+    s->withhold = withhold_plane + 1;
     return ST_OK;
 }
 

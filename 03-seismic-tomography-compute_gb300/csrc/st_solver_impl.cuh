@@ -54,7 +54,8 @@ class PinnedVec {
 
 struct st_solver {
     int device = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      // where the handle's work runs (own_stream or a caller's)
+    cudaStream_t own_stream = nullptr;  // created with the handle
     stg::Layout L{};
     st_grid_params grid{};
     st_solver_config cfg{};
@@ -93,6 +94,8 @@ struct st_solver {
     void* ckpt_buf = nullptr;       // checkpointed adjoint: working set, state slots, segment snapshots
     size_t ckpt_cap = 0;
     int sponge_mode = ST_SPONGE_REFERENCE;  // ST_SPONGE_STABLE: damp the new field (Cerjan form)
+    unsigned long long wait_limit_ns = 0;   // bounded-wait limit of the stencil kernels (0: 2 s)
+    int withhold = 0;                       // st_solver_set_wait_test: plane + 1 withheld at the next launch
     int* zlim = nullptr;                // terrain: per-column z limits (st_solver_set_terrain), or null
     st_slice_stream* slices = nullptr;  // RTM slice stream (configure_rtm), borrowed
     int slice_interval = 0;             // capture every slice_interval steps
@@ -157,6 +160,7 @@ int checkpointed_adjoint(st_solver* s, const st_shot* shot, int snap_kind, int s
                          const float* force, float* image, float* illum, float* grad_c, float* seis,
                          const std::function<int()>& before_backward, st_checkpoint_stats* stats);
 // Helpers of the engine a solver's RTM driver owns (st_rtm_engine.cu).
+void rtm_engine_set_stream(st_rtm_engine* e, cudaStream_t stream);
 int rtm_engine_create_on_stream(int64_t nx, int64_t ny, int64_t nz, double dx, double dy, double dz, int device,
                                 cudaStream_t stream, st_rtm_engine** out);
 // image += fwd * adj, illum += fwd^2 (FP64) over the interior of two device-layout fields.

@@ -447,6 +447,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo<EPI, SNAP_IN>::MINB))
     auto issue = [&](int i) {
         const int s = i % STAGES;
         const int xd = xa + i;
+        if (i + 1 == a.withhold) return;  // fault-path test hook: this stage never completes
         mbar_arrive_expect_tx(&bar[s], G::STAGE_TX);
         tma_load_3d(cur_tile(s), &map_cur, &bar[s], z0, y0, xd);
         tma_load_3d(prev_tile(s), &map_prev, &bar[s], z0 + Layout::ZOFF, y0 + 1, xd);
@@ -635,7 +636,8 @@ __global__ void __launch_bounds__(NTHREADS, (Geo<EPI, SNAP_IN>::MINB))
     if (i < nplanes) {
         // A wait gave up: drain the copies still in flight (bounded), then leave.
         if (tid == 0) {
-            for (int j = i; j < issued; ++j) mbar_wait_bounded(&bar[j % STAGES], (j / STAGES) & 1, a.timeout_ns);
+            for (int j = i; j < issued; ++j)
+                if (j + 1 != a.withhold) mbar_wait_bounded(&bar[j % STAGES], (j / STAGES) & 1, WAIT_DRAIN_NS);
             atomicOr(a.flags, FLAG_TIMEOUT);
         }
         __syncthreads();
@@ -963,6 +965,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
 
     auto issue = [&](int i) {
         const int s = i % STAGES;
+        if (i + 1 == a.withhold) return;  // fault-path test hook: this stage never completes
         const int xd = xa - 1 + i;  // device x of interior plane xa - 2 + i
         const int xi = xa - 3 + i;  // interior plane of the imaging / gradient operands
         const bool acc = (ADJ || GRD) && xi >= xa && xi < xb;
@@ -1278,7 +1281,8 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     if (i < nplanes) {
         // A wait gave up: drain the copies still in flight (bounded), then leave.
         if (tid == 0) {
-            for (int j = i; j < issued; ++j) mbar_wait_bounded(&bar[j % STAGES], (j / STAGES) & 1, a.timeout_ns);
+            for (int j = i; j < issued; ++j)
+                if (j + 1 != a.withhold) mbar_wait_bounded(&bar[j % STAGES], (j / STAGES) & 1, WAIT_DRAIN_NS);
             atomicOr(a.flags, FLAG_TIMEOUT);
         }
         __syncthreads();

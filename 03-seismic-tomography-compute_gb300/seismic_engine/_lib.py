@@ -134,6 +134,7 @@ SIGNATURES = {
     "st_solver_get_snapshots": [_vp, _d, C.c_int64],
     "st_solver_fault_stats": [_vp, C.POINTER(FaultStatsC)],
     "st_solver_reset_fault_stats": [_vp],
+    "st_solver_set_wait_test": [_vp, C.c_ulonglong, C.c_int],
     "st_solver_set_fault_param": [_vp, C.c_int, C.c_double],
     "st_solver_fault_param": [_vp, C.c_int, _d],
     "st_solver_configure_rtm": [_vp, C.POINTER(RtmConfigC)],
@@ -147,6 +148,7 @@ SIGNATURES = {
     "st_solver_device_field": [_vp, C.c_int, C.POINTER(_vp)],
     "st_solver_set_step_fusion": [_vp, C.c_int],
     "st_solver_stream": [_vp, C.POINTER(_vp)],
+    "st_solver_set_stream": [_vp, _vp],
     "st_solver_last_phase_ms": [_vp, C.POINTER(C.c_float)],
     "st_launch_count": [C.POINTER(C.c_longlong)],
     "st_shot_forward": [_vp, C.POINTER(ShotC), _vp, C.c_int, _vp, _vp],

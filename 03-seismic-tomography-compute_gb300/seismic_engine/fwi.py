@@ -15,9 +15,16 @@ from .wave import WaveEquationSolver, _shot_c
 
 
 def set_velocity_device(solver: WaveEquationSolver, vel: torch.Tensor):
+    """Sets the model from a CUDA tensor. Inside solver.on_stream(torch's
+    current stream) the copy is ordered on that stream; otherwise the current
+    stream is synchronised first so the tensor is complete."""
     v = vel.detach().to(device="cuda", dtype=torch.float32).contiguous()
+    cur = torch.cuda.current_stream()
+    if solver.stream_ptr() != cur.cuda_stream:
+        cur.synchronize()
     call("st_solver_set_velocity_device", solver.handle, v.data_ptr())
-    torch.cuda.current_stream().synchronize()
+    if solver.stream_ptr() != cur.cuda_stream:
+        torch.cuda.ExternalStream(solver.stream_ptr()).synchronize()
 
 
 def _ckpt(checkpoint):
@@ -63,17 +70,19 @@ def fwi_gradient(solver, src, wavelet, nt, rec, d_obs, grad_v=None, snap_kind=_l
 class SeismicModeling(torch.autograd.Function):
     """d = F(v): seismograms [n_shots, nt, nrec] of every shot for velocity v.
     backward: the exact adjoint of the discrete forward map (fused GPU
-    kernel), forward snapshots recomputed and stored with snap_kind."""
+    kernel), forward snapshots recomputed and stored with snap_kind. Both run
+    on torch's current stream (the solver is switched to it for the call), so
+    they are ordered with the surrounding torch work without a device sync."""
 
     @staticmethod
     def forward(ctx, vel, solver, shots, nt, snap_kind, checkpoint=None):
         from .wave import shot_forward
-        set_velocity_device(solver, vel)
         nrec = shots[0].rec.count
-        out = torch.zeros((len(shots), nt, nrec), device="cuda", dtype=torch.float32)
-        for i, sh in enumerate(shots):
-            shot_forward(solver, sh.src, sh.wavelet, nt, sh.rec, seis=out[i])
-        torch.cuda.synchronize()
+        with solver.on_stream(torch.cuda.current_stream()):
+            set_velocity_device(solver, vel)
+            out = torch.zeros((len(shots), nt, nrec), device="cuda", dtype=torch.float32)
+            for i, sh in enumerate(shots):
+                shot_forward(solver, sh.src, sh.wavelet, nt, sh.rec, seis=out[i])
         ctx.save_for_backward(vel)
         ctx.solver, ctx.shots, ctx.nt, ctx.snap_kind, ctx.checkpoint = solver, shots, nt, snap_kind, checkpoint
         return out.to(vel.dtype)
@@ -82,13 +91,13 @@ class SeismicModeling(torch.autograd.Function):
     def backward(ctx, grad_out):
         (vel,) = ctx.saved_tensors
         solver = ctx.solver
-        set_velocity_device(solver, vel)
-        g = torch.zeros(vel.shape, device="cuda", dtype=torch.float32)
-        go = grad_out.to(dtype=torch.float32).contiguous()
-        for i, sh in enumerate(ctx.shots):
-            shot_gradient(solver, sh.src, sh.wavelet, ctx.nt, sh.rec, go[i].contiguous(), g, ctx.snap_kind,
-                          checkpoint=ctx.checkpoint)
-        torch.cuda.synchronize()
+        with solver.on_stream(torch.cuda.current_stream()):
+            set_velocity_device(solver, vel)
+            g = torch.zeros(vel.shape, device="cuda", dtype=torch.float32)
+            go = grad_out.to(dtype=torch.float32).contiguous()
+            for i, sh in enumerate(ctx.shots):
+                shot_gradient(solver, sh.src, sh.wavelet, ctx.nt, sh.rec, go[i].contiguous(), g, ctx.snap_kind,
+                              checkpoint=ctx.checkpoint)
         return g.to(vel.dtype), None, None, None, None, None
 
 

@@ -403,6 +403,30 @@ class WaveEquationSolver:
         call("st_solver_stream", self._h, C.byref(p))
         return p.value or 0
 
+    def set_stream(self, stream):
+        """Runs the solver's work on `stream` (a torch.cuda.Stream, a raw
+        cudaStream_t as int, or None for the solver's own stream); queued work
+        stays ordered before it."""
+        ptr = getattr(stream, "cuda_stream", stream)
+        call("st_solver_set_stream", self._h, C.c_void_p(int(ptr)) if ptr else None)
+
+    def on_stream(self, stream):
+        """Context manager: the solver's work inside runs on `stream` (default:
+        torch's current stream), so it is ordered with the surrounding torch
+        work without any device-wide synchronisation."""
+        import contextlib
+
+        @contextlib.contextmanager
+        def cm():
+            import torch
+            st = stream if stream is not None else torch.cuda.current_stream()
+            self.set_stream(st)
+            try:
+                yield st
+            finally:
+                self.set_stream(None)
+        return cm()
+
 
 class FaultTolerance:
     """seismic::FaultTolerance (core/fault_tolerance.h:31-97) of a solver:

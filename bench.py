@@ -78,6 +78,8 @@ def parse():
     ap.add_argument("--tomo-rays", type=int, default=2_000_000, help="rays of the --kernel spmv matrix")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner solve")
     ap.add_argument("--no-rays", action="store_true", help="skip the sampled-ray forward/gradient measurement")
+    ap.add_argument("--dry-run", action="store_true",
+                    help="check the multi-process plumbing only (set-up, barrier, max over ranks); no GPU work")
     return ap.parse_args()
 
 
@@ -256,6 +258,14 @@ def cpu_baseline(w, target_s):
                       f"{cores} threads)"}
 
 
+def _ref_note():
+    import platform
+    if platform.machine() in ("x86_64", "AMD64"):
+        return "the reference's own single-threaded C++ is the oracle's pin, not timed here"
+    return (f"the reference's own C++ uses x86 intrinsics (immintrin.h) and does not build on this "
+            f"{platform.machine()} host")
+
+
 def run_reference(args):
     world, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
     if rank != 0:
@@ -280,8 +290,8 @@ def run_reference(args):
         "config": config_dict(w, args.snap, world),
         "cpu_baseline": {"value": value, "unit": "Gpts/s", "cores": cores, "kind": "port",
                          "sample": f"each step: {nt_s} forward + {nt_s} adjoint/imaging steps of the "
-                                   f"{w.nx}^3 workload in FP64 (the reference's CPU step restated in C; "
-                                   f"the reference sources are not available on this machine)"},
+                                   f"{w.nx}^3 workload in FP64 (the reference's CPU step restated in C, "
+                                   f"OpenMP over {cores} threads; {_ref_note()})"},
         "e2e": {"value": value, "unit": "Gpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -779,8 +789,42 @@ def _snap(name):
     return {"bf16": _lib.ST_SNAP_BF16, "fp16": _lib.ST_SNAP_FP16, "fp32": _lib.ST_SNAP_FP32}[name]
 
 
+def launch_replicas(n, argv):
+    """`--gpus N` run outside torchrun: start N replica processes through
+    torch.distributed.run (one per GPU, LOCAL_RANK = device, rendezvous on
+    127.0.0.1); rank 0 prints the JSON line. Returns their exit status."""
+    import socket
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        port = so.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", f"--master-port={port}", os.path.abspath(__file__), *argv]
+    return subprocess.call(cmd)
+
+
+def run_dry(args):
+    """The replica plumbing of run_gpu without GPU work: each rank times a
+    token sleep; the line carries the max over ranks."""
+    world, rank, _ = dist_setup(args)
+    barrier(world)
+    t0 = time.perf_counter()
+    time.sleep(0.01 * (1 + rank))
+    el = max_over_ranks(time.perf_counter() - t0, world)
+    barrier(world)
+    if rank == 0:
+        print(json.dumps({"dry_run": True, "n_gpus": world, "max_rank_seconds": el}), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return launch_replicas(args.gpus, sys.argv[1:])
+    if args.dry_run:
+        return run_dry(args)
     if args.kernel:
         return run_kernel(args)
     if args.workload == "large":

@@ -173,6 +173,15 @@ int st_solver_fault_stats(st_solver* s, st_fault_stats* out);
  * >= 1 (the repair clamp only; the solver's set_amplitude_limit sets both,
  * wave_equation.cpp:453-456), cfl_safety_factor in [0.01, 0.99]. */
 enum st_fault_param { ST_FT_MAX_REPAIR_ATTEMPTS = 0, ST_FT_AMPLITUDE_LIMIT = 1, ST_FT_CFL_SAFETY_FACTOR = 2 };
+/* Test hook of the bounded-wait error path (no reference counterpart): every
+ * wait of the solver's stencil kernels gives up after limit_ns of GPU time (0 =
+ * the default, 2 s). With withhold_plane >= 0 the next stencil launch never
+ * copies that plane of each CTA's march, so the waits on it run out: the
+ * launch drains its other copies (always with the full 2 s limit) and exits,
+ * and the call returns ST_ERR_TIMEOUT with the handle still usable (its field
+ * values are then undefined until reset_field). The withheld plane applies to
+ * one launch; the limit stays until changed. */
+int st_solver_set_wait_test(st_solver* s, unsigned long long limit_ns, int withhold_plane);
 int st_solver_reset_fault_stats(st_solver* s);
 int st_solver_set_fault_param(st_solver* s, int which, double value);
 int st_solver_fault_param(st_solver* s, int which, double* out);
@@ -193,6 +202,12 @@ int st_solver_device_field(st_solver* s, int which, float** out);
 int st_solver_set_step_fusion(st_solver* s, int steps);
 /* The CUDA stream the handle orders its work on (a cudaStream_t). */
 int st_solver_stream(st_solver* s, void** out);
+/* Runs the handle's work on `stream` (a cudaStream_t of the handle's device,
+ * e.g. the caller's torch stream; NULL = the handle's own stream again). The
+ * work already queued on the previous stream stays ordered before anything
+ * issued afterwards; calls that return host-visible results synchronise that
+ * stream only, never the whole device. The stream must outlive its use. */
+int st_solver_set_stream(st_solver* s, void* stream);
 /* Device time of the two phases of the last st_rtm_shot on this handle, from
  * CUDA events recorded on its stream: out[0] = forward pass (fused steps with
  * snapshot store), out[1] = backward pass (fused adjoint steps with imaging). */

@@ -120,6 +120,35 @@ def test_autograd_function_matches_entry_point(se):
     assert rel(vv.grad.reshape(-1).cpu().numpy(), g.cpu().numpy()) < 1e-5
 
 
+def test_autograd_function_on_a_side_stream(se, monkeypatch):
+    """The autograd Function runs on torch's current stream: on a side stream,
+    with torch.cuda.synchronize made to fail, the seismograms and the
+    gradient equal those of the same call on the default stream bit for bit."""
+    import torch
+    w, s = case(se, n=(18, 16, 20), nt=40, seed=25)
+    shots = [w.shots[0]]
+    v = torch.from_numpy(w.vel.astype(np.float32)).cuda()
+    v0 = v.clone().requires_grad_(True)
+    d0 = se.fwi.modeling(v0, s, shots, w.nt)
+    (d0.double() ** 2).sum().backward()
+    torch.cuda.synchronize()
+
+    def no_device_sync(*a, **k):
+        raise AssertionError("device-wide synchronisation inside the autograd Function")
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        monkeypatch.setattr(torch.cuda, "synchronize", no_device_sync)
+        v1 = v.clone().requires_grad_(True)
+        d1 = se.fwi.modeling(v1, s, shots, w.nt)
+        (d1.double() ** 2).sum().backward()
+        monkeypatch.undo()
+    side.synchronize()
+    assert s.stream_ptr() != side.cuda_stream  # the solver is back on its own stream
+    assert torch.equal(d0, d1)
+    assert torch.equal(v0.grad, v1.grad)
+
+
 def test_exact_gradient_vs_reference_pointwise_formula(se):
     """The reference's adjoint-state gradient (seismic_tomography/gradient.py:
     24-40) is the pointwise g = -u * lambda * 2 v dt^2; summed over time that is

@@ -47,3 +47,19 @@ def test_two_rank_gloo_helpers():
     for rank, (p, out) in enumerate(zip(procs, outs)):
         assert p.returncode == 0, out
         assert f"ok {rank}" in out, out
+
+
+def test_gpus_flag_launches_replicas_without_torchrun():
+    """`bench.py --gpus 2` outside torchrun starts two replica processes
+    itself (torch.distributed.run on 127.0.0.1, gloo here) and rank 0 prints
+    one line with the max over both ranks."""
+    import json
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    env["CUDA_VISIBLE_DEVICES"] = ""
+    r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--gpus", "2", "--dry-run"], env=env,
+                       capture_output=True, text=True, timeout=240)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    assert d["dry_run"] and d["n_gpus"] == 2 and d["max_rank_seconds"] >= 0.02
