@@ -78,6 +78,8 @@ def parse():
     ap.add_argument("--tomo-rays", type=int, default=2_000_000, help="rays of the --kernel spmv matrix")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner solve")
     ap.add_argument("--no-rays", action="store_true", help="skip the sampled-ray forward/gradient measurement")
+    ap.add_argument("--no-512", action="store_true", help="skip the 512^3 roofline leg")
+    ap.add_argument("--no-large", action="store_true", help="skip the 512^3 adjoint tomography iteration")
     ap.add_argument("--dry-run", action="store_true",
                     help="check the multi-process plumbing only (set-up, barrier, max over ranks); no GPU work")
     return ap.parse_args()
@@ -592,8 +594,14 @@ def run_gpu(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
     s.close()
-    if rank == 0 and world == 1 and not args.no_tomo:
+    if rank == 0 and world == 1 and not args.no_512:
         del image, illum, refl, data
+        torch.cuda.empty_cache()
+        line["roofline_512"] = run_512_leg(args)
+    if rank == 0 and world == 1 and not args.no_large:
+        torch.cuda.empty_cache()
+        line["large_iteration"] = large_iteration(args)
+    if rank == 0 and world == 1 and not args.no_tomo:
         torch.cuda.empty_cache()
         line["tomography"] = run_tomography(args)
     if rank == 0 and world == 1 and not args.no_rays:
@@ -605,6 +613,70 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+def run_512_leg(args, nt=200):
+    """The propagator kernels at 512^3 (the large workload's grid and model,
+    its first shot and 256x256 receivers): a 200-step BF16 RTM shot with two
+    steps per launch and one with one step per launch; per-launch times from
+    the passes' CUDA events, algorithmic bytes as the headline roofline."""
+    import torch
+    import seismic_engine as se
+    from seismic_engine import _lib
+    import ctypes as C
+    w = se.workloads.large_512(nt=nt)
+    sh = w.shots[0]
+    n = w.nx
+    cfg = se.SolverConfig(dt=w.dt, nt=nt, sponge_width=w.sponge_width, sponge_damping=w.sponge_damping,
+                          sponge_mode=w.sponge_mode)
+    s = se.WaveEquationSolver(se.GridParams(n, n, n, w.d, w.d, w.d), cfg)
+    s.set_velocity_field(se.workloads.to_reference_layout(w.vel))
+    data = torch.randn((nt, sh.rec.count), device="cuda", generator=torch.Generator("cuda").manual_seed(5)) * 1e-3
+    npts = n ** 3
+    image, illum = torch.zeros(npts, device="cuda"), torch.zeros(npts, device="cuda")
+    L = _lib.load()
+    peak, kind = measured_peaks()
+    out = {"workload": f"{w.name} model, shot 0, {nt} steps, BF16 snapshots, {sh.rec.nx}x{sh.rec.ny} receivers",
+           "peak": peak, "peak_kind": f"{kind} copy bandwidth", "unit": "GB/s"}
+    for fused in (2, 1):
+        s.set_step_fusion(fused)
+        ph = (C.c_float * 2)()
+        fwd, bwd, tot = [], [], []
+        for i in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            st = torch.cuda.ExternalStream(s.stream_ptr())
+            e0.record(st)
+            se.rtm_shot(s, sh.src, sh.wavelet, nt, sh.rec, data, image, illum, snap_kind=_lib.ST_SNAP_BF16)
+            e1.record(st)
+            torch.cuda.synchronize()
+            L.st_solver_last_phase_ms(s.handle, ph)
+            if i > 0:
+                fwd.append(ph[0])
+                bwd.append(ph[1])
+                tot.append(e0.elapsed_time(e1))
+        launches = nt // fused
+        fb, bb = alg_bytes("bf16", fused == 2)
+        f_ms, b_ms = statistics.mean(fwd) / launches, statistics.mean(bwd) / launches
+        key = "pair" if fused == 2 else "one_step"
+        out[key] = {
+            "forward": {"launch_ms": f_ms, "alg_bytes_per_launch": fb * npts,
+                        "achieved": fb * npts / f_ms / 1e6, "frac": fb * npts / f_ms / 1e6 / peak},
+            "adjoint_imaging": {"launch_ms": b_ms, "alg_bytes_per_launch": bb * npts,
+                                "achieved": bb * npts / b_ms / 1e6, "frac": bb * npts / b_ms / 1e6 / peak},
+            "shot_gpts_per_s": 2.0 * nt * npts / (statistics.mean(tot) / 1e3) / 1e9,
+        }
+    s.close()
+    return out
+
+
+def large_iteration(args):
+    """One iteration of the large workload (512^3, 8 shots x 4000 steps,
+    checkpointed BF16 adjoint gradient, PCG update on 256^3) as in
+    `--workload large`; returns its timing dictionary."""
+    import types
+    a = types.SimpleNamespace(**vars(args))
+    a.nt, a.compare = 4000, False
+    return _large(a)
 
 
 def run_kernel(args):
@@ -719,11 +791,19 @@ def laplacian_csr(n, mu=1.0):
 
 
 def run_large(args):
+    """One adjoint tomography iteration on the 512^3 workload (see _large).
+    Prints one JSON line."""
+    line = _large(args)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _large(args):
     """One adjoint tomography iteration on the 512^3 workload: 8 shots one
     after another, each forward + checkpointed adjoint gradient (BF16 segment
     snapshots), the summed velocity gradient restricted to a 256^3 inversion
     grid (2x2x2 means) and a Jacobi-PCG model update (I + mu L^T L) x = g,
-    L the 7-point Laplacian (mu = 1). Prints one JSON line."""
+    L the 7-point Laplacian (mu = 1)."""
     import torch
     import seismic_engine as se
     import seismic_engine.fwi as fwi
@@ -779,9 +859,9 @@ def run_large(args):
     if args.compare:
         line["fp32_checkpointed"] = iteration(_snap("fp32"), True)
         line["plain_cg"] = iteration(_snap("bf16"), False)
-    print(json.dumps(line), flush=True)
     s.close()
-    return 0
+    L.close()
+    return line
 
 
 def _snap(name):

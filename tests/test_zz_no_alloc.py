@@ -61,6 +61,12 @@ def test_static_cg_matches_allocating_cg(se, jacobi):
         assert rel_sta < 1e-6
         xr, xs = x_ref.cpu().numpy(), x_sta.cpu().numpy()
         assert np.linalg.norm(xs - xr) <= 1e-5 * np.linalg.norm(xr), call
+    # and it allocates nothing: the device's free memory is the same before and
+    # after a further call (the static scratch was set up by the calls above)
+    free0 = torch.cuda.mem_get_info()[0]
+    solve(lib, "st_cg_device_static", m, b, x_sta, jacobi)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
 
 
 def test_static_cg_rejects_oversized_system(se):
