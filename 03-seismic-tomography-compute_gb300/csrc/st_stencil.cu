@@ -821,14 +821,19 @@ __device__ __forceinline__ void adj_update4(const StepArgs& a, const float u0[4]
     }
 }
 
-__device__ __forceinline__ void sponge4(const StepArgs& a, const float* dtab, int dx, const int dyz[4], bool far,
-                                        float D[4]) {
+// Sponge factors of a 4-point group: D(min(dx, dyz)) for each point, formed
+// as min(D(dx), D(dyz)) from the y/z factors Dyz the thread looked up once
+// (the table is non-decreasing in the distance, so this is bit for bit the
+// same), or 1 when the group lies beyond the sponge on every axis.
+__device__ __forceinline__ void sponge4f(const StepArgs& a, const float* dtab, int dx, const float Dyz[4], bool far,
+                                         float D[4]) {
     if (far && dx >= a.sw) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) D[k] = 1.0f;
     } else {
+        const float Dx = dx < a.sw ? dtab[dx] : 1.0f;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) D[k] = sponge_tab(a, dtab, min(dx, dyz[k]));
+        for (int k = 0; k < 4; ++k) D[k] = fminf(Dx, Dyz[k]);
     }
 }
 
@@ -932,6 +937,17 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     if (tab_smem)
         for (int i = tid; i < a.sw; i += NTHREADS) dtab_s[i] = a.dtab[i];
     const float* dtab = tab_smem ? dtab_s : a.dtab;
+    // The sponge factor of a point is D(min(dx, dyz)) = min(D(dx), D(dyz)):
+    // the table grows with the distance, so the y/z factors are looked up once
+    // (from the global table: the shared copy is complete only after the
+    // barrier below) and each plane takes one lookup for x.
+    float Dc[4], Dr[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        Dc[k] = dyz_c[k] < a.sw ? a.dtab[dyz_c[k]] : 1.0f;
+        Dr[k] = dyz_r[k] < a.sw ? a.dtab[dyz_r[k]] : 1.0f;
+    }
+    const float Dz = dyz_z < a.sw ? a.dtab[dyz_z] : 1.0f;
     // imaging: snapshot scales of steps t and t-1; forward: inverse scales of
     // the two stored snapshots (u_t and u_{t-1})
     float scale_a = 0.0f, scale_b = 0.0f;
@@ -1030,7 +1046,9 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     int i = 0;
     // one plane; q0 / q1 / q2 are the queue slots of planes i-2 / i-1 / i
     // (for the u' queue: i-3 / i-2 / i-1); returns true when a wait gave up
-    auto plane = [&](const int q0, const int q1, const int q2) -> bool {
+    // cs / csp: the stage of plane i / i-1 (literals in the unrolled forward
+    // loop, so every shared-memory address there is a constant offset)
+    auto plane = [&](const int q0, const int q1, const int q2, const int cs, const int csp) -> bool {
         float(&um)[4] = U[q0];
         float(&up)[4] = U[q2];
         float(&rm)[4] = R[q0];
@@ -1040,16 +1058,16 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
         float(&lm)[4] = Lq[q0];
         float(&l0)[4] = Lq[q1];
         float(&lp)[4] = Lq[q2];
-        if (!mbar_wait_bounded(&bar[s], parity, a.timeout_ns)) timed_out = 1;
+        if (!mbar_wait_bounded(&bar[cs], parity, a.timeout_ns)) timed_out = 1;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             rp[k] = 0.0f;
             lp[k] = 0.0f;
         }
         zp_ = 0.0f;
-        ld4(st_cur(s) + tcen, up);
-        if (has_yr) ld4(st_cur(s) + tyr, rp);
-        if (has_zr) zp_ = st_cur(s)[tzr];
+        ld4(st_cur(cs) + tcen, up);
+        if (has_yr) ld4(st_cur(cs) + tyr, rp);
+        if (has_zr) zp_ = st_cur(cs)[tzr];
         float cnow[4] = {0, 0, 0, 0};
         int irx = -1;
         if (i >= 2) {
@@ -1063,9 +1081,9 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
             if (any_rec && xin) irx = rec_line(x, a.rx0, a.rsx, a.rnx);
             const int irx_a = (BACK ? a.force_row : a.seis_row) ? irx : -1;  // step t's receivers
             const bool inj_a = inj && (a.inj_steps & 1) && x == a.inj_x;
-            const float* T = st_cur(sp);
-            const float* P = st_prev(sp);
-            const float* Cc = st_c(sp);
+            const float* T = st_cur(csp);
+            const float* P = st_prev(csp);
+            const float* Cc = st_c(csp);
             float* Lw = lb(i - 1);
             // centre
             ld4(Cc + rcen, cnow);
@@ -1075,7 +1093,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                 ld4(P + rcen, pv);
                 ld4(T + tcen - W, ym);
                 ld4(T + tcen + W, yp);
-                sponge4(a, dtab, dx, dyz_c, far_c, D);
+                sponge4f(a, dtab, dx, Dc, far_c, D);
                 const bool rc = irx_a >= 0 && iry_c >= 0;
                 const int q = rc ? irx_a * a.rny + iry_c : 0;
                 adj_update4(a, c0, pv, um, up, ym, yp, T[tcen - 1], T[tcen + 4], cnow, D, a.force_row, q,
@@ -1093,18 +1111,20 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                     }
                     if constexpr (SNAPS) {
                         if (own) {
-                            const long long cb = ((long long)x * a.ny + yc) * a.nz + zc;
+                            // plane x = xa - 3 + i: one plane past sub-step B's (cb),
+                            // except at i = 3 where both name the chunk's first plane
+                            const long long cbA = cb + (i >= 4 ? cplane : 0);
                             float qv[4];
 #pragma unroll
                             for (int k = 0; k < 4; ++k) {
                                 qv[k] = c0[k] * scale_a;
                                 amax1 = fmaxf(amax1, fabsf(lp[k]));
                             }
-                            snap_store4<SK>(a.snap_out, cb, qv);
+                            snap_store4<SK>(a.snap_out, cbA, qv);
                             if (a.snap_out2) {
 #pragma unroll
                                 for (int k = 0; k < 4; ++k) qv[k] = pv[k] * scale_b;
-                                snap_store4<SK>(a.snap_out2, cb, qv);
+                                snap_store4<SK>(a.snap_out2, cbA, qv);
                             }
                         }
                     }
@@ -1120,7 +1140,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                     ld4(Cc + ryr, cv);
                     ld4(T + tyr - W, ym);
                     ld4(T + tyr + W, yp);
-                    sponge4(a, dtab, dx, dyz_r, false, D);
+                    sponge4f(a, dtab, dx, Dr, false, D);
                     const bool rr = BACK && irx_a >= 0 && iry_r >= 0;
                     adj_update4(a, c0, pv, rm, rp, ym, yp, T[tyr - 1], T[tyr + 4], cv, D, a.force_row,
                                 rr ? irx_a * a.rny + iry_r : 0, rr ? rkr : -1, res, &fired);
@@ -1135,7 +1155,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
             if (has_zr) {
                 float res = 0.0f;
                 if (xin && zrin) {
-                    const float D = sponge_tab(a, dtab, min(dx, dyz_z));
+                    const float D = fminf(dx < a.sw ? dtab[dx] : 1.0f, Dz);
                     const float u = T[tzr], c = Cc[rzr];
                     const float upd = D * P[rzr];
                     const float ym = T[tzr - W], yp = T[tzr + W], zm = T[tzr - 1], zp = T[tzr + 1];
@@ -1158,7 +1178,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
             float ym[4], yp[4], D[4], res[4];
             ld4(Lr + rcen - W, ym);
             ld4(Lr + rcen + W, yp);
-            sponge4(a, dtab, dx, dyz_c, far_c, D);
+            sponge4f(a, dtab, dx, Dc, far_c, D);
             const float* rows2 = BACK ? a.force_row2 : a.seis_row2;
             const bool rc = rows2 && irx_prev >= 0 && iry_c >= 0;
             const int q = rc ? irx_prev * a.rny + iry_c : 0;
@@ -1186,10 +1206,10 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                 // imaging: step t pairs lambda_t with the snapshot of t, step t-1
                 // pairs lambda' with the snapshot of t-1, in that order
                 float fa[4], fb[4], im[4], il[4];
-                snap_smem4<SK>(st_sa(sp), ccen, fa);
-                snap_smem4<SK>(st_sb(sp), ccen, fb);
-                ld4(st_img(sp) + ccen, im);
-                ld4(st_ill(sp) + ccen, il);
+                snap_smem4<SK>(st_sa(csp), ccen, fa);
+                snap_smem4<SK>(st_sb(csp), ccen, fb);
+                ld4(st_img(csp) + ccen, im);
+                ld4(st_ill(csp) + ccen, il);
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const float w = a.stable_sponge ? cprev[k] * D[k] : cprev[k];
@@ -1213,9 +1233,9 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                 // gradient: step t pairs lambda_t with L(snapshot of t), step t-1
                 // pairs lambda' with L(snapshot of t-1), in that order
                 float fa[4], fb[4], g[4];
-                snap_lap4<SK, G::GSW>(st_sa(sp), st_sa(s), gsrow, sm_a, a, scale_a, fa);
-                snap_lap4<SK, G::GSW>(st_sb(sp), st_sb(s), gsrow, sm_b, a, scale_b, fb);
-                ld4(st_img(sp) + ccen, g);
+                snap_lap4<SK, G::GSW>(st_sa(csp), st_sa(cs), gsrow, sm_a, a, scale_a, fa);
+                snap_lap4<SK, G::GSW>(st_sb(csp), st_sb(cs), gsrow, sm_b, a, scale_b, fb);
+                ld4(st_img(csp) + ccen, g);
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     g[k] = fmaf(um[k] / cprev[k], fa[k], g[k]);
@@ -1227,8 +1247,8 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
         if constexpr (GRD) {
             // the snapshot centres of plane i-2 are the next plane's x-1 values
             if (i >= 3) {
-                snap_smem4<SK>(st_sa(sp), gsrow, sm_a);
-                snap_smem4<SK>(st_sb(sp), gsrow, sm_b);
+                snap_smem4<SK>(st_sa(csp), gsrow, sm_a);
+                snap_smem4<SK>(st_sb(csp), gsrow, sm_b);
             }
         }
 #pragma unroll
@@ -1250,19 +1270,20 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
         return false;
     };
     if constexpr (FWD) {
+        static_assert(STAGES == 3, "the unrolled forward loop names the stages of a 3-deep ring");
         while (i < nplanes) {
-            if (plane(0, 1, 2)) break;
+            if (plane(0, 1, 2, 0, 2)) break;
             if (++i == nplanes) break;
-            if (plane(1, 2, 0)) break;
+            if (plane(1, 2, 0, 1, 0)) break;
             if (++i == nplanes) break;
-            if (plane(2, 0, 1)) break;
+            if (plane(2, 0, 1, 2, 1)) break;
             ++i;
         }
     } else {
         // the adjoint modes' larger body measured 7% slower unrolled (the
         // three copies), so they keep one copy and rotate the slots
         while (i < nplanes) {
-            if (plane(0, 1, 2)) break;
+            if (plane(0, 1, 2, s, sp)) break;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 U[0][k] = U[1][k];
