@@ -1060,11 +1060,8 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
         float(&lp)[4] = Lq[q2];
         if (!mbar_wait_bounded(&bar[cs], parity, a.timeout_ns)) timed_out = 1;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            rp[k] = 0.0f;
-            lp[k] = 0.0f;
-        }
-        zp_ = 0.0f;
+        for (int k = 0; k < 4; ++k) lp[k] = 0.0f;
+        // rp / zp_ are read only by the ring warps, which load them here
         ld4(st_cur(cs) + tcen, up);
         if (has_yr) ld4(st_cur(cs) + tyr, rp);
         if (has_zr) zp_ = st_cur(cs)[tzr];
@@ -1288,13 +1285,21 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
             for (int k = 0; k < 4; ++k) {
                 U[0][k] = U[1][k];
                 U[1][k] = U[2][k];
-                R[0][k] = R[1][k];
-                R[1][k] = R[2][k];
                 Lq[0][k] = Lq[1][k];
                 Lq[1][k] = Lq[2][k];
             }
-            Zq[0] = Zq[1];
-            Zq[1] = Zq[2];
+            // the ring queues only in the warps that own the ring tasks
+            if (has_yr) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    R[0][k] = R[1][k];
+                    R[1][k] = R[2][k];
+                }
+            }
+            if (has_zr) {
+                Zq[0] = Zq[1];
+                Zq[1] = Zq[2];
+            }
             ++i;
         }
     }
