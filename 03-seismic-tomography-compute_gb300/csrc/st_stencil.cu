@@ -888,50 +888,51 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     if (xa >= xb) return;  // uniform over the CTA
     const int nplanes = xb - xa + 4;
 
-    // the thread's tasks: the centre group (row yc, z zc .. zc+3); the lanes of
-    // warp 0 also take the ring rows y0-1 (lanes 0-15) and y0+16 (lanes 16-31)
-    // at z-group lane % 16, the lanes of the last warp the ring points z0-1
-    // (even lanes) and z0+64 (odd lanes) of row y0 + lane / 2
+    // the thread's tasks: the centre group (row yc, z zc .. zc+3) and, for
+    // threads 0 .. 159 (warps 0-4), one point of sub-step A's ring: threads
+    // 0-63 row y0-1 and 64-127 row y0+16 at z0 + (tid & 63), threads 128-159
+    // the points z0-1 (even) and z0+64 (odd) of row y0 + (tid - 128) / 2.
+    // One point per lane keeps the extra work of any warp to one scalar
+    // update, so no warp holds the others up at the plane barrier.
     const int warp = tid >> 5, lane = tid & 31;
+    (void)warp;
+    (void)lane;
     const int zc = z0 + 4 * tz4;
     const int yc = y0 + yr;
     const bool cin = yc < a.ny && zc < a.nz;
-    const bool has_yr = warp == 0;
-    const int zcr = z0 + 4 * (lane & 15);
-    const int yring = lane < 16 ? y0 - 1 : y0 + G::TYV;
-    const bool yrin = has_yr && yring >= 0 && yring < a.ny && zcr < a.nz;
-    const bool has_zr = warp == NTHREADS / 32 - 1;
-    const int yz = y0 + (lane >> 1);
-    const int zring = (lane & 1) ? z0 + TZ : z0 - 1;
-    const bool zrin = has_zr && yz < a.ny && zring >= 0 && zring < a.nz;
+    constexpr int NRING = 2 * TZ + 2 * G::TYV;
+    static_assert(NRING <= NTHREADS, "one ring point per thread");
+    const bool has_ring = tid < NRING;
+    int yq, zq;
+    if (tid < 2 * TZ) {
+        yq = tid < TZ ? y0 - 1 : y0 + G::TYV;
+        zq = z0 + (tid & (TZ - 1));
+    } else {
+        const int q = tid - 2 * TZ;
+        yq = y0 + (q >> 1);
+        zq = (q & 1) ? z0 + TZ : z0 - 1;
+    }
+    const bool ringin = has_ring && yq >= 0 && yq < a.ny && zq >= 0 && zq < a.nz;
     // y/z distances to the nearest face (sponge), fixed over the march; far_c:
     // the centre group is beyond the sponge along y and z
-    int dyz_c[4], dyz_r[4];
-    const int dyc = min(yc, a.ny - 1 - yc), dyr = min(yring, a.ny - 1 - yring);
+    int dyz_c[4];
+    const int dyc = min(yc, a.ny - 1 - yc);
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        dyz_c[k] = min(dyc, min(zc + k, a.nz - 1 - (zc + k)));
-        dyz_r[k] = min(dyr, min(zcr + k, a.nz - 1 - (zcr + k)));
-    }
+    for (int k = 0; k < 4; ++k) dyz_c[k] = min(dyc, min(zc + k, a.nz - 1 - (zc + k)));
     const bool far_c = min(min(dyz_c[0], dyz_c[1]), min(dyz_c[2], dyz_c[3])) >= a.sw;
-    const int dyz_z = min(min(yz, a.ny - 1 - yz), min(zring, a.nz - 1 - zring));
+    const int dyz_q = min(min(yq, a.ny - 1 - yq), min(zq, a.nz - 1 - zq));
     // receivers: forcing (adjoint) at every task, sampling (forward) at the
-    // centre only; rk / rkr: the receiver plane's point in the centre /
-    // ring-row group
+    // centre only; rk: the receiver plane's point in the centre group
     const bool recs = BACK ? (a.force_row || a.force_row2) : (a.seis_row || a.seis_row2);
     const int rk = (recs && a.rz >= zc && a.rz < zc + 4) ? a.rz - zc : -1;
-    const int rkr = (BACK && recs && has_yr && a.rz >= zcr && a.rz < zcr + 4) ? a.rz - zcr : -1;
     const int iry_c = rk >= 0 ? rec_line(yc, a.ry0, a.rsy, a.rny) : -1;
-    const int iry_r = rkr >= 0 ? rec_line(yring, a.ry0, a.rsy, a.rny) : -1;
-    const int iry_z = BACK && recs && has_zr && zring == a.rz ? rec_line(yz, a.ry0, a.rsy, a.rny) : -1;
-    const bool any_rec = iry_c >= 0 || iry_r >= 0 || iry_z >= 0;
+    const int iry_q = BACK && recs && ringin && zq == a.rz ? rec_line(yq, a.ry0, a.rsy, a.rny) : -1;
+    const bool any_rec = iry_c >= 0 || iry_q >= 0;
     // forward source injection (a.inj_steps bit 0: sub-step A, bit 1: B) at
-    // point inj_kc / inj_kr of the centre / ring-row group, or the ring point
+    // point inj_kc of the centre group, or the ring point
     const bool inj = FWD && a.inj_x >= 0;
     const int inj_kc = (inj && a.inj_y == yc && a.inj_z >= zc && a.inj_z < zc + 4) ? a.inj_z - zc : -1;
-    const int inj_kr = (inj && has_yr && a.inj_y == yring && a.inj_z >= zcr && a.inj_z < zcr + 4) ? a.inj_z - zcr
-                                                                                                  : -1;
-    const bool inj_z = inj && has_zr && a.inj_y == yz && a.inj_z == zring;
+    const bool inj_q = inj && has_ring && a.inj_y == yq && a.inj_z == zq;
 
     const bool tab_smem = a.sw <= DTAB_MAX;
     if (tab_smem)
@@ -941,13 +942,11 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     // the table grows with the distance, so the y/z factors are looked up once
     // (from the global table: the shared copy is complete only after the
     // barrier below) and each plane takes one lookup for x.
-    float Dc[4], Dr[4];
+    // (distances below 0 belong to points outside the grid, never updated)
+    float Dc[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        Dc[k] = dyz_c[k] < a.sw ? a.dtab[dyz_c[k]] : 1.0f;
-        Dr[k] = dyz_r[k] < a.sw ? a.dtab[dyz_r[k]] : 1.0f;
-    }
-    const float Dz = dyz_z < a.sw ? a.dtab[dyz_z] : 1.0f;
+    for (int k = 0; k < 4; ++k) Dc[k] = (dyz_c[k] >= 0 && dyz_c[k] < a.sw) ? a.dtab[dyz_c[k]] : 1.0f;
+    const float Dq = (dyz_q >= 0 && dyz_q < a.sw) ? a.dtab[dyz_q] : 1.0f;
     // imaging: snapshot scales of steps t and t-1; forward: inverse scales of
     // the two stored snapshots (u_t and u_{t-1})
     float scale_a = 0.0f, scale_b = 0.0f;
@@ -1016,17 +1015,16 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     }
 
     const int tcen = (yr + 2) * W + 4 * tz4 + 4;                 // centre in a current-field tile
-    const int tyr = (yring - y0 + 2) * W + (zcr - z0) + 4;       // ring row in a current-field tile
-    const int tzr = (yz - y0 + 2) * W + (zring - z0 + 4);        // ring point in a current-field tile
-    const int rcen = tcen - W, ryr = tyr - W, rzr = tzr - W;     // the same in ring-geometry tiles
+    const int tq = has_ring ? (yq - y0 + 2) * W + (zq - z0 + 4) : 0;  // ring point in a current-field tile
+    const int rcen = tcen - W, rq = tq - W;                      // the same in ring-geometry tiles
     const int ccen = yr * TZ + 4 * tz4;                          // centre in the compact tiles
     const int gsrow = (yr + 1) * G::GSW + 4 * tz4 + G::GSOFF;    // centre in the gradient's snapshot tiles
-    // current-field queues (x-1, x, x+1) of the three tasks, the u' queue of
-    // the centre (planes i-3, i-2, i-1) and c of the centre at plane i-2
-    // The queues have period 3 along x: in the forward mode the plane loop
-    // is unrolled three times and each copy names the slots in its own order,
-    // so the queues rotate by renaming, not by register moves.
-    float U[3][4] = {}, R[3][4] = {}, Zq[3] = {}, Lq[3][4] = {};
+    // current-field queues (x-1, x, x+1) of the centre group and of the ring
+    // point, the u' queue of the centre (planes i-3, i-2, i-1) and c of the
+    // centre at plane i-2. The queues have period 3 along x: in the forward
+    // mode the plane loop is unrolled three times and each copy names the
+    // slots in its own order, so the queues rotate by renaming, not by moves.
+    float U[3][4] = {}, Qq[3] = {}, Lq[3][4] = {};
     float cprev[4] = {0, 0, 0, 0};
     float sm_a[4] = {0, 0, 0, 0}, sm_b[4] = {0, 0, 0, 0};  // gradient: snapshot centres at plane i-3
     int irx_prev = -1;  // receiver column of plane i-2
@@ -1051,20 +1049,17 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     auto plane = [&](const int q0, const int q1, const int q2, const int cs, const int csp) -> bool {
         float(&um)[4] = U[q0];
         float(&up)[4] = U[q2];
-        float(&rm)[4] = R[q0];
-        float(&rp)[4] = R[q2];
-        float& zm_ = Zq[q0];
-        float& zp_ = Zq[q2];
+        float& qm_ = Qq[q0];
+        float& qp_ = Qq[q2];
         float(&lm)[4] = Lq[q0];
         float(&l0)[4] = Lq[q1];
         float(&lp)[4] = Lq[q2];
         if (!mbar_wait_bounded(&bar[cs], parity, a.timeout_ns)) timed_out = 1;
 #pragma unroll
         for (int k = 0; k < 4; ++k) lp[k] = 0.0f;
-        // rp / zp_ are read only by the ring warps, which load them here
+        // qp_ is read only by the ring threads, which load it here
         ld4(st_cur(cs) + tcen, up);
-        if (has_yr) ld4(st_cur(cs) + tyr, rp);
-        if (has_zr) zp_ = st_cur(cs)[tzr];
+        if (has_ring) qp_ = st_cur(cs)[tq];
         float cnow[4] = {0, 0, 0, 0};
         int irx = -1;
         if (i >= 2) {
@@ -1128,42 +1123,21 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                 }
             }
             st4(Lw + rcen, lp);
-            if (has_yr) {
-                float res[4] = {0, 0, 0, 0};
-                if (xin && yrin) {
-                    float c0[4], pv[4], ym[4], yp[4], cv[4], D[4];
-                    ld4(T + tyr, c0);
-                    ld4(P + ryr, pv);
-                    ld4(Cc + ryr, cv);
-                    ld4(T + tyr - W, ym);
-                    ld4(T + tyr + W, yp);
-                    sponge4f(a, dtab, dx, Dr, false, D);
-                    const bool rr = BACK && irx_a >= 0 && iry_r >= 0;
-                    adj_update4(a, c0, pv, rm, rp, ym, yp, T[tyr - 1], T[tyr + 4], cv, D, a.force_row,
-                                rr ? irx_a * a.rny + iry_r : 0, rr ? rkr : -1, res, &fired);
-                    if (FWD && inj_a) {
-#pragma unroll
-                        for (int k = 0; k < 4; ++k)
-                            if (k == inj_kr) res[k] += a.inj_val;
-                    }
-                }
-                st4(Lw + ryr, res);
-            }
-            if (has_zr) {
+            if (has_ring) {
                 float res = 0.0f;
-                if (xin && zrin) {
-                    const float D = fminf(dx < a.sw ? dtab[dx] : 1.0f, Dz);
-                    const float u = T[tzr], c = Cc[rzr];
-                    const float upd = D * P[rzr];
-                    const float ym = T[tzr - W], yp = T[tzr + W], zm = T[tzr - 1], zp = T[tzr + 1];
-                    res = update_fast(u, upd, zm_, zp_, ym, yp, zm, zp, c, a.ax, a.ay, a.az);
+                if (xin && ringin) {
+                    const float D = fminf(dx < a.sw ? dtab[dx] : 1.0f, Dq);
+                    const float u = T[tq], c = Cc[rq];
+                    const float upd = D * P[rq];
+                    const float ym = T[tq - W], yp = T[tq + W], zm = T[tq - 1], zp = T[tq + 1];
+                    res = update_fast(u, upd, qm_, qp_, ym, yp, zm, zp, c, a.ax, a.ay, a.az);
                     if (!(fabsf(res) <= a.amp))
-                        res = update_guarded(u, upd, zm_, zp_, ym, yp, zm, zp, c, a.ax, a.ay, a.az, a.amp, &fired);
-                    if (BACK && irx_a >= 0 && iry_z >= 0) res = fmaf(c, a.force_row[irx_a * a.rny + iry_z], res);
+                        res = update_guarded(u, upd, qm_, qp_, ym, yp, zm, zp, c, a.ax, a.ay, a.az, a.amp, &fired);
+                    if (BACK && irx_a >= 0 && iry_q >= 0) res = fmaf(c, a.force_row[irx_a * a.rny + iry_q], res);
                     if (a.stable_sponge) res *= D;
-                    if (FWD && inj_a && inj_z) res += a.inj_val;
+                    if (FWD && inj_a && inj_q) res += a.inj_val;
                 }
-                Lw[rzr] = res;
+                Lw[rq] = res;
             }
         }
         if (i >= 4 && cin) {
@@ -1288,17 +1262,10 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                 Lq[0][k] = Lq[1][k];
                 Lq[1][k] = Lq[2][k];
             }
-            // the ring queues only in the warps that own the ring tasks
-            if (has_yr) {
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    R[0][k] = R[1][k];
-                    R[1][k] = R[2][k];
-                }
-            }
-            if (has_zr) {
-                Zq[0] = Zq[1];
-                Zq[1] = Zq[2];
+            // the ring queue only in the threads that own a ring point
+            if (has_ring) {
+                Qq[0] = Qq[1];
+                Qq[1] = Qq[2];
             }
             ++i;
         }
