@@ -822,19 +822,12 @@ __device__ __forceinline__ void adj_update4(const StepArgs& a, const float u0[4]
 }
 
 // Sponge factors of a 4-point group: D(min(dx, dyz)) for each point, formed
-// as min(D(dx), D(dyz)) from the y/z factors Dyz the thread looked up once
-// (the table is non-decreasing in the distance, so this is bit for bit the
-// same), or 1 when the group lies beyond the sponge on every axis.
-__device__ __forceinline__ void sponge4f(const StepArgs& a, const float* dtab, int dx, const float Dyz[4], bool far,
-                                         float D[4]) {
-    if (far && dx >= a.sw) {
+// as min(D(dx), D(dyz)) from the plane's x factor Dx and the y/z factors Dyz
+// the thread looked up once (the table is non-decreasing in the distance and
+// at most 1, so this is bit for bit the same).
+__device__ __forceinline__ void sponge4f(float Dx, const float Dyz[4], float D[4]) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) D[k] = 1.0f;
-    } else {
-        const float Dx = dx < a.sw ? dtab[dx] : 1.0f;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) D[k] = fminf(Dx, Dyz[k]);
-    }
+    for (int k = 0; k < 4; ++k) D[k] = fminf(Dx, Dyz[k]);
 }
 
 // Laplacian of a snapshot at the four z of a centre group, scaled, with the
@@ -913,13 +906,11 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
         zq = (q & 1) ? z0 + TZ : z0 - 1;
     }
     const bool ringin = has_ring && yq >= 0 && yq < a.ny && zq >= 0 && zq < a.nz;
-    // y/z distances to the nearest face (sponge), fixed over the march; far_c:
-    // the centre group is beyond the sponge along y and z
+    // y/z distances to the nearest face (sponge), fixed over the march
     int dyz_c[4];
     const int dyc = min(yc, a.ny - 1 - yc);
 #pragma unroll
     for (int k = 0; k < 4; ++k) dyz_c[k] = min(dyc, min(zc + k, a.nz - 1 - (zc + k)));
-    const bool far_c = min(min(dyz_c[0], dyz_c[1]), min(dyz_c[2], dyz_c[3])) >= a.sw;
     const int dyz_q = min(min(yq, a.ny - 1 - yq), min(zq, a.nz - 1 - zq));
     // receivers: forcing (adjoint) at every task, sampling (forward) at the
     // centre only; rk: the receiver plane's point in the centre group
@@ -937,7 +928,12 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     const bool tab_smem = a.sw <= DTAB_MAX;
     if (tab_smem)
         for (int i = tid; i < a.sw; i += NTHREADS) dtab_s[i] = a.dtab[i];
-    const float* dtab = tab_smem ? dtab_s : a.dtab;
+    // x factor of a plane: the shared copy of the table when it has one
+    // (addressed as shared memory, not through a generic pointer)
+    auto x_factor = [&](int dx) -> float {
+        if (dx >= a.sw) return 1.0f;
+        return tab_smem ? dtab_s[dx] : __ldg(a.dtab + dx);
+    };
     // The sponge factor of a point is D(min(dx, dyz)) = min(D(dx), D(dyz)):
     // the table grows with the distance, so the y/z factors are looked up once
     // (from the global table: the shared copy is complete only after the
@@ -1077,6 +1073,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
             const float* P = st_prev(csp);
             const float* Cc = st_c(csp);
             float* Lw = lb(i - 1);
+            const float Dx = xin ? x_factor(dx) : 1.0f;
             // centre
             ld4(Cc + rcen, cnow);
             if (xin && cin) {
@@ -1085,7 +1082,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                 ld4(P + rcen, pv);
                 ld4(T + tcen - W, ym);
                 ld4(T + tcen + W, yp);
-                sponge4f(a, dtab, dx, Dc, far_c, D);
+                sponge4f(Dx, Dc, D);
                 const bool rc = irx_a >= 0 && iry_c >= 0;
                 const int q = rc ? irx_a * a.rny + iry_c : 0;
                 adj_update4(a, c0, pv, um, up, ym, yp, T[tcen - 1], T[tcen + 4], cnow, D, a.force_row, q,
@@ -1126,7 +1123,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
             if (has_ring) {
                 float res = 0.0f;
                 if (xin && ringin) {
-                    const float D = fminf(dx < a.sw ? dtab[dx] : 1.0f, Dq);
+                    const float D = fminf(Dx, Dq);
                     const float u = T[tq], c = Cc[rq];
                     const float upd = D * P[rq];
                     const float ym = T[tq - W], yp = T[tq + W], zm = T[tq - 1], zp = T[tq + 1];
@@ -1149,7 +1146,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
             float ym[4], yp[4], D[4], res[4];
             ld4(Lr + rcen - W, ym);
             ld4(Lr + rcen + W, yp);
-            sponge4f(a, dtab, dx, Dc, far_c, D);
+            sponge4f(x_factor(dx), Dc, D);
             const float* rows2 = BACK ? a.force_row2 : a.seis_row2;
             const bool rc = rows2 && irx_prev >= 0 && iry_c >= 0;
             const int q = rc ? irx_prev * a.rny + iry_c : 0;
