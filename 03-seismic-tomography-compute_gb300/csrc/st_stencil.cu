@@ -1237,8 +1237,11 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
         if (tid == 0 && i >= 1 && issued < nplanes) issue(issued++);
         return false;
     };
-    if constexpr (FWD) {
-        static_assert(STAGES == 3, "the unrolled forward loop names the stages of a 3-deep ring");
+    // The forward and imaging modes unroll the plane loop three times (the
+    // imaging mode measured 1% faster so since its ring work shrank); the
+    // gradient mode keeps one copy of its larger body and rotates the slots.
+    if constexpr (FWD || MODE == MODE_ADJ) {
+        static_assert(STAGES == 3, "the unrolled loop names the stages of a 3-deep ring");
         while (i < nplanes) {
             if (plane(0, 1, 2, 0, 2)) break;
             if (++i == nplanes) break;
@@ -1248,8 +1251,6 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
             ++i;
         }
     } else {
-        // the adjoint modes' larger body measured 7% slower unrolled (the
-        // three copies), so they keep one copy and rotate the slots
         while (i < nplanes) {
             if (plane(0, 1, 2, s, sp)) break;
 #pragma unroll
