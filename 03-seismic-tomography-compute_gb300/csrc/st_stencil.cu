@@ -199,10 +199,16 @@ __device__ __forceinline__ float update_fast(float u, float upd, float xm, float
 // The reference's guarded update (wave_equation.cpp:342-399), taken only when
 // the fast result is non-finite or beyond the amplitude limit. A non-finite
 // input always makes the fast result non-finite (c, 1/d^2 > 0), so the fast
-// path is exact whenever it is taken.
-__device__ __noinline__ float update_guarded(float u, float upd, float xm, float xp, float ym, float yp, float zm,
-                                             float zp, float c, float ax, float ay, float az, float amp,
-                                             int* fired) {
+// path is exact whenever it is taken. GINL: inlined at the call site (the
+// two-step forward and imaging kernels measured faster so, with fewer
+// registers); otherwise one out-of-line copy shared by the call sites.
+template <bool GINL = false>
+__device__ __forceinline__ float update_guarded(float u, float upd, float xm, float xp, float ym, float yp, float zm,
+                                                float zp, float c, float ax, float ay, float az, float amp,
+                                                int* fired);
+__device__ __forceinline__ float guarded_body(float u, float upd, float xm, float xp, float ym, float yp, float zm,
+                                              float zp, float c, float ax, float ay, float az, float amp,
+                                              int* fired) {
     if (!isfinite(u) || !isfinite(upd)) {
         *fired = 1;
         return 0.0f;
@@ -217,6 +223,17 @@ __device__ __noinline__ float update_guarded(float u, float upd, float xm, float
         *fired = 1;
     }
     return fminf(fmaxf(nv, -amp), amp);
+}
+__device__ __noinline__ float guarded_call(float u, float upd, float xm, float xp, float ym, float yp, float zm,
+                                           float zp, float c, float ax, float ay, float az, float amp, int* fired) {
+    return guarded_body(u, upd, xm, xp, ym, yp, zm, zp, c, ax, ay, az, amp, fired);
+}
+template <bool GINL>
+__device__ __forceinline__ float update_guarded(float u, float upd, float xm, float xp, float ym, float yp, float zm,
+                                                float zp, float c, float ax, float ay, float az, float amp,
+                                                int* fired) {
+    if constexpr (GINL) return guarded_body(u, upd, xm, xp, ym, yp, zm, zp, c, ax, ay, az, amp, fired);
+    else return guarded_call(u, upd, xm, xp, ym, yp, zm, zp, c, ax, ay, az, amp, fired);
 }
 
 // Per-row bookkeeping of one thread (4 consecutive z of one y row).
@@ -782,14 +799,14 @@ __device__ __forceinline__ void st4(float* p, const float v[4]) {
     *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
 }
 
-// Four point updates in fd_step_kernel's order: the update (the guarded form
-// where the fast one is out of range), the adjoint receiver forcing
-// c * force[q] at point rk (rk < 0: none), then the stable damping.
-__device__ __forceinline__ void adj_update4(const StepArgs& a, const float u0[4], const float pv[4],
-                                            const float um[4], const float up[4], const float ym[4],
-                                            const float yp[4], float zm0, float zp3, const float cv[4],
-                                            const float D[4], const float* force, int q, int rk, float res[4],
-                                            int* fired) {
+// Four point updates in fd_step_kernel's order, first part: the update (the
+// guarded form where the fast one is out of range). The caller then adds the
+// adjoint receiver forcing, applies the stable damping (stable_damp4) and, in
+// the forward mode, samples the receivers and injects the source.
+template <bool GINL>
+__device__ __forceinline__ void update4(const StepArgs& a, const float u0[4], const float pv[4], const float um[4],
+                                        const float up[4], const float ym[4], const float yp[4], float zm0, float zp3,
+                                        const float cv[4], const float D[4], float res[4], int* fired) {
     float upd[4];
     bool bad = false;
 #pragma unroll
@@ -806,15 +823,14 @@ __device__ __forceinline__ void adj_update4(const StepArgs& a, const float u0[4]
             if (fabsf(res[k]) <= a.amp) continue;
             const float zm = k == 0 ? zm0 : u0[k - 1];
             const float zp = k == 3 ? zp3 : u0[k + 1];
-            res[k] = update_guarded(u0[k], upd[k], um[k], up[k], ym[k], yp[k], zm, zp, cv[k], a.ax, a.ay, a.az,
-                                    a.amp, fired);
+            res[k] = update_guarded<GINL>(u0[k], upd[k], um[k], up[k], ym[k], yp[k], zm, zp, cv[k], a.ax, a.ay, a.az,
+                                          a.amp, fired);
         }
     }
-    if (rk >= 0) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (k == rk) res[k] = fmaf(cv[k], force[q], res[k]);
-    }
+}
+
+// The stable sponge mode damps the new values as well.
+__device__ __forceinline__ void stable_damp4(const StepArgs& a, const float D[4], float res[4]) {
     if (a.stable_sponge) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) res[k] *= D[k];
@@ -851,6 +867,19 @@ __device__ __forceinline__ void snap_lap4(const unsigned char* S, const unsigned
     }
 }
 
+// What one iteration of fd_step2_kernel's plane loop runs, fixed at compile
+// time where the loop position fixes it. Sub-step A: A_RT (decided from the
+// plane index, for the gradient's rolled loop), A_NONE (the first two planes),
+// A_EDGE (a halo plane beside the chunk: the grid test at run time, no
+// sampling, snapshots or maxima), A_OWN (a plane of the chunk). Sub-step B:
+// B_RT (from the plane index), B_NONE (the first four planes), B_ON.
+enum : int { A_RT, A_NONE, A_EDGE, A_OWN };
+enum : int { B_RT, B_NONE, B_ON };
+template <int PA_, int PB_>
+struct PlaneKind {
+    static constexpr int PA = PA_, PB = PB_;
+};
+
 template <int MODE, int SK>
 __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     fd_step2_kernel(const __grid_constant__ CUtensorMap map_cur, const __grid_constant__ CUtensorMap map_prev,
@@ -863,6 +892,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     constexpr bool FWD = MODE == MODE_FWD;
     constexpr bool BACK = !FWD;                // receiver forcing, snapshots read
     constexpr bool SNAPS = FWD && SK != SNAP_NONE;
+    constexpr bool GINL = !GRD;                // the guarded update inlined (not in the larger gradient body)
     constexpr int W = G::W;
     constexpr int STAGES = G::STAGES;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -924,6 +954,9 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     const bool inj = FWD && a.inj_x >= 0;
     const int inj_kc = (inj && a.inj_y == yc && a.inj_z >= zc && a.inj_z < zc + 4) ? a.inj_z - zc : -1;
     const bool inj_q = inj && has_ring && a.inj_y == yq && a.inj_z == zq;
+    // the thread holds a receiver or the source point: the only threads that
+    // run the per-plane receiver and source work
+    const bool special = any_rec || inj_kc >= 0 || inj_q;
 
     const bool tab_smem = a.sw <= DTAB_MAX;
     if (tab_smem)
@@ -1040,9 +1073,12 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     int i = 0;
     // one plane; q0 / q1 / q2 are the queue slots of planes i-2 / i-1 / i
     // (for the u' queue: i-3 / i-2 / i-1); returns true when a wait gave up
-    // cs / csp: the stage of plane i / i-1 (literals in the unrolled forward
-    // loop, so every shared-memory address there is a constant offset)
-    auto plane = [&](const int q0, const int q1, const int q2, const int cs, const int csp) -> bool {
+    // cs / csp: the stage of plane i / i-1 (literals in the unrolled loops,
+    // so every shared-memory address there is a constant offset); kind: a
+    // PlaneKind, what the iteration runs
+    auto plane = [&](auto kind, const int q0, const int q1, const int q2, const int cs, const int csp) -> bool {
+        constexpr int PA = decltype(kind)::PA;
+        constexpr int PB = decltype(kind)::PB;
         float(&um)[4] = U[q0];
         float(&up)[4] = U[q2];
         float& qm_ = Qq[q0];
@@ -1058,17 +1094,24 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
         if (has_ring) qp_ = st_cur(cs)[tq];
         float cnow[4] = {0, 0, 0, 0};
         int irx = -1;
-        if (i >= 2) {
+        const bool runA = PA == A_RT ? i >= 2 : PA != A_NONE;
+        const bool runB = PB == B_RT ? i >= 4 : PB == B_ON;
+        if (runA) {
             // sub-step A on plane i-1 (interior x = xa - 3 + i); it writes the
             // ring buffer of plane i-1, which no thread reads before the
             // barrier that ends this iteration
             const int x = xa - 3 + i;
-            const bool xin = x >= 0 && x < a.nx;
-            const bool own = x >= xa && x < xb;  // this chunk's plane: sampling, snapshots, max
+            const bool xin = PA == A_OWN || (x >= 0 && x < a.nx);
+            // this chunk's plane: sampling, snapshots, maxima
+            const bool own = PA == A_OWN || (PA == A_RT && x >= xa && x < xb);
             const int dx = min(x, a.nx - 1 - x);
-            if (any_rec && xin) irx = rec_line(x, a.rx0, a.rsx, a.rnx);
-            const int irx_a = (BACK ? a.force_row : a.seis_row) ? irx : -1;  // step t's receivers
-            const bool inj_a = inj && (a.inj_steps & 1) && x == a.inj_x;
+            int irx_a = -1;  // receiver column of step t's receivers
+            bool inj_a = false;
+            if (special) {
+                if (any_rec && xin) irx = rec_line(x, a.rx0, a.rsx, a.rnx);
+                irx_a = (BACK ? a.force_row : a.seis_row) ? irx : -1;
+                inj_a = inj && (a.inj_steps & 1) && x == a.inj_x;
+            }
             const float* T = st_cur(csp);
             const float* P = st_prev(csp);
             const float* Cc = st_c(csp);
@@ -1083,26 +1126,35 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                 ld4(T + tcen - W, ym);
                 ld4(T + tcen + W, yp);
                 sponge4f(Dx, Dc, D);
-                const bool rc = irx_a >= 0 && iry_c >= 0;
+                update4<GINL>(a, c0, pv, um, up, ym, yp, T[tcen - 1], T[tcen + 4], cnow, D, lp, &fired);
+                const bool rc = special && irx_a >= 0 && iry_c >= 0;
                 const int q = rc ? irx_a * a.rny + iry_c : 0;
-                adj_update4(a, c0, pv, um, up, ym, yp, T[tcen - 1], T[tcen + 4], cnow, D, a.force_row, q,
-                            BACK && rc ? rk : -1, lp, &fired);
-                if constexpr (FWD) {
-                    if (own && rc) {
+                if constexpr (BACK) {
+                    if (rc) {
 #pragma unroll
                         for (int k = 0; k < 4; ++k)
-                            if (k == rk) a.seis_row[q] = lp[k];
+                            if (k == rk) lp[k] = fmaf(cnow[k], a.force_row[q], lp[k]);
                     }
-                    if (inj_a) {
+                }
+                stable_damp4(a, D, lp);
+                if constexpr (FWD) {
+                    if (special) {
+                        if (own && rc) {
 #pragma unroll
-                        for (int k = 0; k < 4; ++k)
-                            if (k == inj_kc) lp[k] += a.inj_val;
+                            for (int k = 0; k < 4; ++k)
+                                if (k == rk) a.seis_row[q] = lp[k];
+                        }
+                        if (inj_a) {
+#pragma unroll
+                            for (int k = 0; k < 4; ++k)
+                                if (k == inj_kc) lp[k] += a.inj_val;
+                        }
                     }
                     if constexpr (SNAPS) {
                         if (own) {
                             // plane x = xa - 3 + i: one plane past sub-step B's (cb),
                             // except at i = 3 where both name the chunk's first plane
-                            const long long cbA = cb + (i >= 4 ? cplane : 0);
+                            const long long cbA = cb + (runB ? cplane : 0);
                             float qv[4];
 #pragma unroll
                             for (int k = 0; k < 4; ++k) {
@@ -1129,15 +1181,17 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                     const float ym = T[tq - W], yp = T[tq + W], zm = T[tq - 1], zp = T[tq + 1];
                     res = update_fast(u, upd, qm_, qp_, ym, yp, zm, zp, c, a.ax, a.ay, a.az);
                     if (!(fabsf(res) <= a.amp))
-                        res = update_guarded(u, upd, qm_, qp_, ym, yp, zm, zp, c, a.ax, a.ay, a.az, a.amp, &fired);
-                    if (BACK && irx_a >= 0 && iry_q >= 0) res = fmaf(c, a.force_row[irx_a * a.rny + iry_q], res);
+                        res = update_guarded<GINL>(u, upd, qm_, qp_, ym, yp, zm, zp, c, a.ax, a.ay, a.az, a.amp,
+                                                   &fired);
+                    if (BACK && special && irx_a >= 0 && iry_q >= 0)
+                        res = fmaf(c, a.force_row[irx_a * a.rny + iry_q], res);
                     if (a.stable_sponge) res *= D;
-                    if (FWD && inj_a && inj_q) res += a.inj_val;
+                    if (FWD && special && inj_a && inj_q) res += a.inj_val;
                 }
                 Lw[rq] = res;
             }
         }
-        if (i >= 4 && cin) {
+        if (runB && cin) {
             // sub-step B and the stores on plane i-2 (interior x = xa - 4 + i),
             // from the ring buffer of plane i-2 (complete since the last barrier)
             const int x = xa - 4 + i;
@@ -1147,21 +1201,30 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
             ld4(Lr + rcen - W, ym);
             ld4(Lr + rcen + W, yp);
             sponge4f(x_factor(dx), Dc, D);
+            update4<GINL>(a, l0, um, lm, lp, ym, yp, Lr[rcen - 1], Lr[rcen + 4], cprev, D, res, &fired);
             const float* rows2 = BACK ? a.force_row2 : a.seis_row2;
-            const bool rc = rows2 && irx_prev >= 0 && iry_c >= 0;
+            const bool rc = special && rows2 && irx_prev >= 0 && iry_c >= 0;
             const int q = rc ? irx_prev * a.rny + iry_c : 0;
-            adj_update4(a, l0, um, lm, lp, ym, yp, Lr[rcen - 1], Lr[rcen + 4], cprev, D, a.force_row2, q,
-                        BACK && rc ? rk : -1, res, &fired);
-            if constexpr (FWD) {
+            if constexpr (BACK) {
                 if (rc) {
 #pragma unroll
                     for (int k = 0; k < 4; ++k)
-                        if (k == rk) a.seis_row2[q] = res[k];
+                        if (k == rk) res[k] = fmaf(cprev[k], a.force_row2[q], res[k]);
                 }
-                if (inj && (a.inj_steps & 2) && x == a.inj_x) {
+            }
+            stable_damp4(a, D, res);
+            if constexpr (FWD) {
+                if (special) {
+                    if (rc) {
 #pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        if (k == inj_kc) res[k] += a.inj_val2;
+                        for (int k = 0; k < 4; ++k)
+                            if (k == rk) a.seis_row2[q] = res[k];
+                    }
+                    if (inj && (a.inj_steps & 2) && x == a.inj_x) {
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if (k == inj_kc) res[k] += a.inj_val2;
+                    }
                 }
                 if constexpr (SNAPS) {
 #pragma unroll
@@ -1227,32 +1290,93 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
             s = 0;
             parity ^= 1u;
         }
-        if (i >= 4) {
+        if (runB) {
             ob += a.plane;
             cb += cplane;
         }
         // every thread is done with the slot of plane i-1 and the ring buffer
         // of plane i-2: refill the one, let the next iteration overwrite the other
         if (__syncthreads_or(timed_out)) return true;
-        if (tid == 0 && i >= 1 && issued < nplanes) issue(issued++);
+        const bool refill = (PA == A_RT || PA == A_NONE) ? i >= 1 : true;
+        if (tid == 0 && refill && issued < nplanes) issue(issued++);
         return false;
     };
-    // The forward and imaging modes unroll the plane loop three times (the
-    // imaging mode measured 1% faster so since its ring work shrank); the
-    // gradient mode keeps one copy of its larger body and rotates the slots.
     if constexpr (FWD || MODE == MODE_ADJ) {
+        // The forward and imaging modes name every queue slot and stage by a
+        // literal: the first four planes one by one, the planes where both
+        // sub-steps run in a loop unrolled three times (the x-queues have
+        // period 3 and rotate by renaming), then the last plane with its
+        // queues moved to slots 0-2 and the stages from s / sp.
         static_assert(STAGES == 3, "the unrolled loop names the stages of a 3-deep ring");
-        while (i < nplanes) {
-            if (plane(0, 1, 2, 0, 2)) break;
-            if (++i == nplanes) break;
-            if (plane(1, 2, 0, 1, 0)) break;
-            if (++i == nplanes) break;
-            if (plane(2, 0, 1, 2, 1)) break;
+        using KFill = PlaneKind<A_NONE, B_NONE>;
+        using KHalo = PlaneKind<A_EDGE, B_NONE>;
+        using KFirst = PlaneKind<A_OWN, B_NONE>;
+        using KBoth = PlaneKind<A_OWN, B_ON>;
+        using KLast = PlaneKind<A_EDGE, B_ON>;
+        const int last = nplanes - 1;  // >= 4: a chunk holds at least one plane
+        bool stop = plane(KFill{}, 0, 1, 2, 0, 2);
+        if (!stop) {
             ++i;
+            stop = plane(KFill{}, 1, 2, 0, 1, 0);
+        }
+        if (!stop) {
+            ++i;
+            stop = plane(KHalo{}, 2, 0, 1, 2, 1);
+        }
+        if (!stop) {
+            ++i;
+            stop = plane(KFirst{}, 0, 1, 2, 0, 2);
+        }
+        if (!stop) {
+            ++i;
+            int ph = 1;  // i % 3 at i = 4
+            while (i < last) {
+                if ((stop = plane(KBoth{}, 1, 2, 0, 1, 0)) || ++i == last) {
+                    ph = 2;
+                    break;
+                }
+                if ((stop = plane(KBoth{}, 2, 0, 1, 2, 1)) || ++i == last) {
+                    ph = 0;
+                    break;
+                }
+                if ((stop = plane(KBoth{}, 0, 1, 2, 0, 2)) || ++i == last) {
+                    ph = 1;
+                    break;
+                }
+            }
+            if (!stop) {
+                // slots (p, p+1) of phase p hold planes i-2, i-1: move them to (0, 1)
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if (ph == 1) {
+                        U[0][k] = U[1][k];
+                        U[1][k] = U[2][k];
+                        Lq[0][k] = Lq[1][k];
+                        Lq[1][k] = Lq[2][k];
+                    } else if (ph == 2) {
+                        const float tu = U[0][k], tl = Lq[0][k];
+                        U[0][k] = U[2][k];
+                        U[1][k] = tu;
+                        Lq[0][k] = Lq[2][k];
+                        Lq[1][k] = tl;
+                    }
+                }
+                if (ph == 1) {
+                    Qq[0] = Qq[1];
+                    Qq[1] = Qq[2];
+                } else if (ph == 2) {
+                    const float tq_ = Qq[0];
+                    Qq[0] = Qq[2];
+                    Qq[1] = tq_;
+                }
+                if (!plane(KLast{}, 0, 1, 2, s, sp)) ++i;
+            }
         }
     } else {
+        // the gradient mode keeps one copy of its larger body and rotates the slots
+        using KRun = PlaneKind<A_RT, B_RT>;
         while (i < nplanes) {
-            if (plane(0, 1, 2, s, sp)) break;
+            if (plane(KRun{}, 0, 1, 2, s, sp)) break;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 U[0][k] = U[1][k];
