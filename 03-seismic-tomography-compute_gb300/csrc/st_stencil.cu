@@ -1120,8 +1120,9 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
             // centre
             ld4(Cc + rcen, cnow);
             if (xin && cin) {
-                float c0[4], pv[4], ym[4], yp[4], D[4];
-                ld4(T + tcen, c0);
+                // the centre values of plane i-1: the queue slot loaded one iteration ago
+                const float(&c0)[4] = U[q1];
+                float pv[4], ym[4], yp[4], D[4];
                 ld4(P + rcen, pv);
                 ld4(T + tcen - W, ym);
                 ld4(T + tcen + W, yp);
@@ -1176,7 +1177,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                 float res = 0.0f;
                 if (xin && ringin) {
                     const float D = fminf(Dx, Dq);
-                    const float u = T[tq], c = Cc[rq];
+                    const float u = Qq[q1], c = Cc[rq];  // u: loaded one iteration ago
                     const float upd = D * P[rq];
                     const float ym = T[tq - W], yp = T[tq + W], zm = T[tq - 1], zp = T[tq + 1];
                     res = update_fast(u, upd, qm_, qp_, ym, yp, zm, zp, c, a.ax, a.ay, a.az);
