@@ -772,7 +772,9 @@ struct Geo2 {
     static constexpr int TX_FIELDS = CUR_BYTES + 2 * RING_BYTES;
     static constexpr int TX_SNAPS = 2 * SNAP_TILE;         // the two snapshot tiles
     static constexpr int TX_ACC = (IMG ? 2 : 1) * CTR;     // image + illumination, or gradient
-    static constexpr int STAGES = 3;
+    // the forward stage is small enough for a fourth slot at two CTAs per SM:
+    // two planes in flight instead of one
+    static constexpr int STAGES = MODE == MODE_FWD ? 4 : 3;
     static constexpr int SMEM = STAGES * STAGE_BYTES + 2 * RING_PAD + EXTRA_BYTES;
     static constexpr int FIT = SM_SMEM / (SMEM + 1024);
     // two resident CTAs per SM: the forward mode would fit three in shared
@@ -1308,39 +1310,40 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
         // sub-steps run in a loop unrolled three times (the x-queues have
         // period 3 and rotate by renaming), then the last plane with its
         // queues moved to slots 0-2 and the stages from s / sp.
-        static_assert(STAGES == 3, "the unrolled loop names the stages of a 3-deep ring");
+        // (with a 4-deep ring the stages come from s / sp: the queue period is 3)
+        constexpr bool LIT = STAGES == 3;
         using KFill = PlaneKind<A_NONE, B_NONE>;
         using KHalo = PlaneKind<A_EDGE, B_NONE>;
         using KFirst = PlaneKind<A_OWN, B_NONE>;
         using KBoth = PlaneKind<A_OWN, B_ON>;
         using KLast = PlaneKind<A_EDGE, B_ON>;
         const int last = nplanes - 1;  // >= 4: a chunk holds at least one plane
-        bool stop = plane(KFill{}, 0, 1, 2, 0, 2);
+        bool stop = plane(KFill{}, 0, 1, 2, LIT ? 0 : s, LIT ? 2 : sp);
         if (!stop) {
             ++i;
-            stop = plane(KFill{}, 1, 2, 0, 1, 0);
+            stop = plane(KFill{}, 1, 2, 0, LIT ? 1 : s, LIT ? 0 : sp);
         }
         if (!stop) {
             ++i;
-            stop = plane(KHalo{}, 2, 0, 1, 2, 1);
+            stop = plane(KHalo{}, 2, 0, 1, LIT ? 2 : s, LIT ? 1 : sp);
         }
         if (!stop) {
             ++i;
-            stop = plane(KFirst{}, 0, 1, 2, 0, 2);
+            stop = plane(KFirst{}, 0, 1, 2, LIT ? 0 : s, LIT ? 2 : sp);
         }
         if (!stop) {
             ++i;
             int ph = 1;  // i % 3 at i = 4
             while (i < last) {
-                if ((stop = plane(KBoth{}, 1, 2, 0, 1, 0)) || ++i == last) {
+                if ((stop = plane(KBoth{}, 1, 2, 0, LIT ? 1 : s, LIT ? 0 : sp)) || ++i == last) {
                     ph = 2;
                     break;
                 }
-                if ((stop = plane(KBoth{}, 2, 0, 1, 2, 1)) || ++i == last) {
+                if ((stop = plane(KBoth{}, 2, 0, 1, LIT ? 2 : s, LIT ? 1 : sp)) || ++i == last) {
                     ph = 0;
                     break;
                 }
-                if ((stop = plane(KBoth{}, 0, 1, 2, 0, 2)) || ++i == last) {
+                if ((stop = plane(KBoth{}, 0, 1, 2, LIT ? 0 : s, LIT ? 2 : sp)) || ++i == last) {
                     ph = 1;
                     break;
                 }
