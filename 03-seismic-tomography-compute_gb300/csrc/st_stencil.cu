@@ -791,11 +791,6 @@ __device__ __forceinline__ int rec_line(int v, int v0, int sv, int nv) {
     return d / sv < nv ? d / sv : -1;
 }
 
-// Sponge factor for distance d >= 0 to the nearest face.
-__device__ __forceinline__ float sponge_tab(const StepArgs& a, const float* dtab, int d) {
-    return d < a.sw ? dtab[d] : 1.0f;
-}
-
 __device__ __forceinline__ void ld4(const float* p, float v[4]) { f4_to(*reinterpret_cast<const float4*>(p), v); }
 __device__ __forceinline__ void st4(float* p, const float v[4]) {
     *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
@@ -1106,6 +1101,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
             const bool xin = PA == A_OWN || (x >= 0 && x < a.nx);
             // this chunk's plane: sampling, snapshots, maxima
             const bool own = PA == A_OWN || (PA == A_RT && x >= xa && x < xb);
+            (void)own;  // read by the forward mode only
             const int dx = min(x, a.nx - 1 - x);
             int irx_a = -1;  // receiver column of step t's receivers
             bool inj_a = false;
