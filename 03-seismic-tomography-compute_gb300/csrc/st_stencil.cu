@@ -772,14 +772,16 @@ struct Geo2 {
     static constexpr int TX_FIELDS = CUR_BYTES + 2 * RING_BYTES;
     static constexpr int TX_SNAPS = 2 * SNAP_TILE;         // the two snapshot tiles
     static constexpr int TX_ACC = (IMG ? 2 : 1) * CTR;     // image + illumination, or gradient
-    // the forward stage is small enough for a fourth slot at two CTAs per SM:
-    // two planes in flight instead of one
-    static constexpr int STAGES = MODE == MODE_FWD ? 4 : 3;
+    // the forward stage is small enough for five slots at two CTAs per SM:
+    // three planes in flight instead of one (256^3: 0.0901 ms with 3 stages,
+    // 0.0827 with 4, 0.0820 with 5, 0.0826 with 6). The imaging mode's
+    // stage fits three; a fourth, with its imaging tiles in a ring of three
+    // slots of their own, measured slower (0.1380 against 0.1283 ms).
+    static constexpr int STAGES = MODE == MODE_FWD ? 5 : 3;
     static constexpr int SMEM = STAGES * STAGE_BYTES + 2 * RING_PAD + EXTRA_BYTES;
     static constexpr int FIT = SM_SMEM / (SMEM + 1024);
-    // two resident CTAs per SM: the forward mode would fit three in shared
-    // memory, but capped at 80 registers it spilled and measured 0.080 against
-    // 0.060 ms per step at 256^3
+    // two resident CTAs per SM: three (80 registers) spilled in the forward
+    // mode and measured 0.1009 against 0.0941 ms per pair at 256^3 (3 stages)
     static constexpr int MINB = FIT < 2 ? FIT : 2;
 };
 
@@ -1306,7 +1308,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
         // sub-steps run in a loop unrolled three times (the x-queues have
         // period 3 and rotate by renaming), then the last plane with its
         // queues moved to slots 0-2 and the stages from s / sp.
-        // (with a 4-deep ring the stages come from s / sp: the queue period is 3)
+        // (with a deeper ring the stages come from s / sp: the queue period is 3)
         constexpr bool LIT = STAGES == 3;
         using KFill = PlaneKind<A_NONE, B_NONE>;
         using KHalo = PlaneKind<A_EDGE, B_NONE>;
