@@ -200,8 +200,8 @@ __device__ __forceinline__ float update_fast(float u, float upd, float xm, float
 // the fast result is non-finite or beyond the amplitude limit. A non-finite
 // input always makes the fast result non-finite (c, 1/d^2 > 0), so the fast
 // path is exact whenever it is taken. GINL: inlined at the call site (the
-// two-step forward and imaging kernels measured faster so, with fewer
-// registers); otherwise one out-of-line copy shared by the call sites.
+// two-step kernels measured faster so); otherwise one out-of-line copy
+// shared by the call sites.
 template <bool GINL = false>
 __device__ __forceinline__ float update_guarded(float u, float upd, float xm, float xp, float ym, float yp, float zm,
                                                 float zp, float c, float ax, float ay, float az, float amp,
@@ -363,10 +363,10 @@ __device__ __forceinline__ void process_row(const StepArgs& a, const RowCtx& R, 
             float g[4];
             f4_to(acc0, g);
 #pragma unroll
-            for (int k = 0; k < 4; ++k) g[k] = fmaf(u0[k] / cv[k], fin[k], g[k]);
+            for (int k = 0; k < 4; ++k) g[k] = fmaf(__fdividef(u0[k], cv[k]), fin[k], g[k]);
             *reinterpret_cast<float4*>(a.grad + cbase) = make_float4(g[0], g[1], g[2], g[3]);
         } else {
-            for (int k = 0; k < zvalid; ++k) a.grad[cbase + k] += (u0[k] / cv[k]) * fin[k];
+            for (int k = 0; k < zvalid; ++k) a.grad[cbase + k] += __fdividef(u0[k], cv[k]) * fin[k];
         }
     }
 }
@@ -867,13 +867,12 @@ __device__ __forceinline__ void snap_lap4(const unsigned char* S, const unsigned
 }
 
 // What one iteration of fd_step2_kernel's plane loop runs, fixed at compile
-// time where the loop position fixes it. Sub-step A: A_RT (decided from the
-// plane index, for the gradient's rolled loop), A_NONE (the first two planes),
+// time by the loop position. Sub-step A: A_NONE (the first two planes),
 // A_EDGE (a halo plane beside the chunk: the grid test at run time, no
 // sampling, snapshots or maxima), A_OWN (a plane of the chunk). Sub-step B:
-// B_RT (from the plane index), B_NONE (the first four planes), B_ON.
-enum : int { A_RT, A_NONE, A_EDGE, A_OWN };
-enum : int { B_RT, B_NONE, B_ON };
+// B_NONE (the first four planes), B_ON.
+enum : int { A_NONE, A_EDGE, A_OWN };
+enum : int { B_NONE, B_ON };
 template <int PA_, int PB_>
 struct PlaneKind {
     static constexpr int PA = PA_, PB = PB_;
@@ -891,7 +890,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
     constexpr bool FWD = MODE == MODE_FWD;
     constexpr bool BACK = !FWD;                // receiver forcing, snapshots read
     constexpr bool SNAPS = FWD && SK != SNAP_NONE;
-    constexpr bool GINL = !GRD;                // the guarded update inlined (not in the larger gradient body)
+    constexpr bool GINL = true;                // the guarded update inlined
     constexpr int W = G::W;
     constexpr int STAGES = G::STAGES;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -1093,8 +1092,8 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
         if (has_ring) qp_ = st_cur(cs)[tq];
         float cnow[4] = {0, 0, 0, 0};
         int irx = -1;
-        const bool runA = PA == A_RT ? i >= 2 : PA != A_NONE;
-        const bool runB = PB == B_RT ? i >= 4 : PB == B_ON;
+        constexpr bool runA = PA != A_NONE;
+        constexpr bool runB = PB == B_ON;
         if (runA) {
             // sub-step A on plane i-1 (interior x = xa - 3 + i); it writes the
             // ring buffer of plane i-1, which no thread reads before the
@@ -1102,7 +1101,7 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
             const int x = xa - 3 + i;
             const bool xin = PA == A_OWN || (x >= 0 && x < a.nx);
             // this chunk's plane: sampling, snapshots, maxima
-            const bool own = PA == A_OWN || (PA == A_RT && x >= xa && x < xb);
+            const bool own = PA == A_OWN;
             (void)own;  // read by the forward mode only
             const int dx = min(x, a.nx - 1 - x);
             int irx_a = -1;  // receiver column of step t's receivers
@@ -1270,8 +1269,8 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                 ld4(st_img(csp) + ccen, g);
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    g[k] = fmaf(um[k] / cprev[k], fa[k], g[k]);
-                    g[k] = fmaf(l0[k] / cprev[k], fb[k], g[k]);
+                    g[k] = fmaf(__fdividef(um[k], cprev[k]), fa[k], g[k]);
+                    g[k] = fmaf(__fdividef(l0[k], cprev[k]), fb[k], g[k]);
                 }
                 st4(a.grad + cb, g);
             }
@@ -1298,17 +1297,17 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
         // every thread is done with the slot of plane i-1 and the ring buffer
         // of plane i-2: refill the one, let the next iteration overwrite the other
         if (__syncthreads_or(timed_out)) return true;
-        const bool refill = (PA == A_RT || PA == A_NONE) ? i >= 1 : true;
+        const bool refill = PA == A_NONE ? i >= 1 : true;
         if (tid == 0 && refill && issued < nplanes) issue(issued++);
         return false;
     };
-    if constexpr (FWD || MODE == MODE_ADJ) {
-        // The forward and imaging modes name every queue slot and stage by a
-        // literal: the first four planes one by one, the planes where both
+    {
+        // Every queue slot (and, with a 3-deep ring, every stage) is named by
+        // a literal: the first four planes one by one, the planes where both
         // sub-steps run in a loop unrolled three times (the x-queues have
         // period 3 and rotate by renaming), then the last plane with its
-        // queues moved to slots 0-2 and the stages from s / sp.
-        // (with a deeper ring the stages come from s / sp: the queue period is 3)
+        // queues moved to slots 0-2 and the stages from s / sp. A deeper ring
+        // takes its stages from s / sp throughout.
         constexpr bool LIT = STAGES == 3;
         using KFill = PlaneKind<A_NONE, B_NONE>;
         using KHalo = PlaneKind<A_EDGE, B_NONE>;
@@ -1373,25 +1372,6 @@ __global__ void __launch_bounds__(NTHREADS, (Geo2<MODE, SK>::MINB))
                 }
                 if (!plane(KLast{}, 0, 1, 2, s, sp)) ++i;
             }
-        }
-    } else {
-        // the gradient mode keeps one copy of its larger body and rotates the slots
-        using KRun = PlaneKind<A_RT, B_RT>;
-        while (i < nplanes) {
-            if (plane(KRun{}, 0, 1, 2, s, sp)) break;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                U[0][k] = U[1][k];
-                U[1][k] = U[2][k];
-                Lq[0][k] = Lq[1][k];
-                Lq[1][k] = Lq[2][k];
-            }
-            // the ring queue only in the threads that own a ring point
-            if (has_ring) {
-                Qq[0] = Qq[1];
-                Qq[1] = Qq[2];
-            }
-            ++i;
         }
     }
 
