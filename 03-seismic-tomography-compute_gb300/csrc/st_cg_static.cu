@@ -28,8 +28,9 @@ constexpr long long kMaxN = ST_CG_STATIC_MAX_N;
 
 // Five work vectors (r, z, p, q = A p, Jacobi diagonal) of kMaxN floats each,
 // followed by the FP64 scalar block. Shared by every call on a device.
-static __device__ __align__(256) float g_cg_scratch[5 * kMaxN + 64];
-static_assert(sizeof(stg::CgScalars) <= 64 * sizeof(float), "CG scalar block does not fit the scratch tail");
+constexpr int kTail = 256;
+static __device__ __align__(256) float g_cg_scratch[5 * kMaxN + kTail];
+static_assert(sizeof(stg::CgScalars) <= kTail * sizeof(float), "CG scalar block does not fit the scratch tail");
 
 std::mutex g_mu;
 float* g_scratch_ptr[64] = {nullptr};  // device address of g_cg_scratch, per device

@@ -427,10 +427,13 @@ int st_normal_cg_device(st_csr* m, const float* d, double lam, int max_iter, dou
     W.t = sc.get<float>((size_t)rows);
     W.sc = sc.get<CgScalars>(1);
     float* b = rhs ? rhs : sc.get<float>((size_t)n);
-    float* dinv = jacobi ? sc.get<float>((size_t)n) : nullptr;
-    ST_ALLOC(W.r && W.z && W.p && W.q && W.t && W.sc && b && (!jacobi || dinv));
+    const bool use_jacobi = (jacobi & ST_CG_JACOBI) != 0;
+    const bool confirm = (jacobi & ST_CG_CONFIRM_TRUE) != 0;
+    float* dinv = use_jacobi ? sc.get<float>((size_t)n) : nullptr;
+    float* res = sc.get<float>((size_t)n);
+    ST_ALLOC(W.r && W.z && W.p && W.q && W.t && W.sc && b && (!use_jacobi || dinv) && res);
     if (d) ST_TRY(launch_spmv(m->AT, d, b, nullptr, 0.0f, nullptr, nullptr, nullptr, m->stream));
-    if (jacobi) ST_TRY(launch_normal_jacobi(m->AT, lam, dinv, m->stream));
+    if (use_jacobi) ST_TRY(launch_normal_jacobi(m->AT, lam, dinv, m->stream));
     CgProblem P;
     P.A = &m->A;
     P.AT = &m->AT;
@@ -442,18 +445,33 @@ int st_normal_cg_device(st_csr* m, const float* d, double lam, int max_iter, dou
     CgResult R;
     ST_TRY(run_cg(P, W, max_iter, tol, 16, &R, m->stream));
     if (R.iters == 0) ST_CUDA(cudaMemsetAsync(x, 0, (size_t)std::max<long long>(n, 1) * 4, m->stream));
-    if (true_rel) {
-        // ||A^T d - (A^T A + lam I) x|| / ||A^T d|| in FP64
+    // ||A^T d - (A^T A + lam I) x|| / ||A^T d|| in FP64 (t and q are rewritten by every iteration)
+    auto residual = [&](double* out) -> int {
         ST_TRY(launch_spmv(m->A, x, W.t, nullptr, 0.0f, nullptr, nullptr, nullptr, m->stream));
         ST_TRY(launch_spmv(m->AT, W.t, W.q, x, (float)lam, nullptr, nullptr, nullptr, m->stream));
-        ST_TRY(launch_residual(W.r, b, W.q, n, m->stream));
-        ST_TRY(launch_sumsq(W.r, n, m->dacc, m->stream));
+        ST_TRY(launch_residual(res, b, W.q, n, m->stream));
+        ST_TRY(launch_sumsq(res, n, m->dacc, m->stream));
         ST_TRY(launch_sumsq(b, n, m->dacc + 1, m->stream));
         double h[2];
         ST_CUDA(cudaMemcpyAsync(h, m->dacc, 16, cudaMemcpyDeviceToHost, m->stream));
         ST_CUDA(cudaStreamSynchronize(m->stream));
-        *true_rel = h[1] > 0 ? std::sqrt(h[0] / h[1]) : 0.0;
+        *out = h[1] > 0 ? std::sqrt(h[0] / h[1]) : 0.0;
+        return ST_OK;
+    };
+    // With ST_CG_CONFIRM_TRUE the stop is confirmed on the true residual: the
+    // FP32 recurrence residual drifts from it, so while the true one is above
+    // tol the solve continues (same Krylov state) to a recurrence target
+    // scaled by their ratio, a few times at most.
+    double tr = 0.0;
+    if (confirm || true_rel) ST_TRY(residual(&tr));
+    for (int round = 0; confirm && round < 4 && tr > tol && !R.breakdown && R.iters > 0 && R.iters < max_iter &&
+                        R.rel < tol;
+         ++round) {
+        const double target = R.rel * (tol / tr) * 0.98;
+        ST_TRY(resume_cg(P, W, max_iter, target, 16, &R, m->stream));
+        ST_TRY(residual(&tr));
     }
+    if (true_rel) *true_rel = tr;
     ST_CUDA(cudaStreamSynchronize(m->stream));
     if (iters) *iters = R.iters;
     if (final_rel) *final_rel = R.rel;

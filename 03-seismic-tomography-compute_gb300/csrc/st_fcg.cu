@@ -19,8 +19,10 @@ extern "C" int st_pcnet_apply(st_pcnet* p, const float* r, const float* dinv, fl
 namespace stg {
 namespace {
 
+// Four CTAs per SM: each thread takes a few elements, so that the per-thread
+// FP64 sums and block reductions (a slow pipe on this GPU) stay small.
 unsigned fcg_blocks(long long n) {
-    return (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152LL * 8));
+    return (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152LL * 4));
 }
 
 __device__ __forceinline__ void block_sum3(double a, double b, double c, double* da, double* db, double* dc) {
@@ -64,8 +66,13 @@ __global__ void fcg_dots_pq(const float* __restrict__ p, const float* __restrict
 // x += alpha p, r -= alpha q, rr = r.r
 __global__ void fcg_update(float* __restrict__ x, float* __restrict__ r, const float* __restrict__ p,
                            const float* __restrict__ q, long long n, FcgScalars* s) {
-    const double pq = s->pq;
-    const float alpha = pq != 0.0 ? (float)(s->pr / pq) : 0.0f;
+    __shared__ float s_alpha;  // formed once per block
+    if (threadIdx.x == 0) {
+        const double pq = s->pq;
+        s_alpha = pq != 0.0 ? (float)(s->pr / pq) : 0.0f;
+    }
+    __syncthreads();
+    const float alpha = s_alpha;
     double a = 0.0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         x[i] = fmaf(alpha, p[i], x[i]);
@@ -91,9 +98,17 @@ __global__ void fcg_dots_z(const float* __restrict__ z, const float* __restrict_
 // p = z - beta p (z replaced by dinv r when it is not a descent direction)
 __global__ void fcg_pupdate(float* __restrict__ p, const float* __restrict__ z, const float* __restrict__ r,
                             const float* __restrict__ dinv, long long n, const FcgScalars* s, int first) {
-    const bool use_z = s->zr > 0.0;
-    const double pq = s->pq;
-    const float beta = first || pq == 0.0 ? 0.0f : (float)((use_z ? s->zq : s->jq) / pq);
+    __shared__ float s_beta;  // formed once per block
+    __shared__ int s_use_z;
+    if (threadIdx.x == 0) {
+        const bool uz = s->zr > 0.0;
+        const double pq = s->pq;
+        s_beta = first || pq == 0.0 ? 0.0f : (float)((uz ? s->zq : s->jq) / pq);
+        s_use_z = uz;
+    }
+    __syncthreads();
+    const bool use_z = s_use_z;
+    const float beta = s_beta;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float zi = use_z ? z[i] : dinv[i] * r[i];
         p[i] = first ? zi : fmaf(-beta, p[i], zi);

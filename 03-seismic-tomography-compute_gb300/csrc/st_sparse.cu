@@ -45,6 +45,13 @@ unsigned blocks_for(long long work, int threads = 256) {
     return (unsigned)std::max<long long>(1, std::min<long long>(b, grid_cap()));
 }
 
+// The CG vector kernels: four CTAs per SM (each thread a few elements), so
+// that their per-thread FP64 partial sums and block reductions stay small.
+unsigned cg_blocks(long long work) {
+    long long b = (work + 255) / 256;
+    return (unsigned)std::max<long long>(1, std::min<long long>(b, grid_cap() / 4));
+}
+
 // ---------------------------------------------------------------- builder kernels
 template <class TI>
 __global__ void keys_kernel(const TI* __restrict__ r, const TI* __restrict__ c, long long n, long long R, long long Cc,
@@ -148,8 +155,14 @@ __global__ void fill_last_kernel(long long* rp, long long R, const long long* to
 // y[row] = sum val*x[col] with G threads per row (FP32 accumulation, a
 // G-way strided partial sum per row reduced by shuffles), optional
 // y += add_scale * add and FP64 accumulation of dot(pdot, y).
-template <int G>
-__global__ void __launch_bounds__(256) spmv_kernel(const long long* __restrict__ rp, const int* __restrict__ col,
+// Each lane first loads the column and value of up to K of its row's entries
+// (coalesced), then issues all K gathers of x before it sums: the gathers,
+// which wait on L2, are all in flight at once (the rest of a longer row
+// follows in a loop). PF: the group pulls the columns and values of the row
+// it takes two rows on into L2. Resident CTAs per SM are pinned (six at 40
+// registers, five at 48 for the 10-entry variant): the gathers need the warps.
+template <int G, int K, bool PF>
+__global__ void __launch_bounds__(256, K >= 10 ? 5 : 6) spmv_kernel(const long long* __restrict__ rp, const int* __restrict__ col,
                                                    const float* __restrict__ val, const float* __restrict__ x,
                                                    float* __restrict__ y, long long rows, const float* __restrict__ add,
                                                    float add_scale, const float* __restrict__ pdot,
@@ -164,16 +177,13 @@ __global__ void __launch_bounds__(256) spmv_kernel(const long long* __restrict__
     // full-warp shuffles below always see all 32 lanes
     const long long gfirst = (blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31u)) / G;
     double local = 0.0;
-    constexpr long long PF = 2;  // rows ahead (measured: 1 -> 1.67 ms, 2 -> 1.57, 3 -> 1.61 for A x + A^T y)
+    constexpr long long PFR = 2;  // rows ahead
     for (long long it = 0; gfirst + it * stride < rows; ++it) {
         const long long row = gid + it * stride;
         const bool active = row < rows;
         const long long a = active ? rp[row] : 0, b = active ? rp[row + 1] : 0;
-        // the group's row after next: pull its columns and values into L2 now, so
-        // its loads wait on L2 rather than DRAM (one 128-byte line per lane);
-        // short rows (small G) are left to the caches
-        if (G >= 8 && active && row + PF * stride < rows) {
-            const long long na = rp[row + PF * stride], nb = rp[row + PF * stride + 1];
+        if (PF && active && row + PFR * stride < rows) {
+            const long long na = rp[row + PFR * stride], nb = rp[row + PFR * stride + 1];
             const long long l0 = na >> 5, l1 = (nb + 31) >> 5;  // 32 four-byte entries per line
             for (long long l = l0 + lane; l < l1; l += G) {
                 const long long e = l << 5;
@@ -181,21 +191,24 @@ __global__ void __launch_bounds__(256) spmv_kernel(const long long* __restrict__
                 asm volatile("prefetch.global.L2 [%0];" ::"l"(val + e));
             }
         }
-        // four independent gathers in flight per lane on long rows
-        float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
-        long long p = a + lane;
-        for (; p + 3 * G < b; p += 4 * G) {
-            const int c0 = __ldg(col + p), c1 = __ldg(col + p + G), c2 = __ldg(col + p + 2 * G),
-                      c3 = __ldg(col + p + 3 * G);
-            const float v0 = __ldg(val + p), v1 = __ldg(val + p + G), v2 = __ldg(val + p + 2 * G),
-                        v3 = __ldg(val + p + 3 * G);
-            s0 = fmaf(v0, __ldg(x + c0), s0);
-            s1 = fmaf(v1, __ldg(x + c1), s1);
-            s2 = fmaf(v2, __ldg(x + c2), s2);
-            s3 = fmaf(v3, __ldg(x + c3), s3);
+        int cs[K];
+        float vs[K], xs[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const long long e = a + lane + (long long)k * G;
+            cs[k] = e < b ? __ldg(col + e) : 0;
+            vs[k] = e < b ? __ldg(val + e) : 0.0f;
         }
-        for (; p < b; p += G) s0 = fmaf(__ldg(val + p), __ldg(x + __ldg(col + p)), s0);
-        float sum = (s0 + s1) + (s2 + s3);
+#pragma unroll
+        for (int k = 0; k < K; ++k) xs[k] = (a + lane + (long long)k * G < b) ? __ldg(x + cs[k]) : 0.0f;
+        float s0 = 0.0f, s1 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < K; k += 2) {
+            s0 = fmaf(vs[k], xs[k], s0);
+            if (k + 1 < K) s1 = fmaf(vs[k + 1], xs[k + 1], s1);
+        }
+        for (long long p = a + lane + (long long)K * G; p < b; p += G) s0 = fmaf(__ldg(val + p), __ldg(x + __ldg(col + p)), s0);
+        float sum = s0 + s1;
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(FULL, sum, o, G);
         if (lane == 0 && active) {
@@ -205,23 +218,29 @@ __global__ void __launch_bounds__(256) spmv_kernel(const long long* __restrict__
         }
     }
     if (dot_acc) {
-        for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(FULL, local, o);
+        // only the groups' first lanes hold row products: fold those of the
+        // warp (none to fold for one group per warp), then the block's warps,
+        // into one of the accumulator's CG_SLOTS addresses
+        for (int o = 16; o >= G; o >>= 1) local += __shfl_xor_sync(FULL, local, o);
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = local;
         __syncthreads();
         if (threadIdx.x == 0) {
             double t = 0.0;
             for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
-            atomicAdd(dot_acc, t);
+            atomicAdd(dot_acc + blockIdx.x % CG_SLOTS, t);
         }
     }
 }
 
-template <int G>
+template <int G, int K, bool PF>
 int launch_spmv_g(const DevCsr& A, const float* x, float* y, const float* add, float add_scale, const float* pdot,
                   double* dot_acc, const int* done, cudaStream_t st) {
-    const long long threads = A.rows * G;
-    spmv_kernel<G><<<blocks_for(threads), 256, 0, st>>>(A.row_ptr, A.col, A.val, x, y, A.rows, add, add_scale, pdot,
-                                                         dot_acc, done);
+    // up to 64 CTAs of 256 threads per SM, the rest by the grid-stride loop
+    // (measured on the 2M-ray matrix: 16 per SM 0.58 ms, 32 0.56, 64 0.54 for A x)
+    const long long b = (A.rows * G + 255) / 256;
+    const unsigned blocks = (unsigned)std::max<long long>(1, std::min<long long>(b, (long long)grid_cap() * 4));
+    spmv_kernel<G, K, PF><<<blocks, 256, 0, st>>>(A.row_ptr, A.col, A.val, x, y, A.rows, add, add_scale, pdot, dot_acc,
+                                                  done);
     count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;
@@ -237,7 +256,9 @@ __global__ void f32_to_f64_kernel(const float* a, double* b, long long n) {
         b[i] = (double)a[i];
 }
 
-__device__ __forceinline__ void block_add2(double a, double b, double* acc_a, double* acc_b) {
+// Block sums of a and b added to acc_a / acc_b; slots > 1: into slot
+// blockIdx % slots of each (the CG accumulators).
+__device__ __forceinline__ void block_add2(double a, double b, double* acc_a, double* acc_b, int slots = 1) {
     __shared__ double ra[8], rb[8];
     for (int o = 16; o > 0; o >>= 1) {
         a += __shfl_xor_sync(FULL, a, o);
@@ -254,8 +275,8 @@ __device__ __forceinline__ void block_add2(double a, double b, double* acc_a, do
             ta += ra[w];
             tb += rb[w];
         }
-        if (acc_a) atomicAdd(acc_a, ta);
-        if (acc_b) atomicAdd(acc_b, tb);
+        if (acc_a) atomicAdd(acc_a + blockIdx.x % slots, ta);
+        if (acc_b) atomicAdd(acc_b + blockIdx.x % slots, tb);
     }
 }
 
@@ -274,25 +295,38 @@ __global__ void cg_init_kernel(const float* __restrict__ b, const float* __restr
         a += (double)bi * (double)zi;
         c += (double)bi * (double)bi;
     }
-    block_add2(a, c, rz, bb);
+    block_add2(a, c, rz, bb, CG_SLOTS);
 }
 
 // x += alpha p, r -= alpha q, z = M r; acc rz_new = <r,z>, rr = <r,r>.
 // alpha = rz_old / pq; |pq| < 1e-30 stops the solve (sparse_ops.cpp:37,88).
+// The scalars are formed once per block (FP64 is a slow pipe on this GPU).
 __global__ void cg_update_kernel(long long n, float* __restrict__ x, float* __restrict__ r, float* __restrict__ z,
                                  const float* __restrict__ p, const float* __restrict__ q,
                                  const float* __restrict__ dinv, CgScalars* sc, int k) {
-    if (sc->done) return;
-    const double pq = sc->acc[k % 3].pq;
-    if (fabs(pq) < 1e-30) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            sc->done = 1;
-            sc->breakdown = 1;
+    __shared__ float s_alpha;
+    __shared__ int s_stop;
+    if (threadIdx.x == 0) {
+        int stop = sc->done;
+        float alpha = 0.0f;
+        if (!stop) {
+            const double pq = cg_slot_sum(sc->acc[k % 3].pq);
+            if (fabs(pq) < 1e-30) {
+                stop = 1;
+                if (blockIdx.x == 0) {
+                    sc->done = 1;
+                    sc->breakdown = 1;
+                }
+            } else {
+                alpha = (float)(cg_slot_sum(sc->acc[(k + 2) % 3].rzn) / pq);
+            }
         }
-        return;
+        s_alpha = alpha;
+        s_stop = stop;
     }
-    const double rz_old = sc->acc[(k + 2) % 3].rzn;
-    const float alpha = (float)(rz_old / pq);
+    __syncthreads();
+    if (s_stop) return;
+    const float alpha = s_alpha;
     double a = 0.0, c = 0.0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         x[i] = fmaf(alpha, p[i], x[i]);
@@ -303,7 +337,7 @@ __global__ void cg_update_kernel(long long n, float* __restrict__ x, float* __re
         a += (double)ri * (double)zi;
         c += (double)ri * (double)ri;
     }
-    block_add2(a, c, &sc->acc[k % 3].rzn, &sc->acc[k % 3].rr);
+    block_add2(a, c, sc->acc[k % 3].rzn, sc->acc[k % 3].rr, CG_SLOTS);
 }
 
 // Convergence test after the update (sqrt(rr)/||b|| < tol) and
@@ -311,22 +345,32 @@ __global__ void cg_update_kernel(long long n, float* __restrict__ x, float* __re
 // iteration k+1.
 __global__ void cg_pupdate_kernel(long long n, float* __restrict__ p, const float* __restrict__ z, CgScalars* sc,
                                   int k, double tol) {
-    if (sc->done) return;
-    const double rr = sc->acc[k % 3].rr;
-    const double rel = sqrt(rr) / sqrt(sc->bb);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        sc->iters = k + 1;
-        sc->rel = rel;
-        CgAcc& nxt = sc->acc[(k + 1) % 3];
-        nxt.pq = 0.0;
-        nxt.rr = 0.0;
-        nxt.rzn = 0.0;
+    __shared__ float s_beta;
+    __shared__ int s_stop;
+    if (threadIdx.x == 0) {
+        int stop = sc->done;
+        float beta = 0.0f;
+        if (!stop) {
+            const double rel = sqrt(cg_slot_sum(sc->acc[k % 3].rr)) / sqrt(cg_slot_sum(sc->bb));
+            if (blockIdx.x == 0) {
+                sc->iters = k + 1;
+                sc->rel = rel;
+                CgAcc& nxt = sc->acc[(k + 1) % 3];
+                for (int i = 0; i < CG_SLOTS; ++i) nxt.pq[i] = nxt.rr[i] = nxt.rzn[i] = 0.0;
+            }
+            if (rel < tol) {
+                stop = 1;
+                if (blockIdx.x == 0) sc->done = 1;
+            } else {
+                beta = (float)(cg_slot_sum(sc->acc[k % 3].rzn) / cg_slot_sum(sc->acc[(k + 2) % 3].rzn));
+            }
+        }
+        s_beta = beta;
+        s_stop = stop;
     }
-    if (rel < tol) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) sc->done = 1;
-        return;
-    }
-    const float beta = (float)(sc->acc[k % 3].rzn / sc->acc[(k + 2) % 3].rzn);
+    __syncthreads();
+    if (s_stop) return;
+    const float beta = s_beta;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         p[i] = fmaf(beta, p[i], z[i]);
 }
@@ -562,19 +606,20 @@ int launch_spmv(const DevCsr& A, const float* x, float* y, const float* add, flo
         return e ? std::atoi(e) : 0;
     }();
     switch (forced) {
-        case 32: return launch_spmv_g<32>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
-        case 16: return launch_spmv_g<16>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
-        case 8: return launch_spmv_g<8>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
-        case 4: return launch_spmv_g<4>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
+        case 32: return launch_spmv_g<32, 6, false>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
+        case 16: return launch_spmv_g<16, 10, true>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
+        case 8: return launch_spmv_g<8, 4, true>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
+        case 4: return launch_spmv_g<4, 4, false>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
         default: break;
     }
     // measured on the 2M-ray matrix (180 entries per row) and its transpose (360): 16 threads per
-    // row 0.67 ms against 0.77 with 32; the transpose 0.80 ms with 32 against 0.93 with 16
-    if (avg >= 256) return launch_spmv_g<32>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
-    if (avg >= 24) return launch_spmv_g<16>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
-    if (avg >= 10) return launch_spmv_g<8>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
-    if (avg >= 5) return launch_spmv_g<4>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
-    return launch_spmv_g<2>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
+    // row with 10 entries held per lane and the L2 prefetch 0.545 ms; the transpose with 32
+    // threads, 6 entries per lane and no prefetch 0.599 ms (before the held entries: 0.66 / 0.80)
+    if (avg >= 256) return launch_spmv_g<32, 6, false>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
+    if (avg >= 24) return launch_spmv_g<16, 10, true>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
+    if (avg >= 10) return launch_spmv_g<8, 4, true>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
+    if (avg >= 5) return launch_spmv_g<4, 4, false>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
+    return launch_spmv_g<2, 4, false>(A, x, y, add, add_scale, pdot, dot_acc, done, st);
 }
 
 int launch_f64_to_f32(const double* a, float* b, long long n, cudaStream_t st) {
@@ -643,13 +688,16 @@ int launch_fd_triplets(const double* vel, long long nx, long long ny, long long 
 }
 
 // ---------------------------------------------------------------- CG driver
+int cg_loop(const CgProblem& P, CgWork& W, int k0, int max_iter, double tol, int check_every, CgResult* res,
+            cudaStream_t st);
+
 int run_cg(const CgProblem& P, CgWork& W, int max_iter, double tol, int check_every, CgResult* res,
            cudaStream_t st) {
     const long long n = P.n;
     ST_CUDA(cudaMemsetAsync(W.sc, 0, sizeof(CgScalars), st));
     // iteration -1 stores rz in acc[2].rzn
-    cg_init_kernel<<<blocks_for(n), 256, 0, st>>>(P.b, P.dinv, n, P.x, W.r, P.dinv ? W.z : nullptr, W.p,
-                                                   &W.sc->acc[2].rzn, &W.sc->bb);
+    cg_init_kernel<<<cg_blocks(n), 256, 0, st>>>(P.b, P.dinv, n, P.x, W.r, P.dinv ? W.z : nullptr, W.p,
+                                                   W.sc->acc[2].rzn, W.sc->bb);
     count_launch();
     ST_CUDA(cudaGetLastError());
     CgScalars h{};
@@ -658,22 +706,44 @@ int run_cg(const CgProblem& P, CgWork& W, int max_iter, double tol, int check_ev
     res->iters = 0;
     res->rel = 0.0;
     res->breakdown = 0;
-    if (std::sqrt(h.bb) < 1e-30) return ST_OK;  // sparse_ops.cpp:22,83
+    if (std::sqrt(cg_slot_sum(h.bb)) < 1e-30) return ST_OK;  // sparse_ops.cpp:22,83
+    return cg_loop(P, W, 0, max_iter, tol, check_every, res, st);
+}
+
+int resume_cg(const CgProblem& P, CgWork& W, int max_iter, double tol, int check_every, CgResult* res,
+              cudaStream_t st) {
+    if (res->breakdown || res->iters == 0 || res->iters >= max_iter) return ST_OK;
+    // the last iteration stopped before p = z + beta p: clear the stop and
+    // run that update (a zero tolerance never stops it)
+    const int k = res->iters;
+    ST_CUDA(cudaMemsetAsync(&W.sc->done, 0, sizeof(int), st));
+    cg_pupdate_kernel<<<cg_blocks(P.n), 256, 0, st>>>(P.n, W.p, P.dinv ? W.z : W.r, W.sc, k - 1, 0.0);
+    count_launch();
+    ST_CUDA(cudaGetLastError());
+    return cg_loop(P, W, k, max_iter, tol, check_every, res, st);
+}
+
+// Iterations k0 .. of a solve whose state is in W (check_every iterations
+// between host reads of the scalars).
+int cg_loop(const CgProblem& P, CgWork& W, int k0, int max_iter, double tol, int check_every, CgResult* res,
+            cudaStream_t st) {
+    const long long n = P.n;
+    CgScalars h{};
     const float* zp = P.dinv ? W.z : W.r;
-    int k = 0;
+    int k = k0;
     while (k < max_iter) {
         const int batch = std::min(check_every, max_iter - k);
         for (int j = 0; j < batch; ++j, ++k) {
             if (P.AT) {
                 ST_TRY(launch_spmv(*P.A, W.p, W.t, nullptr, 0.0f, nullptr, nullptr, &W.sc->done, st));
-                ST_TRY(launch_spmv(*P.AT, W.t, W.q, W.p, (float)P.lam, W.p, &W.sc->acc[k % 3].pq, &W.sc->done, st));
+                ST_TRY(launch_spmv(*P.AT, W.t, W.q, W.p, (float)P.lam, W.p, W.sc->acc[k % 3].pq, &W.sc->done, st));
             } else {
-                ST_TRY(launch_spmv(*P.A, W.p, W.q, nullptr, 0.0f, W.p, &W.sc->acc[k % 3].pq, &W.sc->done, st));
+                ST_TRY(launch_spmv(*P.A, W.p, W.q, nullptr, 0.0f, W.p, W.sc->acc[k % 3].pq, &W.sc->done, st));
             }
-            cg_update_kernel<<<blocks_for(n), 256, 0, st>>>(n, P.x, W.r, P.dinv ? W.z : nullptr, W.p, W.q, P.dinv,
+            cg_update_kernel<<<cg_blocks(n), 256, 0, st>>>(n, P.x, W.r, P.dinv ? W.z : nullptr, W.p, W.q, P.dinv,
                                                              W.sc, k);
             count_launch();
-            cg_pupdate_kernel<<<blocks_for(n), 256, 0, st>>>(n, W.p, zp, W.sc, k, tol);
+            cg_pupdate_kernel<<<cg_blocks(n), 256, 0, st>>>(n, W.p, zp, W.sc, k, tol);
             count_launch();
             ST_CUDA(cudaGetLastError());
         }

@@ -49,22 +49,32 @@ class DeviceBuffers {
     size_t failed_bytes_ = 0;
 };
 
-// FP64 accumulators of one CG iteration (three rotating slots).
+// FP64 accumulators of one CG iteration (three rotating sets). Each is
+// spread over CG_SLOTS addresses (a block adds into slot blockIdx % CG_SLOTS)
+// so that the blocks' atomics do not all queue on one address; readers sum
+// the slots.
+constexpr int CG_SLOTS = 8;
 struct CgAcc {
-    double pq;   // <p, A p>
-    double rr;   // <r, r> after the update
-    double rzn;  // <r, z> after the update
+    double pq[CG_SLOTS];   // <p, A p>
+    double rr[CG_SLOTS];   // <r, r> after the update
+    double rzn[CG_SLOTS];  // <r, z> after the update
 };
 
 struct CgScalars {
     CgAcc acc[3];
-    double bb;   // <b, b>
-    double rel;  // sqrt(rr)/||b|| of the last iteration
+    double bb[CG_SLOTS];  // <b, b>
+    double rel;           // sqrt(rr)/||b|| of the last iteration
     int iters;
     int done;
     int breakdown;
     int pad_;
 };
+
+inline __host__ __device__ double cg_slot_sum(const double* s) {
+    double t = 0.0;
+    for (int i = 0; i < CG_SLOTS; ++i) t += s[i];
+    return t;
+}
 
 // Operator and preconditioner of one solve: A (square) or A^T A + lam I
 // (A rectangular, AT its explicit transpose); dinv = Jacobi diagonal or null.
@@ -114,6 +124,10 @@ int launch_dot64(const double* a, const double* b, long long n, double* acc, cud
 int launch_fd_triplets(const double* vel, long long nx, long long ny, long long nz, double idx2, double idy2,
                        double idz2, double dt2, long long* tr, long long* tc, double* tv, cudaStream_t st);
 int run_cg(const CgProblem& P, CgWork& W, int max_iter, double tol, int check_every, CgResult* res, cudaStream_t st);
+// Continues a solve that run_cg stopped at tolerance (state in W, res from that
+// call) down to the tighter recurrence tolerance tol, up to max_iter in all.
+int resume_cg(const CgProblem& P, CgWork& W, int max_iter, double tol, int check_every, CgResult* res,
+              cudaStream_t st);
 
 // Flexible CG on (A^T A + lam I) x = b (st_fcg.cu); pc = the learned network
 // (null: Jacobi with dinv). Work vectors r, z, p, q, ax of A.cols floats, t of

@@ -23,6 +23,10 @@ ST_ERR_STATE = -4
 ST_ERR_TIMEOUT = -5
 ST_ERR_UNSUPPORTED = -6
 
+# flags of st_normal_cg_device's jacobi argument
+ST_CG_JACOBI = 1
+ST_CG_CONFIRM_TRUE = 2
+
 ST_FIELD_CURRENT, ST_FIELD_PREVIOUS, ST_FIELD_NEXT, ST_FIELD_VELOCITY = 0, 1, 2, 3
 ST_SNAP_NONE, ST_SNAP_BF16, ST_SNAP_FP16, ST_SNAP_FP32 = 0, 1, 2, 3
 ST_SPONGE_REFERENCE, ST_SPONGE_STABLE = 0, 1

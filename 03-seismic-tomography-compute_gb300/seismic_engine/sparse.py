@@ -232,14 +232,17 @@ def compute_fd_stencil(nx, ny, nz, velocity, dx, dy, dz, dt) -> CSRMatrix:
 
 
 def normal_cg_device(A: CSRMatrix, d, lam: float, x, max_iter: int = 1000, tol: float = 1e-6,
-                     jacobi: bool = True, rhs=None):
+                     jacobi: bool = True, rhs=None, confirm_true: bool = False):
     """(A^T A + lam I) x = A^T d on torch CUDA float32 tensors; returns
     (iterations, recurrence relative residual, true relative residual).
-    With d = None the right-hand side is rhs itself."""
+    With d = None the right-hand side is rhs itself. confirm_true: the stop
+    is confirmed on the true residual (the solve continues while it is above
+    tol)."""
     it = C.c_int()
     rel = C.c_double()
     true_rel = C.c_double()
+    flags = (_lib.ST_CG_JACOBI if jacobi else 0) | (_lib.ST_CG_CONFIRM_TRUE if confirm_true else 0)
     call("st_normal_cg_device", A.handle, d.data_ptr() if d is not None else None, float(lam), int(max_iter),
-         float(tol), int(jacobi),
+         float(tol), flags,
          x.data_ptr(), rhs.data_ptr() if rhs is not None else None, C.byref(it), C.byref(rel), C.byref(true_rel))
     return it.value, rel.value, true_rel.value

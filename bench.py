@@ -351,7 +351,7 @@ def run_tomography(args):
     x = torch.zeros(n ** 3, device="cuda")
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    it, rel, true_rel = se.normal_cg_device(A, d, tp.lam, x, 20000, 1e-6, True)
+    it, rel, true_rel = se.normal_cg_device(A, d, tp.lam, x, 20000, 1e-6, True, confirm_true=True)
     torch.cuda.synchronize()
     t_cg = time.perf_counter() - t0
     out["jacobi_cg"] = {"iterations": it, "seconds": t_cg, "ms_per_iteration": 1e3 * t_cg / max(it, 1),
@@ -841,7 +841,8 @@ def _large(args):
         x = torch.zeros_like(gr)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        it, rel, true_rel = se.normal_cg_device(L, None, 1.0, x, 5000, 1e-6, jacobi, rhs=gr.clone())
+        it, rel, true_rel = se.normal_cg_device(L, None, 1.0, x, 5000, 1e-6, jacobi, rhs=gr.clone(),
+                                                confirm_true=True)
         torch.cuda.synchronize()
         t_cg = time.perf_counter() - t1
         return {"seconds": t_grad + t_cg, "gradient_s": t_grad, "cg_s": t_cg, "cg_iterations": it,

@@ -739,12 +739,19 @@ int st_normal_fcg_device(st_csr* A, const float* d, double lam, int max_iter, do
 /* dinv (device FP32, cols) = 1 / (column sums of A^2 + lam): the Jacobi
  * preconditioner of A^T A + lam I (asynchronous on the matrix's stream). */
 int st_csr_normal_jacobi(st_csr* A, double lam, float* dinv);
+/* Flags of st_normal_cg_device's `jacobi` argument. */
+enum { ST_CG_JACOBI = 1, ST_CG_CONFIRM_TRUE = 2 };
 /* Tomography solve: (A^T A + lam I) x = A^T d for a rectangular A (no
  * reference counterpart), Jacobi diagonal = column sums of A^2 + lam when
- * jacobi != 0. rhs (may be NULL) receives A^T d; with d == NULL, rhs is the
- * given right-hand side instead (e.g. a gradient for the regularised update
- * (I + mu L^T L) x = g with A = sqrt(mu) L, lam = 1). true_rel (may be NULL)
- * receives the FP64 relative true residual ||rhs - (A^T A + lam I) x|| / ||rhs||. */
+ * jacobi & ST_CG_JACOBI. rhs (may be NULL) receives A^T d; with d == NULL, rhs
+ * is the given right-hand side instead (e.g. a gradient for the regularised
+ * update (I + mu L^T L) x = g with A = sqrt(mu) L, lam = 1). true_rel (may be
+ * NULL) receives the FP64 relative true residual ||rhs - (A^T A + lam I) x|| /
+ * ||rhs||. The solve stops when the recurrence residual falls below tol; with
+ * jacobi & ST_CG_CONFIRM_TRUE the stop is confirmed on the true residual:
+ * while that is above tol, the iteration continues to a tighter recurrence
+ * target (at most four times, within max_iter). iters and final_rel are those
+ * of the last iteration. */
 int st_normal_cg_device(st_csr* A, const float* d, double lam, int max_iter, double tol, int jacobi, float* x,
                         float* rhs, int* iters, double* final_rel, double* true_rel);
 /* Replaces dot_product (sparse_ops.cpp:172-187): FP64 inner product. */

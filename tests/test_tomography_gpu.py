@@ -76,3 +76,29 @@ def test_normal_cg_on_ray_system(se, oracle):
     res = atb - oracle.normal_apply(om, tp.lam, xg)
     assert np.linalg.norm(res) <= 2e-6 * np.linalg.norm(atb)
     assert np.linalg.norm(xg - xr) <= 2e-2 * np.linalg.norm(xr)
+
+
+def test_normal_cg_confirms_the_true_residual(se, oracle):
+    """ST_CG_CONFIRM_TRUE: the stop is confirmed on the FP64 true residual,
+    which then meets the tolerance the FP32 recurrence alone may miss; the
+    solve without the flag stops on the recurrence. (The FP64 dot products
+    are summed by atomics, so two solves may differ in the last bits and, at
+    the stop, by an iteration.)"""
+    import torch
+    n = 20
+    tp = se.workloads.tomography_small(n=n, n_rays=6000)
+    m = se.CSRMatrix()
+    m.build_ray_matrix(tp.ends, n, n, n)
+    rp, col, val = oracle.ray_matrix(tp.ends, n, n, n)
+    om = oracle.csr(tp.ends.shape[0], n ** 3, rp, col, val.astype(np.float32).astype(np.float64))
+    b = se.workloads.noisy_data(oracle.spmv(om, tp.x_true), tp.noise_level, tp.noise_seed)
+    d = torch.from_numpy(b.astype(np.float32)).cuda()
+    for tol in (1e-5, 1e-6, 3e-7):
+        x0 = torch.zeros(n ** 3, device="cuda")
+        it0, rel0, tr0 = se.normal_cg_device(m, d, tp.lam, x0, 20000, tol, True)
+        x1 = torch.zeros(n ** 3, device="cuda")
+        it1, rel1, tr1 = se.normal_cg_device(m, d, tp.lam, x1, 20000, tol, True, confirm_true=True)
+        assert rel0 < tol and it1 >= it0 - 1
+        assert tr1 <= tol, (tol, tr0, tr1, it0, it1)
+        if tr0 <= tol:  # nothing to confirm: the same solve
+            assert abs(it1 - it0) <= 1
