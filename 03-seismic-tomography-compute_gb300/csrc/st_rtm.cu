@@ -297,8 +297,11 @@ int st_shot_adjoint(st_solver* s, const st_shot* shot, const float* data, float*
     return (fl & FLAG_GUARD) ? ST_NAN_DETECTED_AND_REPAIRED : ST_OK;
 }
 
-int st_rtm_shot(st_solver* s, const st_shot* shot, const float* data, int snap_kind, void* snaps,
-                unsigned* snap_amax, float* image, float* illum, float* refl) {
+// RTM shot; data_ready (may be null): an event the adjoint pass waits on
+// before it reads `data` (the host entry point's upload runs beside the
+// forward pass).
+static int rtm_shot_impl(st_solver* s, const st_shot* shot, const float* data, int snap_kind, void* snaps,
+                         unsigned* snap_amax, float* image, float* illum, float* refl, cudaEvent_t data_ready) {
     ST_CHECK(s && shot && image && illum, ST_ERR_ARG, "null argument");
     ST_TRY(require_no_terrain(s));
     ST_CHECK(snap_kind >= ST_SNAP_BF16 && snap_kind <= ST_SNAP_FP32, ST_ERR_ARG,
@@ -320,6 +323,7 @@ int st_rtm_shot(st_solver* s, const st_shot* shot, const float* data, int snap_k
     ST_CUDA(cudaEventRecord(s->ev[0], s->stream));
     ST_TRY(shot_forward_impl(s, shot, nullptr, snap_kind, snaps, amax));
     ST_CUDA(cudaEventRecord(s->ev[1], s->stream));
+    if (data_ready) ST_CUDA(cudaStreamWaitEvent(s->stream, data_ready, 0));
     ST_TRY(rtm_backward_impl(s, shot, data, snap_kind, snaps, amax, image, illum));
     ST_CUDA(cudaEventRecord(s->ev[2], s->stream));
     s->phases_recorded = 1;
@@ -327,6 +331,11 @@ int st_rtm_shot(st_solver* s, const st_shot* shot, const float* data, int snap_k
     unsigned fl = 0;
     ST_TRY(read_flags(s, &fl));
     return (fl & FLAG_GUARD) ? ST_NAN_DETECTED_AND_REPAIRED : ST_OK;
+}
+
+int st_rtm_shot(st_solver* s, const st_shot* shot, const float* data, int snap_kind, void* snaps,
+                unsigned* snap_amax, float* image, float* illum, float* refl) {
+    return rtm_shot_impl(s, shot, data, snap_kind, snaps, snap_amax, image, illum, refl, nullptr);
 }
 
 int st_rtm_shot_host(st_solver* s, const double* vp, int64_t vp_count, const st_shot* shot, const float* data_host,
@@ -351,13 +360,24 @@ int st_rtm_shot_host(st_solver* s, const double* vp, int64_t vp_count, const st_
     double* out64 = reinterpret_cast<double*>(aux + amax_bytes + 3 * img_bytes);
     ST_TRY(ensure_buffer(s, &s->snap_buf, &s->snap_cap, snap_total));
     float* data = nullptr;
+    cudaEvent_t data_ready = nullptr;
     if (dbytes > 0) {
         ST_CHECK(data_host, ST_ERR_ARG, "receiver data missing");
         ST_TRY(ensure_buffer(s, &s->data_buf, &s->data_cap, dbytes));
         data = static_cast<float*>(s->data_buf);
-        ST_CUDA(cudaMemcpyAsync(data, data_host, dbytes, cudaMemcpyHostToDevice, s->stream));
+        // the receiver data is read only by the adjoint pass: upload it on a
+        // second stream while the forward pass runs (the buffer's last reader,
+        // the previous call, has finished: every call ends synchronised)
+        if (!s->copy_stream) {
+            ST_CUDA(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+            ST_CUDA(cudaEventCreateWithFlags(&s->ev_copy, cudaEventDisableTiming));
+        }
+        ST_CUDA(cudaMemcpyAsync(data, data_host, dbytes, cudaMemcpyHostToDevice, s->copy_stream));
+        ST_CUDA(cudaEventRecord(s->ev_copy, s->copy_stream));
+        data_ready = s->ev_copy;
     }
-    int rc = st_rtm_shot(s, shot, data, snap_kind, s->snap_buf, amax, image, illum, refl);
+    int rc = rtm_shot_impl(s, shot, data, snap_kind, s->snap_buf, amax, image, illum, refl, data_ready);
+    if (rc < 0 && s->copy_stream) cudaStreamSynchronize(s->copy_stream);
     if (rc < 0) return rc;
     const float* srcs[3] = {image, illum, refl};
     double* dsts[3] = {image_host, illum_host, refl_host};

@@ -532,6 +532,11 @@ int st_solver_destroy(st_solver* s) {
     cudaFree(s->vel_dev);
     for (int k = 0; k < 3; ++k)
         if (s->ev[k]) cudaEventDestroy(s->ev[k]);
+    if (s->ev_copy) cudaEventDestroy(s->ev_copy);
+    if (s->copy_stream) {
+        cudaStreamSynchronize(s->copy_stream);
+        cudaStreamDestroy(s->copy_stream);
+    }
     if (s->stream != s->own_stream) cudaStreamSynchronize(s->stream);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     delete s;

@@ -117,6 +117,10 @@ struct st_solver {
     // [0] start, [1] forward done, [2] backward done
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     int phases_recorded = 0;
+    // host entry points: a second stream that uploads the receiver data while
+    // the forward pass runs, and the event the adjoint pass waits on
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copy = nullptr;
 };
 
 
