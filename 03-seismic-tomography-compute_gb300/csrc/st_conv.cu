@@ -422,6 +422,262 @@ int make_conv_map(CUtensorMap* map, const __nv_bfloat16* base, long long rows, i
     return ST_OK;
 }
 
+// ---------------------------------------------------------------- weight gradient
+// dW[co][ci][tap] += sum over interior voxels v of g[v][co] x[v + s_tap][ci]
+// for a 32 -> 32 layer, on the tensor cores: an implicit GEMM with
+// M = (tap, ci) in 7 tiles of 4 taps x 32 input channels (the last tile has 3
+// taps), N = 32 output channels and K = the padded volume's rows q, split
+// over CTAs (each CTA one M tile and one K range; FP32 atomics add the
+// partial tiles). g's border rows are zeroed on the way in, so a K step may
+// run over them; x's border is zero by the padded convention, and rows past
+// the volume arrive as zeros from the TMA bounds fill.
+//
+// Per K step of 64 rows the TMA brings [64 rows][32 ch] tiles of x (one per
+// tap of the tile, shifted by the tap's row offset) and of g into a ring of
+// raw stages. Channels-last rows are channel-contiguous, but both operands
+// of the contraction over q must be K-major (q contiguous): warps 2-5
+// transpose the tiles 8x8 at a time with ldmatrix.trans / stmatrix into the
+// canonical no-swizzle K-major layout (8 rows x 16-byte core matrices; A:
+// LBO 2048 between K blocks, SBO 128 between M blocks; B: LBO 512, SBO 128)
+// of an operand stage; warp 1 issues four tcgen05.mma (M=128, N=32, K=16) per
+// step into a 32-column TMEM accumulator; warps 2-5 then read it back
+// (tcgen05.ld) and add it to dW. Every wait is bounded as in the forward conv.
+constexpr int WG_KSTEP = 64;
+constexpr int WG_TILES = 7;
+constexpr int WG_NRAW = 3;
+constexpr int WG_NOP = 2;
+constexpr int WG_RAW_TILE = WG_KSTEP * CH * 2;  // 4096
+constexpr int WG_RAW_BYTES = 5 * WG_RAW_TILE;   // four x tiles + the g tile
+constexpr int WG_A_BYTES = TM * WG_KSTEP * 2;   // 16384
+constexpr int WG_B_BYTES = CH * WG_KSTEP * 2;   // 4096
+constexpr int WG_OP_BYTES = WG_A_BYTES + WG_B_BYTES;
+constexpr int WG_THREADS = 192;
+constexpr int WG_TMEM_COLS = 32;
+
+struct WgradArgs {
+    float* dw;
+    int D, H, W;
+    long long rows;  // (D+2)(H+2)(W+2)
+    int ksteps;      // ceil(rows / 64)
+    int splits;      // CTAs per M tile
+    unsigned* flags;
+    unsigned long long timeout_ns;
+};
+
+struct WgradSmem {
+    uint64_t raw_full[WG_NRAW], raw_empty[WG_NRAW], op_full[WG_NOP], op_empty[WG_NOP], done;
+    uint32_t tmem_base;
+    int abort;
+};
+
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t addr, uint32_t r[4]) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(addr)
+                 : "memory");
+}
+__device__ __forceinline__ void stsm_x4(uint32_t addr, const uint32_t r[4]) {
+    asm volatile("stmatrix.sync.aligned.m8n8.x4.shared.b16 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(r[0]),
+                 "r"(r[1]), "r"(r[2]), "r"(r[3])
+                 : "memory");
+}
+__device__ __forceinline__ void named_sync_128() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
+__global__ void __launch_bounds__(WG_THREADS, 1)
+    conv32_wgrad_tc_kernel(const __grid_constant__ CUtensorMap mx, const __grid_constant__ CUtensorMap mg,
+                           const WgradArgs a) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char* smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    unsigned char* raw = smem;
+    unsigned char* ops = smem + WG_NRAW * WG_RAW_BYTES;
+    WgradSmem* cs = reinterpret_cast<WgradSmem*>(ops + WG_NOP * WG_OP_BYTES);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tile = blockIdx.x % WG_TILES, split = blockIdx.x / WG_TILES;
+    const int ntap = tile == WG_TILES - 1 ? NTAP - 4 * (WG_TILES - 1) : 4;
+    const int k0 = (int)((long long)a.ksteps * split / a.splits);
+    const int nk = (int)((long long)a.ksteps * (split + 1) / a.splits) - k0;
+    const int W2 = a.W + 2;
+    const int PL = (a.H + 2) * W2;
+    const uint64_t lim = a.timeout_ns;
+    const uint64_t dlim = lim > WAIT_DRAIN_NS ? lim : WAIT_DRAIN_NS;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < WG_NRAW; ++s) {
+            mbar_init(&cs->raw_full[s], 1);
+            mbar_init(&cs->raw_empty[s], 128);
+        }
+        for (int s = 0; s < WG_NOP; ++s) {
+            mbar_init(&cs->op_full[s], 128);
+            mbar_init(&cs->op_empty[s], 1);
+        }
+        mbar_init(&cs->done, 1);
+        cs->abort = 0;
+        fence_mbar_init();
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&cs->tmem_base)),
+                     "r"(WG_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        tc_fence_before();
+    }
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = cs->tmem_base;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int k = 0;
+            for (; k < nk; ++k) {
+                const int s = k % WG_NRAW;
+                if (k >= WG_NRAW && !mbar_wait_bounded(&cs->raw_empty[s], ((k / WG_NRAW) - 1) & 1, lim)) {
+                    atomicOr(a.flags, CONV_FLAG_TIMEOUT);
+                    cs->abort = 1;
+                    break;
+                }
+                if (read_abort(&cs->abort)) break;
+                const int q0 = (k0 + k) * WG_KSTEP;
+                unsigned char* rb = raw + s * WG_RAW_BYTES;
+                mbar_arrive_expect_tx(&cs->raw_full[s], (uint32_t)(ntap + 1) * WG_RAW_TILE);
+                for (int t = 0; t < ntap; ++t) {
+                    const int tap = 4 * tile + t;
+                    const int shift = (tap / 9 - 1) * PL + ((tap / 3) % 3 - 1) * W2 + (tap % 3 - 1);
+                    tma_load_2d(rb + t * WG_RAW_TILE, &mx, &cs->raw_full[s], 0, q0 + shift);
+                }
+                tma_load_2d(rb + 4 * WG_RAW_TILE, &mg, &cs->raw_full[s], 0, q0);
+            }
+            // drain: every issued stage has landed before the CTA may exit
+            for (int f = (k > WG_NRAW ? k - WG_NRAW : 0); f < k; ++f)
+                if (!mbar_wait_bounded(&cs->raw_full[f % WG_NRAW], (f / WG_NRAW) & 1, dlim))
+                    atomicOr(a.flags, CONV_FLAG_TIMEOUT);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            int k = 0;
+            for (; k < nk; ++k) {
+                const int o = k % WG_NOP;
+                if (!mbar_wait_bounded(&cs->op_full[o], (k / WG_NOP) & 1, lim) || read_abort(&cs->abort)) {
+                    atomicOr(a.flags, CONV_FLAG_TIMEOUT);
+                    cs->abort = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t ab = smem_u32(ops + o * WG_OP_BYTES), bb = ab + WG_A_BYTES;
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    mma_bf16(tmem, smem_desc(ab + (uint32_t)j * 4096u, 2048u, 128u),
+                             smem_desc(bb + (uint32_t)j * 1024u, 512u, 128u), (k | j) != 0);
+                mma_commit(&cs->op_empty[o]);
+            }
+            // the last commit tracks every MMA issued: the accumulator is final
+            // (and, after an abort, no MMA is left running when TMEM is freed)
+            if (k > 0) {
+                mma_commit(&cs->done);
+                if (!mbar_wait_bounded(&cs->done, 0, dlim)) atomicOr(a.flags, CONV_FLAG_TIMEOUT);
+            }
+        }
+    } else {
+        // warps 2-5: transposes, then the epilogue. The four warps meet at a
+        // named barrier every step, so none leaves the loop early: after a
+        // failed wait (or another warp's abort) a warp stops waiting and
+        // working but still takes every barrier.
+        const int tt = threadIdx.x - 64, tw = warp - 2;
+        bool ok = true;
+        for (int k = 0; k < nk; ++k) {
+            const int s = k % WG_NRAW, o = k % WG_NOP;
+            if (ok) {
+                bool w = !read_abort(&cs->abort) && mbar_wait_bounded(&cs->raw_full[s], (k / WG_NRAW) & 1, lim);
+                if (w && k >= WG_NOP) w = mbar_wait_bounded(&cs->op_empty[o], ((k / WG_NOP) - 1) & 1, lim);
+                // ldmatrix / stmatrix are warp-collective: a warp-uniform outcome
+                if (!__all_sync(0xffffffffu, w && !read_abort(&cs->abort))) {
+                    if (lane == 0) atomicOr(a.flags, CONV_FLAG_TIMEOUT);
+                    cs->abort = 1;
+                    ok = false;
+                }
+            }
+            unsigned char* rb = raw + s * WG_RAW_BYTES;
+            unsigned char* ob = ops + o * WG_OP_BYTES;
+            if (ok && tt < WG_KSTEP) {
+                // g rows outside the interior contribute nothing
+                const long long q = (long long)(k0 + k) * WG_KSTEP + tt;
+                const int d = (int)(q / PL), rem = (int)(q - (long long)d * PL), h = rem / W2, wv = rem - h * W2;
+                const bool inside = d >= 1 && d <= a.D && h >= 1 && h <= a.H && wv >= 1 && wv <= a.W;
+                if (!inside) {
+                    uint4* row = reinterpret_cast<uint4*>(rb + 4 * WG_RAW_TILE + tt * (CH * 2));
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) row[j] = make_uint4(0u, 0u, 0u, 0u);
+                }
+            }
+            named_sync_128();
+            if (!ok) continue;
+            // 160 blocks of 8 x 8 (A: 4 taps x 8 row blocks x 4 channel blocks; B: 8 x 4),
+            // four per ldmatrix / stmatrix pair; lane l addresses row l % 8 of block l / 8
+            const int r = lane & 7;
+            for (int i = tw; i < 40; i += 4) {
+                const int b = i * 4 + (lane >> 3);
+                uint32_t src, dst;
+                if (b < 128) {
+                    const int t = b >> 5, rem = b & 31, vb = rem >> 2, cb = rem & 3;
+                    if (t >= ntap) continue;  // uniform over the group (32 blocks per tap)
+                    src = smem_u32(rb + t * WG_RAW_TILE + (vb * 8 + r) * (CH * 2) + cb * 16);
+                    dst = smem_u32(ob + vb * 2048 + (t * 4 + cb) * 128 + r * 16);
+                } else {
+                    const int bb = b - 128, vb = bb >> 2, cb = bb & 3;
+                    src = smem_u32(rb + 4 * WG_RAW_TILE + (vb * 8 + r) * (CH * 2) + cb * 16);
+                    dst = smem_u32(ob + WG_A_BYTES + vb * 512 + cb * 128 + r * 16);
+                }
+                uint32_t v4[4];
+                ldsm_x4_trans(src, v4);
+                stsm_x4(dst, v4);
+            }
+            // generic-proxy writes read by the tensor cores, and a raw stage the
+            // TMA overwrites next
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(&cs->op_full[o]);
+            mbar_arrive(&cs->raw_empty[s]);
+        }
+        if (ok && nk > 0) {
+            const bool got = __all_sync(0xffffffffu, mbar_wait_bounded(&cs->done, 0, dlim));
+            if (!got) {
+                if (lane == 0) atomicOr(a.flags, CONV_FLAG_TIMEOUT);
+            } else {
+                tc_fence_after();
+                const int quarter = warp & 3;  // TMEM lanes 32 quarter .. : tap quarter of the tile, ci = lane
+                float v[CH];
+                tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16), v);
+                tc_fence_before();
+                if (quarter < ntap) {
+                    const int tap = 4 * tile + quarter;
+#pragma unroll
+                    for (int co = 0; co < CH; ++co) atomicAdd(&a.dw[((size_t)co * CH + lane) * NTAP + tap], v[co]);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(WG_TMEM_COLS)
+                     : "memory");
+    }
+}
+
+// The padded volume viewed as [rows][32 channels], box {32 channels, 64 rows}.
+int make_wgrad_map(CUtensorMap* map, const __nv_bfloat16* base, long long rows) {
+    EncodeTiledFn enc = nullptr;
+    ST_TRY(get_encode_tiled(&enc));
+    cuuint64_t dims[2] = {CH, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)CH * 2};
+    cuuint32_t box[2] = {CH, WG_KSTEP};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(base), dims, strides, box,
+                     estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    ST_CHECK(r == CUDA_SUCCESS, ST_ERR_CUDA, "cuTensorMapEncodeTiled (wgrad) failed (%d)", (int)r);
+    return ST_OK;
+}
+
 __device__ unsigned g_conv_flags;
 
 }  // namespace
@@ -518,6 +774,42 @@ int st_conv3d_bf16(const void* in, const void* packed_w, const float* bias, cons
     const int grid = std::min(a.units, num_sms_conv());
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     kern<<<grid, CONV_THREADS, smem, st>>>(maps[0], maps[1], maps[2], maps[3], a);
+    count_launch();
+    ST_CUDA(cudaGetLastError());
+    return ST_OK;
+}
+
+int st_conv3d_wgrad(const void* x, const void* g, float* dw, int64_t nx, int64_t ny, int64_t nz, void* stream) {
+    ST_CHECK(x && g && dw, ST_ERR_ARG, "null argument");
+    ST_CHECK(nx > 0 && ny > 0 && nz > 0, ST_ERR_ARG, "bad volume extents");
+    auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+    ST_CHECK(al16(x) && al16(g), ST_ERR_ARG, "conv buffers must be 16-byte aligned");
+    const long long rows = (nx + 2) * (ny + 2) * (nz + 2);
+    ST_CHECK(rows + (ny + 2) * (nz + 2) + nz + 3 < (1ll << 31), ST_ERR_ARG, "volume too large");
+    CUtensorMap mx, mg;
+    ST_TRY(make_wgrad_map(&mx, static_cast<const __nv_bfloat16*>(x), rows));
+    ST_TRY(make_wgrad_map(&mg, static_cast<const __nv_bfloat16*>(g), rows));
+    unsigned* flags = nullptr;
+    ST_CUDA(cudaGetSymbolAddress(reinterpret_cast<void**>(&flags), g_conv_flags));
+    WgradArgs a{};
+    a.dw = dw;
+    a.D = (int)nx;
+    a.H = (int)ny;
+    a.W = (int)nz;
+    a.rows = rows;
+    a.ksteps = (int)((rows + WG_KSTEP - 1) / WG_KSTEP);
+    // two CTAs per SM over the 7 M tiles, at least one K step each
+    a.splits = (int)std::max<long long>(1, std::min<long long>(a.ksteps, (2LL * num_sms_conv() + WG_TILES - 1) / WG_TILES));
+    a.flags = flags;
+    a.timeout_ns = 2000000000ull;
+    const size_t smem = (size_t)WG_NRAW * WG_RAW_BYTES + (size_t)WG_NOP * WG_OP_BYTES + sizeof(WgradSmem) + 1024;
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [&] {
+        attr = cudaFuncSetAttribute(conv32_wgrad_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    });
+    ST_CUDA(attr);
+    conv32_wgrad_tc_kernel<<<WG_TILES * a.splits, WG_THREADS, smem, static_cast<cudaStream_t>(stream)>>>(mx, mg, a);
     count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;

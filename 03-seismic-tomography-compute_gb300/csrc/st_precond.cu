@@ -232,68 +232,6 @@ __global__ void relu_mask_kernel(const __nv_bfloat16* __restrict__ dh, const __n
     }
 }
 
-// dW[co][ci][tap] += sum_v g[v][co] * x[v + s_tap][ci] for a 32 -> 32 layer.
-// Block (range, tap): 256 threads, thread t owns co = t / 8 and ci = 4 (t % 8)
-// .. +3; 64-voxel chunks of g and of the shifted x are staged in shared memory.
-__global__ void __launch_bounds__(256) conv32_wgrad_kernel(const __nv_bfloat16* __restrict__ x,
-                                                           const __nv_bfloat16* __restrict__ g, Vol v,
-                                                           float* __restrict__ dw) {
-    constexpr int CHUNK = 64;
-    __shared__ float gs[CHUNK][CH + 1];
-    __shared__ float xs[CHUNK][CH + 1];
-    const int tap = blockIdx.y;
-    const int W2 = v.nz + 2, P2 = (v.ny + 2) * W2;
-    const long long shift = (long long)(tap / 9 - 1) * P2 + ((tap / 3) % 3 - 1) * W2 + (tap % 3 - 1);
-    const int co = threadIdx.x >> 3, ci0 = (threadIdx.x & 7) * 4;
-    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    const long long n = v.n();
-    const long long per = (n + gridDim.x - 1) / gridDim.x;
-    const long long i0 = blockIdx.x * per, i1 = min(n, i0 + per);
-    for (long long c0 = i0; c0 < i1; c0 += CHUNK) {
-        // stage: 64 voxels x 32 channels of g and of x shifted by the tap
-        for (int e = threadIdx.x; e < CHUNK * 4; e += blockDim.x) {
-            const int vi = e >> 2, part = e & 3;
-            const long long i = c0 + vi;
-            float gg[8], xx[8];
-            if (i < i1) {
-                int px, py, pz;
-                decode(i, v, px, py, pz);
-                const long long q = v.pad_row(px, py, pz);
-                const uint4 ug = reinterpret_cast<const uint4*>(g + q * CH)[part];
-                const uint4 ux = reinterpret_cast<const uint4*>(x + (q + shift) * CH)[part];
-                const __nv_bfloat162* bg = reinterpret_cast<const __nv_bfloat162*>(&ug);
-                const __nv_bfloat162* bx = reinterpret_cast<const __nv_bfloat162*>(&ux);
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const float2 a = __bfloat1622float2(bg[k]), b = __bfloat1622float2(bx[k]);
-                    gg[2 * k] = a.x;
-                    gg[2 * k + 1] = a.y;
-                    xx[2 * k] = b.x;
-                    xx[2 * k + 1] = b.y;
-                }
-            } else {
-#pragma unroll
-                for (int k = 0; k < 8; ++k) gg[k] = xx[k] = 0.0f;
-            }
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                gs[vi][part * 8 + k] = gg[k];
-                xs[vi][part * 8 + k] = xx[k];
-            }
-        }
-        __syncthreads();
-#pragma unroll 8
-        for (int vi = 0; vi < CHUNK; ++vi) {
-            const float a = gs[vi][co];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) acc[k] = fmaf(a, xs[vi][ci0 + k], acc[k]);
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) atomicAdd(&dw[((size_t)co * CH + ci0 + k) * NTAP + tap], acc[k]);
-}
-
 // acc[0] += sum r^2, acc[1] += sum dinv (multi-block, FP64 atomics).
 __global__ void pc_sums_kernel(const float* __restrict__ r, const float* __restrict__ dinv, long long n, double* acc) {
     double a = 0.0, b = 0.0;
@@ -458,16 +396,6 @@ int st_pc_conv1_wgrad(const float* dz, const void* h, float* dw, int64_t nx, int
     const Vol v{(int)nx, (int)ny, (int)nz};
     out_conv_wgrad_kernel<<<dim3(grid_for(v.n(), 64), NTAP), 256, 0, (cudaStream_t)stream>>>(
         dz, static_cast<const __nv_bfloat16*>(h), v, dw);
-    count_launch();
-    ST_CUDA(cudaGetLastError());
-    return ST_OK;
-}
-
-int st_conv3d_wgrad(const void* x, const void* g, float* dw, int64_t nx, int64_t ny, int64_t nz, void* stream) {
-    ST_CHECK(x && g && dw, ST_ERR_ARG, "null argument");
-    const Vol v{(int)nx, (int)ny, (int)nz};
-    conv32_wgrad_kernel<<<dim3(grid_for(v.n(), 48), NTAP), 256, 0, (cudaStream_t)stream>>>(
-        static_cast<const __nv_bfloat16*>(x), static_cast<const __nv_bfloat16*>(g), v, dw);
     count_launch();
     ST_CUDA(cudaGetLastError());
     return ST_OK;

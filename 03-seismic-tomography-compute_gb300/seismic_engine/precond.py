@@ -11,8 +11,10 @@ So CG keeps its theory (a fixed SPD preconditioner), and the untrained
 network (small weights) is Jacobi plus a small correction. The 2K 32 -> 32
 layers of G and G^T run on the tensor cores (st_conv3d_bf16: tcgen05, BF16
 operands, FP32 accumulation; G^T through the transposed weight packing),
-forward and in the backward pass; C, C^T, the weight gradients and the
-scalings are CUDA-core kernels (st_precond.cu). Activations are BF16, and
+forward and in the backward pass, and so do their weight gradients
+(st_conv3d_wgrad: a tcgen05 implicit GEMM contracting over the voxels); C,
+C^T, their weight gradients and the scalings are CUDA-core kernels
+(st_precond.cu). Activations are BF16, and
 the input is scaled by 1 / rms(r) and the output back (z stays linear in r).
 
 Training uses pairs (r_k, e_k = x* - x_k) from plain Jacobi-CG solves of

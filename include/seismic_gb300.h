@@ -546,7 +546,7 @@ int st_conv3d_pack_weights(const float* w_oidhw, void* packed_w, int transpose, 
 int st_conv3d_bf16(const void* in, const void* packed_w, const float* bias, const void* add, void* out, int out_fp32,
                    int64_t D, int64_t H, int64_t W, int relu, void* stream);
 int st_conv3d_check(void* stream);
-/* CUDA-core layers of the learned preconditioner z = dinv r + s_out N(r)
+/* Other layers of the learned preconditioner z = dinv r + s_out N(r)
  * (no reference counterpart). r, dinv, z, zhat: compact FP32 nx*ny*nz
  * (x slowest); h, dh, g: padded channels-last BF16 32-channel volumes;
  * scale, s_out: one device FP32 each. Weights FP32: w_in [32][2][27],
@@ -556,8 +556,11 @@ int st_conv3d_check(void* stream);
  *  st_pc_out_conv      zhat = C_out(h); z = dinv r + s_out zhat (z, zhat may be NULL)
  *  st_pc_out_conv_bwd  dh = C_out^T(dzhat); dw_out += dL/dw_out
  *  st_pc_relu_mask     g = dh * [h > 0]
- *  st_conv3d_wgrad     dw += sum_v g[v] (x) x[v + tap] for a 32 -> 32 layer
- * All asynchronous on `stream`; gradients accumulate (zero them first). */
+ *  st_conv3d_wgrad     dw += sum_v g[v] (x) x[v + tap] for a 32 -> 32 layer, on the
+ *                      tensor cores (tcgen05; g's border rows are ignored; a bounded-wait
+ *                      timeout is reported by st_conv3d_check)
+ * The others run on CUDA cores. All asynchronous on `stream`; gradients
+ * accumulate (zero them first). */
 int st_pc_in_conv(const float* r, const float* dinv, const float* scale, const float* w_in, void* h, int64_t nx,
                   int64_t ny, int64_t nz, void* stream);
 int st_pc_in_conv_wgrad(const float* r, const float* dinv, const float* scale, const void* g, float* dw_in,

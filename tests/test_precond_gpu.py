@@ -1,6 +1,7 @@
 """Learned CG preconditioner on the GPU: its forward pass and the gradients
-of all its layers (tensor-core forward and input-gradient convolutions,
-CUDA-core weight gradients) against the CPU oracle's FP64 restatement with
+of all its layers (tensor-core forward, input-gradient and 32 -> 32
+weight-gradient convolutions; CUDA-core 1 <-> 32 channel layers) against
+the CPU oracle's FP64 restatement with
 BF16 storage emulated (relative L2 <= 1e-2), and the preconditioned flexible
 CG against Jacobi-CG on a small ray system after a short training."""
 import os
@@ -84,3 +85,32 @@ def test_native_fcg_and_trained_preconditioner(se):
     assert abs(it_j - it_cg) <= 0.1 * it_cg + 16
     assert float(torch.linalg.norm(x_j - x_cg)) <= 2e-2 * float(torch.linalg.norm(x_cg))
     assert float(torch.linalg.norm(x_l - x_cg)) <= 2e-2 * float(torch.linalg.norm(x_cg))
+
+
+def test_conv3d_wgrad_tensor_cores_match_fp64(se):
+    """st_conv3d_wgrad (tcgen05 implicit GEMM over the padded rows, split over
+    CTAs) against an FP64 sum over the interior voxels of the same BF16
+    values; the output gradient's border rows hold garbage, which the kernel
+    must ignore. Shapes: small, ragged, and large enough for long K ranges."""
+    import torch
+    from seismic_engine._lib import call
+    st = torch.cuda.current_stream().cuda_stream
+    for shape in ((6, 7, 9), (17, 12, 30), (40, 33, 50)):
+        D, H, W = shape
+        gen = torch.Generator().manual_seed(D)
+        x = torch.zeros((D + 2, H + 2, W + 2, 32))
+        x[1:-1, 1:-1, 1:-1] = torch.randn((D, H, W, 32), generator=gen)
+        g = torch.randn((D + 2, H + 2, W + 2, 32), generator=gen)
+        xb, gb = x.bfloat16(), g.bfloat16()
+        xd, gd = xb.cuda(), gb.cuda()
+        dw = torch.zeros(32 * 32 * 27, device="cuda")
+        call("st_conv3d_wgrad", xd.data_ptr(), gd.data_ptr(), dw.data_ptr(), D, H, W, st)
+        call("st_conv3d_check", st)
+        xf, gi = xb.double(), gb.double()[1:-1, 1:-1, 1:-1]
+        ref = np.zeros((32, 32, 27))
+        for tap in range(27):
+            kd, kh, kw = tap // 9, (tap // 3) % 3, tap % 3
+            xs = xf[kd:kd + D, kh:kh + H, kw:kw + W]
+            ref[:, :, tap] = torch.einsum("dhwo,dhwi->oi", gi, xs).numpy()
+        got = dw.cpu().numpy().reshape(32, 32, 27)
+        assert rel(got, ref) < 1e-5, (shape, rel(got, ref))
