@@ -71,7 +71,7 @@ def parse():
     ap.add_argument("--segment", type=int, default=200, help="checkpoint segment length of --workload large")
     ap.add_argument("--compare", action="store_true",
                     help="--workload large: also time FP32 segment snapshots and unpreconditioned CG")
-    ap.add_argument("--kernel", choices=["conv", "spmv", "rays"], default=None,
+    ap.add_argument("--kernel", choices=["conv", "wgrad", "spmv", "rays"], default=None,
                     help="time one kernel alone (profiling runs) instead of the workload")
     ap.add_argument("--no-tomo", action="store_true", help="skip the tomography CG measurement")
     ap.add_argument("--tomo-n", type=int, default=100, help="cell grid edge of the --kernel spmv matrix")
@@ -681,7 +681,8 @@ def large_iteration(args):
 
 def run_kernel(args):
     """Single-kernel timing for profiling: 'conv' = the tensor-core 3x3x3
-    32 -> 32 convolution on a 100^3 volume; 'spmv' = A x and A^T y of the
+    32 -> 32 convolution on a 100^3 volume; 'wgrad' = its tensor-core weight
+    gradient on the same volume; 'spmv' = A x and A^T y of the
     100^3 / 2M-ray tomography matrix; 'rays' = the sampled-ray forward model
     and gradient of 2M picks. Prints one JSON line."""
     import ctypes as C
@@ -707,6 +708,23 @@ def run_kernel(args):
             assert rc == 0
         flops = 2.0 * n ** 3 * 32 * 32 * 27
         res.update({"workload": f"3x3x3 conv, 32 -> 32 channels, BF16 operands, {n}^3 voxels", "flops": flops})
+    elif args.kernel == "wgrad":
+        n = 100
+        g = torch.Generator(device="cuda").manual_seed(0)
+        x = torch.zeros((n + 2, n + 2, n + 2, 32), dtype=torch.bfloat16, device="cuda")
+        x[1:-1, 1:-1, 1:-1] = torch.randn((n, n, n, 32), device="cuda", generator=g).to(torch.bfloat16)
+        gy = torch.zeros_like(x)
+        gy[1:-1, 1:-1, 1:-1] = torch.randn((n, n, n, 32), device="cuda", generator=g).to(torch.bfloat16)
+        dw = torch.zeros(32 * 32 * 27, device="cuda")
+
+        def one():
+            rc = L.st_conv3d_wgrad(C.c_void_p(x.data_ptr()), C.c_void_p(gy.data_ptr()), C.c_void_p(dw.data_ptr()), n, n,
+                                   n, C.c_void_p(st.cuda_stream))
+            assert rc == 0
+        # the GEMM runs over every padded row (the border rows contribute zero)
+        flops = 2.0 * (n + 2) ** 3 * 32 * 32 * 27
+        res.update({"workload": f"3x3x3 conv weight gradient, 32 -> 32 channels, BF16 operands, {n}^3 voxels",
+                    "flops": flops})
     elif args.kernel == "rays":
         ps = se.workloads.obs_picks()
         rays = se.SampledRays(ps.model, ps.src_xyz, ps.sta_xyz, ps.weight)
