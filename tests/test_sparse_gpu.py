@@ -284,14 +284,16 @@ def test_sparse_ops_match_reference_fixture(se, golden_dir):
     np.testing.assert_array_equal(HR.values(), f32(g["hess_rand_val"]))
 
 
-@pytest.mark.parametrize("per_row", [3, 7, 14, 40, 300])
+@pytest.mark.parametrize("per_row", [3, 7, 14, 40, 200, 300, 600])
 def test_spmv_and_cg_with_ragged_last_sweep(se, per_row):
     """Row counts that are not a multiple of the row groups in a warp (32 / G,
     G = 2..32 threads per row by mean row length), so some groups of a warp
     have no row in the last sweep: SpMV, SpMV^T and CG (whose SpMV fuses the
-    FP64 <p, Ap> reduction) against dense FP64 numpy."""
+    FP64 <p, Ap> reduction) against dense FP64 numpy. Rows of about 200 and
+    1200 entries run past the entries each lane holds (16 threads x 10, 32 x
+    6) into the loop that takes the rest."""
     rng = np.random.default_rng(100 + per_row)
-    n = 333 if per_row < 300 else 1001
+    n = 333 if per_row < 200 else 1001 if per_row < 600 else 1500
     k = max(per_row // 2, 1)
     r = np.repeat(np.arange(n), k)
     c = rng.integers(0, n, r.size)
