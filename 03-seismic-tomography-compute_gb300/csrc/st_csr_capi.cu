@@ -412,8 +412,12 @@ int st_cg(st_csr* m, const double* b, int64_t nb, int max_iter, double tol, int 
 }
 
 // Damped normal equations (A^T A + lam I) x = A^T d of a rectangular A.
-int st_normal_cg_device(st_csr* m, const float* d, double lam, int max_iter, double tol, int jacobi, float* x,
-                        float* rhs, int* iters, double* final_rel, double* true_rel) {
+// The normal-equation CG of st_normal_cg_device, with the stencil
+// preconditioner of st_normal_pcg_stencil_device when stencil is set (three
+// axis weights on a gx x gy x gz cell grid).
+static int normal_cg_impl(st_csr* m, const float* d, double lam, int max_iter, double tol, int jacobi, float* x,
+                          float* rhs, int* iters, double* final_rel, double* true_rel, const float* stencil, int gx,
+                          int gy, int gz) {
     ST_CHECK(m && x && (d || rhs), ST_ERR_ARG, "null argument");
     ST_CUDA(cudaSetDevice(m->device));
     ST_TRY(ensure_transpose(m));
@@ -427,13 +431,15 @@ int st_normal_cg_device(st_csr* m, const float* d, double lam, int max_iter, dou
     W.t = sc.get<float>((size_t)rows);
     W.sc = sc.get<CgScalars>(1);
     float* b = rhs ? rhs : sc.get<float>((size_t)n);
-    const bool use_jacobi = (jacobi & ST_CG_JACOBI) != 0;
+    const bool use_jacobi = (jacobi & ST_CG_JACOBI) != 0 || stencil;
     const bool confirm = (jacobi & ST_CG_CONFIRM_TRUE) != 0;
     float* dinv = use_jacobi ? sc.get<float>((size_t)n) : nullptr;
     float* res = sc.get<float>((size_t)n);
-    ST_ALLOC(W.r && W.z && W.p && W.q && W.t && W.sc && b && (!use_jacobi || dinv) && res);
+    float* sq = stencil ? sc.get<float>((size_t)n) : nullptr;
+    ST_ALLOC(W.r && W.z && W.p && W.q && W.t && W.sc && b && (!use_jacobi || dinv) && res && (!stencil || sq));
     if (d) ST_TRY(launch_spmv(m->AT, d, b, nullptr, 0.0f, nullptr, nullptr, nullptr, m->stream));
     if (use_jacobi) ST_TRY(launch_normal_jacobi(m->AT, lam, dinv, m->stream));
+    if (stencil) ST_TRY(launch_sqrt(dinv, sq, n, m->stream));
     CgProblem P;
     P.A = &m->A;
     P.AT = &m->AT;
@@ -442,6 +448,13 @@ int st_normal_cg_device(st_csr* m, const float* d, double lam, int max_iter, dou
     P.b = b;
     P.x = x;
     P.dinv = dinv;
+    if (stencil) {
+        P.sq = sq;
+        P.gx = gx;
+        P.gy = gy;
+        P.gz = gz;
+        for (int a = 0; a < 3; ++a) P.w[a] = stencil[a];
+    }
     CgResult R;
     ST_TRY(run_cg(P, W, max_iter, tol, 16, &R, m->stream));
     if (R.iters == 0) ST_CUDA(cudaMemsetAsync(x, 0, (size_t)std::max<long long>(n, 1) * 4, m->stream));
@@ -476,6 +489,24 @@ int st_normal_cg_device(st_csr* m, const float* d, double lam, int max_iter, dou
     if (iters) *iters = R.iters;
     if (final_rel) *final_rel = R.rel;
     return ST_OK;
+}
+
+int st_normal_cg_device(st_csr* m, const float* d, double lam, int max_iter, double tol, int jacobi, float* x,
+                        float* rhs, int* iters, double* final_rel, double* true_rel) {
+    return normal_cg_impl(m, d, lam, max_iter, tol, jacobi, x, rhs, iters, final_rel, true_rel, nullptr, 0, 0, 0);
+}
+
+int st_normal_pcg_stencil_device(st_csr* m, const float* d, double lam, const float* w, int64_t nx, int64_t ny,
+                                 int64_t nz, int max_iter, double tol, int flags, float* x, float* rhs, int* iters,
+                                 double* final_rel, double* true_rel) {
+    ST_CHECK(m && w, ST_ERR_ARG, "null argument");
+    ST_CHECK(nx > 0 && ny > 0 && nz > 0 && nx * ny * nz == m->A.cols, ST_ERR_ARG,
+             "grid %lld x %lld x %lld does not match the matrix's %lld columns", (long long)nx, (long long)ny,
+             (long long)nz, m->A.cols);
+    for (int a = 0; a < 3; ++a)
+        ST_CHECK(std::isfinite(w[a]) && w[a] >= 0.0f, ST_ERR_ARG, "stencil weights must be finite and >= 0");
+    return normal_cg_impl(m, d, lam, max_iter, tol, flags, x, rhs, iters, final_rel, true_rel, w, (int)nx, (int)ny,
+                          (int)nz);
 }
 
 int st_normal_fcg_device(st_csr* m, const float* d, double lam, int max_iter, double tol, st_pcnet* pc, float* x,

@@ -301,9 +301,10 @@ __global__ void cg_init_kernel(const float* __restrict__ b, const float* __restr
 // x += alpha p, r -= alpha q, z = M r; acc rz_new = <r,z>, rr = <r,r>.
 // alpha = rz_old / pq; |pq| < 1e-30 stops the solve (sparse_ops.cpp:37,88).
 // The scalars are formed once per block (FP64 is a slow pipe on this GPU).
+// skip_rz: <r, z> comes from the stencil preconditioner's kernel instead.
 __global__ void cg_update_kernel(long long n, float* __restrict__ x, float* __restrict__ r, float* __restrict__ z,
                                  const float* __restrict__ p, const float* __restrict__ q,
-                                 const float* __restrict__ dinv, CgScalars* sc, int k) {
+                                 const float* __restrict__ dinv, CgScalars* sc, int k, int skip_rz) {
     __shared__ float s_alpha;
     __shared__ int s_stop;
     if (threadIdx.x == 0) {
@@ -337,7 +338,35 @@ __global__ void cg_update_kernel(long long n, float* __restrict__ x, float* __re
         a += (double)ri * (double)zi;
         c += (double)ri * (double)ri;
     }
-    block_add2(a, c, sc->acc[k % 3].rzn, sc->acc[k % 3].rr, CG_SLOTS);
+    block_add2(a, c, skip_rz ? nullptr : sc->acc[k % 3].rzn, sc->acc[k % 3].rr, CG_SLOTS);
+}
+
+// z = dinv r + S sum_a w_a (2 v - v(-e_a) - v(+e_a)), v = S r and 0 outside
+// the grid (the weighted Dirichlet Laplacian between the two diagonal
+// scalings: symmetric positive definite with dinv); acc += <r, z>; p = z when
+// p is set (the first iteration).
+__global__ void stencil_prec_kernel(long long n, const float* __restrict__ r, const float* __restrict__ dinv,
+                                    const float* __restrict__ sq, int gx, int gy, int gz, float wx, float wy,
+                                    float wz, float* __restrict__ z, float* __restrict__ p, double* acc,
+                                    const int* done) {
+    if (done && *done) return;
+    const long long sy = gz, sx = (long long)gy * gz;
+    double a = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int iz = (int)(i % gz);
+        const long long t = i / gz;
+        const int iy = (int)(t % gy), ix = (int)(t / gy);
+        const float si = sq[i], ri = r[i], vi = si * ri;
+        auto v = [&](long long j) { return sq[j] * r[j]; };
+        const float lz = 2.0f * vi - (iz > 0 ? v(i - 1) : 0.0f) - (iz < gz - 1 ? v(i + 1) : 0.0f);
+        const float ly = 2.0f * vi - (iy > 0 ? v(i - sy) : 0.0f) - (iy < gy - 1 ? v(i + sy) : 0.0f);
+        const float lx = 2.0f * vi - (ix > 0 ? v(i - sx) : 0.0f) - (ix < gx - 1 ? v(i + sx) : 0.0f);
+        const float zi = fmaf(dinv[i], ri, si * fmaf(wx, lx, fmaf(wy, ly, wz * lz)));
+        z[i] = zi;
+        if (p) p[i] = zi;
+        a += (double)ri * (double)zi;
+    }
+    block_add2(a, 0.0, acc, nullptr, CG_SLOTS);
 }
 
 // Convergence test after the update (sqrt(rr)/||b|| < tol) and
@@ -673,6 +702,18 @@ int launch_dot64(const double* a, const double* b, long long n, double* acc, cud
     return ST_OK;
 }
 
+__global__ void sqrt_kernel(const float* __restrict__ a, float* __restrict__ out, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = sqrtf(a[i]);
+}
+
+int launch_sqrt(const float* a, float* out, long long n, cudaStream_t st) {
+    sqrt_kernel<<<blocks_for(n), 256, 0, st>>>(a, out, n);
+    count_launch();
+    ST_CUDA(cudaGetLastError());
+    return ST_OK;
+}
+
 int launch_residual(float* out, const float* b, const float* Ax, long long n, cudaStream_t st) {
     axpby_kernel<<<blocks_for(n), 256, 0, st>>>(out, b, Ax, 1.0f, n);
     count_launch();
@@ -696,10 +737,18 @@ int run_cg(const CgProblem& P, CgWork& W, int max_iter, double tol, int check_ev
     const long long n = P.n;
     ST_CUDA(cudaMemsetAsync(W.sc, 0, sizeof(CgScalars), st));
     // iteration -1 stores rz in acc[2].rzn
-    cg_init_kernel<<<cg_blocks(n), 256, 0, st>>>(P.b, P.dinv, n, P.x, W.r, P.dinv ? W.z : nullptr, W.p,
-                                                   W.sc->acc[2].rzn, W.sc->bb);
+    // (stencil: p and <r, z> from the preconditioner kernel below)
+    cg_init_kernel<<<cg_blocks(n), 256, 0, st>>>(P.b, P.sq ? nullptr : P.dinv, n, P.x, W.r,
+                                                   P.dinv && !P.sq ? W.z : nullptr, W.p,
+                                                   P.sq ? nullptr : W.sc->acc[2].rzn, W.sc->bb);
     count_launch();
     ST_CUDA(cudaGetLastError());
+    if (P.sq) {
+        stencil_prec_kernel<<<cg_blocks(n), 256, 0, st>>>(n, W.r, P.dinv, P.sq, P.gx, P.gy, P.gz, P.w[0], P.w[1],
+                                                           P.w[2], W.z, W.p, W.sc->acc[2].rzn, nullptr);
+        count_launch();
+        ST_CUDA(cudaGetLastError());
+    }
     CgScalars h{};
     ST_CUDA(cudaMemcpyAsync(&h, W.sc, sizeof(h), cudaMemcpyDeviceToHost, st));
     ST_CUDA(cudaStreamSynchronize(st));
@@ -717,7 +766,7 @@ int resume_cg(const CgProblem& P, CgWork& W, int max_iter, double tol, int check
     // run that update (a zero tolerance never stops it)
     const int k = res->iters;
     ST_CUDA(cudaMemsetAsync(&W.sc->done, 0, sizeof(int), st));
-    cg_pupdate_kernel<<<cg_blocks(P.n), 256, 0, st>>>(P.n, W.p, P.dinv ? W.z : W.r, W.sc, k - 1, 0.0);
+    cg_pupdate_kernel<<<cg_blocks(P.n), 256, 0, st>>>(P.n, W.p, P.dinv || P.sq ? W.z : W.r, W.sc, k - 1, 0.0);
     count_launch();
     ST_CUDA(cudaGetLastError());
     return cg_loop(P, W, k, max_iter, tol, check_every, res, st);
@@ -740,9 +789,15 @@ int cg_loop(const CgProblem& P, CgWork& W, int k0, int max_iter, double tol, int
             } else {
                 ST_TRY(launch_spmv(*P.A, W.p, W.q, nullptr, 0.0f, W.p, W.sc->acc[k % 3].pq, &W.sc->done, st));
             }
-            cg_update_kernel<<<cg_blocks(n), 256, 0, st>>>(n, P.x, W.r, P.dinv ? W.z : nullptr, W.p, W.q, P.dinv,
-                                                             W.sc, k);
+            cg_update_kernel<<<cg_blocks(n), 256, 0, st>>>(n, P.x, W.r, P.dinv && !P.sq ? W.z : nullptr, W.p,
+                                                             W.q, P.sq ? nullptr : P.dinv, W.sc, k, P.sq != nullptr);
             count_launch();
+            if (P.sq) {
+                stencil_prec_kernel<<<cg_blocks(n), 256, 0, st>>>(n, W.r, P.dinv, P.sq, P.gx, P.gy, P.gz, P.w[0],
+                                                                   P.w[1], P.w[2], W.z, nullptr,
+                                                                   W.sc->acc[k % 3].rzn, &W.sc->done);
+                count_launch();
+            }
             cg_pupdate_kernel<<<cg_blocks(n), 256, 0, st>>>(n, W.p, zp, W.sc, k, tol);
             count_launch();
             ST_CUDA(cudaGetLastError());

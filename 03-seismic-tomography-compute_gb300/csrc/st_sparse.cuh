@@ -86,6 +86,12 @@ struct CgProblem {
     const float* b = nullptr;
     float* x = nullptr;
     const float* dinv = nullptr;
+    // stencil preconditioner M r = dinv r + S K (S r) (S = sqrt(dinv), K the
+    // weighted Dirichlet Laplacian of an nx x ny x nz grid, x slowest) when
+    // sq is set; dinv must be set too
+    const float* sq = nullptr;
+    int gx = 0, gy = 0, gz = 0;
+    float w[3] = {0.0f, 0.0f, 0.0f};
 };
 
 struct CgWork {
@@ -120,6 +126,7 @@ int launch_scale(float* v, long long n, float a, cudaStream_t st);
 int launch_add_diag(DevCsr& A, float a, cudaStream_t st);
 int launch_sumsq(const float* v, long long n, double* acc, cudaStream_t st);
 int launch_residual(float* out, const float* b, const float* Ax, long long n, cudaStream_t st);
+int launch_sqrt(const float* a, float* out, long long n, cudaStream_t st);
 int launch_dot64(const double* a, const double* b, long long n, double* acc, cudaStream_t st);
 int launch_fd_triplets(const double* vel, long long nx, long long ny, long long nz, double idx2, double idy2,
                        double idz2, double dt2, long long* tr, long long* tc, double* tv, cudaStream_t st);

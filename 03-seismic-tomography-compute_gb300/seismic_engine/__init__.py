@@ -12,7 +12,7 @@ from .wave import (  # noqa: F401
     WaveField, field_layout, rtm_shot, rtm_shot_checkpointed, rtm_shot_host, shot_adjoint, shot_forward,
     shot_forward_host,
 )
-from .sparse import CSRMatrix, SparseOps, compute_fd_stencil, normal_cg_device  # noqa: F401
+from .sparse import CSRMatrix, SparseOps, compute_fd_stencil, normal_cg_device, normal_pcg_stencil_device  # noqa: F401
 from .fields import check_field_health, clamp_field_safe, repair_field_nan  # noqa: F401
 from .config import (  # noqa: F401
     InversionConfig, ModelConfig, TomographyConfig, load_config,

@@ -257,6 +257,8 @@ SIGNATURES = {
     "st_cg_device_static": [_vp, _vp, _vp, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int), _d],
     "st_normal_cg_device": [_vp, _vp, C.c_double, C.c_int, C.c_double, C.c_int, _vp, _vp, C.POINTER(C.c_int), _d,
                             _d],
+    "st_normal_pcg_stencil_device": [_vp, _vp, C.c_double, _f, C.c_int64, C.c_int64, C.c_int64, C.c_int, C.c_double,
+                                     C.c_int, _vp, _vp, C.POINTER(C.c_int), _d, _d],
     "st_dot": [_d, _d, C.c_int64, C.c_int, _d],
     "st_smooth_gradient": [_d, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_int, _d],
     "st_smooth_gradient_device": [_vp, C.c_int64, C.c_int64, C.c_int64, C.c_double, _vp, _vp, _vp],

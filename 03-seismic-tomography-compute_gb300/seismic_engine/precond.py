@@ -373,3 +373,53 @@ def train_on_ray_systems(n: int = 32, n_rays: int = 60000, seeds=range(1000, 106
     stats = {"systems": len(list(seeds)), "pairs": len(samples), "grid": n, "rays": n_rays, "layers": layers,
              "steps": steps, "data_s": t_data, "train_s": t_train, "loss_jacobi": base, "loss_trained": final}
     return net, stats
+
+
+def fit_stencil_weights(n: int = 50, n_rays: int = 500_000, seeds=(2001,), lam: float = 1e-2, tol: float = 1e-6,
+                        max_iter: int = 20000, common=(0.05, 0.1, 0.2, 0.3, 0.5, 0.8, 1.2), factors=(0.6, 1.6),
+                        sweeps: int = 2):
+    """Fits the three axis weights w of the stencil preconditioner
+    M r = D r + S K_w (S r) (st_normal_pcg_stencil_device, the symmetric form
+    D + S G^T G S with G the weighted axis differences) on training systems:
+    the weights that minimise the mean PCG iteration count to `tol` over
+    seeded ray systems (`ray_system`, other seeds than the system the weights
+    are used on). A search over one common weight, then per-axis coordinate
+    descent over the given factors. Returns (w, stats)."""
+    import time
+    from .sparse import normal_cg_device, normal_pcg_stencil_device
+    t0 = time.perf_counter()
+    systems = [ray_system(n, n_rays, s, lam) for s in seeds]
+    evals = 0
+
+    def iters(w):
+        nonlocal evals
+        tot = 0
+        for A, d in systems:
+            x = torch.zeros(n ** 3, device="cuda")
+            if w is None:
+                it, _, _ = normal_cg_device(A, d, lam, x, max_iter, tol, True)
+            else:
+                it, _, _ = normal_pcg_stencil_device(A, d, lam, w, (n, n, n), x, max_iter, tol)
+            tot += it
+        evals += 1
+        return tot / len(systems)
+
+    base = iters(None)
+    best_w, best = (0.0, 0.0, 0.0), base
+    for a in common:
+        c = iters((a, a, a))
+        if c < best:
+            best_w, best = (a, a, a), c
+    for _ in range(sweeps):
+        for axis in range(3):
+            for f in factors:
+                w = list(best_w)
+                w[axis] *= f
+                c = iters(tuple(w))
+                if c < best:
+                    best_w, best = tuple(w), c
+    for A, _ in systems:
+        A.close()
+    stats = {"systems": len(systems), "grid": n, "rays": n_rays, "jacobi_iterations": base,
+             "fitted_iterations": best, "evaluations": evals, "fit_s": time.perf_counter() - t0}
+    return best_w, stats

@@ -231,6 +231,24 @@ def compute_fd_stencil(nx, ny, nz, velocity, dx, dy, dz, dt) -> CSRMatrix:
     return CSRMatrix().build_fd_stencil_7point(nx, ny, nz, velocity, dx, dy, dz, dt)
 
 
+def normal_pcg_stencil_device(A: CSRMatrix, d, lam: float, w, grid, x, max_iter: int = 1000, tol: float = 1e-6,
+                              rhs=None, confirm_true: bool = False):
+    """(A^T A + lam I) x = A^T d preconditioned by M r = D r + S K (S r)
+    (st_normal_pcg_stencil_device: D Jacobi, S = sqrt(D), K the three-axis
+    weighted Dirichlet Laplacian of the (nx, ny, nz) cell grid with weights
+    w >= 0); returns (iterations, recurrence relative residual, true relative
+    residual)."""
+    it = C.c_int()
+    rel = C.c_double()
+    true_rel = C.c_double()
+    wa = (C.c_float * 3)(*[float(v) for v in w])
+    nx, ny, nz = (int(v) for v in grid)
+    call("st_normal_pcg_stencil_device", A.handle, d.data_ptr() if d is not None else None, float(lam), wa, nx, ny, nz,
+         int(max_iter), float(tol), _lib.ST_CG_CONFIRM_TRUE if confirm_true else 0, x.data_ptr(),
+         rhs.data_ptr() if rhs is not None else None, C.byref(it), C.byref(rel), C.byref(true_rel))
+    return it.value, rel.value, true_rel.value
+
+
 def normal_cg_device(A: CSRMatrix, d, lam: float, x, max_iter: int = 1000, tol: float = 1e-6,
                      jacobi: bool = True, rhs=None, confirm_true: bool = False):
     """(A^T A + lam I) x = A^T d on torch CUDA float32 tensors; returns

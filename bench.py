@@ -356,6 +356,18 @@ def run_tomography(args):
     t_cg = time.perf_counter() - t0
     out["jacobi_cg"] = {"iterations": it, "seconds": t_cg, "ms_per_iteration": 1e3 * t_cg / max(it, 1),
                         "true_rel": true_rel}
+    # the fitted stencil preconditioner: weights learned on another seeded system of the same ray
+    # density (50^3 cells, 500k rays), then applied here
+    w_st, st_stats = pc.fit_stencil_weights()
+    x = torch.zeros(n ** 3, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    it_s, rel_s, true_s = se.normal_pcg_stencil_device(A, d, tp.lam, w_st, (n, n, n), x, 20000, 1e-6, confirm_true=True)
+    torch.cuda.synchronize()
+    t_s = time.perf_counter() - t0
+    out["stencil_pcg"] = {"iterations": it_s, "seconds": t_s, "ms_per_iteration": 1e3 * t_s / max(it_s, 1),
+                          "true_rel": true_s, "time_ratio_vs_jacobi_cg": t_s / t_cg, "weights": list(w_st),
+                          "fit": st_stats}
     if not args.no_learned:
         net, stats = pc.train_on_ray_systems(n=32, n_rays=60000, seeds=range(1000, 1064), lam=tp.lam)
         big = pc.LearnedPreconditioner(n, n, n, layers=net.layers)

@@ -757,6 +757,16 @@ enum { ST_CG_JACOBI = 1, ST_CG_CONFIRM_TRUE = 2 };
  * of the last iteration. */
 int st_normal_cg_device(st_csr* A, const float* d, double lam, int max_iter, double tol, int jacobi, float* x,
                         float* rhs, int* iters, double* final_rel, double* true_rel);
+/* The same solve preconditioned by M r = D r + S K (S r) (no reference
+ * counterpart): D the Jacobi diagonal above, S = sqrt(D), K = sum over the
+ * three axes of w[a] times the 1-D Dirichlet second difference on the
+ * nx x ny x nz cell grid of A's columns (x slowest), w[a] >= 0 (host array):
+ * symmetric positive definite, a 7-point stencil per application. The
+ * weights are fitted on training systems (seismic_engine.precond.
+ * fit_stencil_weights). flags: ST_CG_CONFIRM_TRUE as above (Jacobi implied). */
+int st_normal_pcg_stencil_device(st_csr* A, const float* d, double lam, const float* w, int64_t nx, int64_t ny,
+                                 int64_t nz, int max_iter, double tol, int flags, float* x, float* rhs, int* iters,
+                                 double* final_rel, double* true_rel);
 /* Replaces dot_product (sparse_ops.cpp:172-187): FP64 inner product. */
 int st_dot(const double* a, const double* b, int64_t n, int device, double* out);
 /* Replaces smooth_gradient (sparse_ops.cpp:115-158): truncated Gaussian of
