@@ -71,7 +71,7 @@ def parse():
     ap.add_argument("--segment", type=int, default=200, help="checkpoint segment length of --workload large")
     ap.add_argument("--compare", action="store_true",
                     help="--workload large: also time FP32 segment snapshots and unpreconditioned CG")
-    ap.add_argument("--kernel", choices=["conv", "wgrad", "spmv", "rays"], default=None,
+    ap.add_argument("--kernel", choices=["conv", "wgrad", "fwigrad", "spmv", "rays"], default=None,
                     help="time one kernel alone (profiling runs) instead of the workload")
     ap.add_argument("--no-tomo", action="store_true", help="skip the tomography CG measurement")
     ap.add_argument("--tomo-n", type=int, default=100, help="cell grid edge of the --kernel spmv matrix")
@@ -694,7 +694,8 @@ def large_iteration(args):
 def run_kernel(args):
     """Single-kernel timing for profiling: 'conv' = the tensor-core 3x3x3
     32 -> 32 convolution on a 100^3 volume; 'wgrad' = its tensor-core weight
-    gradient on the same volume; 'spmv' = A x and A^T y of the
+    gradient on the same volume; 'fwigrad' = one shot's FWI gradient on the 256^3
+    workload (--nt steps, 400 by default); 'spmv' = A x and A^T y of the
     100^3 / 2M-ray tomography matrix; 'rays' = the sampled-ray forward model
     and gradient of 2M picks. Prints one JSON line."""
     import ctypes as C
@@ -737,6 +738,25 @@ def run_kernel(args):
         flops = 2.0 * (n + 2) ** 3 * 32 * 32 * 27
         res.update({"workload": f"3x3x3 conv weight gradient, 32 -> 32 channels, BF16 operands, {n}^3 voxels",
                     "flops": flops})
+    elif args.kernel == "fwigrad":
+        import seismic_engine.fwi as fwi
+        nt_ = args.nt if args.nt != 2000 else 400
+        w = se.workloads.rtm_256(nt=nt_)
+        cfg = se.SolverConfig(dt=w.dt, nt=nt_, sponge_width=w.sponge_width, sponge_damping=w.sponge_damping,
+                              sponge_mode=w.sponge_mode)
+        s = se.WaveEquationSolver(se.GridParams(w.nx, w.ny, w.nz, w.d, w.d, w.d), cfg)
+        fwi.set_velocity_device(s, torch.from_numpy(w.vel.astype(np.float32)).cuda())
+        sh = w.shots[0]
+        d_obs = torch.zeros((nt_, sh.rec.count), device="cuda")
+        se.shot_forward(s, sh.src, sh.wavelet, nt_, sh.rec, seis=d_obs)
+        d_obs *= 1.01
+        gv = torch.zeros(w.points, device="cuda")
+        st = torch.cuda.ExternalStream(s.stream_ptr())
+
+        def one():
+            fwi.fwi_gradient(s, sh.src, sh.wavelet, nt_, sh.rec, d_obs, gv, snap_kind=_lib.ST_SNAP_BF16)
+        res.update({"workload": f"FWI gradient of one shot, {w.name}, {nt_} steps, BF16 snapshots (forward + "
+                                f"adjoint with the gradient epilogue)", "steps_per_call": nt_})
     elif args.kernel == "rays":
         ps = se.workloads.obs_picks()
         rays = se.SampledRays(ps.model, ps.src_xyz, ps.sta_xyz, ps.weight)
@@ -801,6 +821,8 @@ def run_kernel(args):
         res["tflops"] = res["flops"] / ms / 1e9
     if "alg_bytes" in res:
         res["gbs"] = res["alg_bytes"] / ms / 1e6
+    if "steps_per_call" in res:
+        res["ms_per_step"] = ms / res["steps_per_call"]
     if args.kernel == "conv":
         assert L.st_conv3d_check(C.c_void_p(st.cuda_stream)) == 0
     print(json.dumps(res), flush=True)
