@@ -712,11 +712,12 @@ int st_cg_device(st_csr* A, const float* b, float* x, int max_iter, double tol, 
  * ST_CG_STATIC_MAX_N floats, 20 MiB) is one file-scope device array that
  * every GPU loading this library keeps until the process exits.
  *  - Systems larger than ST_CG_STATIC_MAX_N unknowns are refused (ST_ERR_ARG).
- *  - The first call on a device looks up the array's device address; make
- *    that first call before any stream capture on that device. The address
- *    is kept for the life of the process: a cudaDeviceReset (or any other
- *    teardown of the device's primary context) makes it stale, as it does
- *    every handle of this library.
+ *  - The call is synchronous (it reads the solver's scalars on the host
+ *    every 16 iterations), so it cannot be captured in a CUDA graph. The
+ *    first call on a device looks up the array's device address, kept for
+ *    the life of the process: a cudaDeviceReset (or any other teardown of the
+ *    device's primary context) makes it stale, as it does every handle of
+ *    this library.
  *  - All calls on a device share the array, so calls that overlap on the GPU
  *    (other host threads, other streams) race; serialise them. The array keeps
  *    the last call's contents; the solver re-initialises everything it reads. */
