@@ -583,6 +583,38 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
         // failed wait (or another warp's abort) a warp stops waiting and
         // working but still takes every barrier.
         const int tt = threadIdx.x - 64, tw = warp - 2;
+        // this lane's row of each of the warp's ten groups of four 8 x 8 blocks
+        // (groups tw, tw + 4, ...; A: 4 taps x 8 row blocks x 4 channel blocks,
+        // B: 8 x 4): source offset in a raw stage, destination offset in an
+        // operand stage. The raw tiles arrive 64-byte swizzled (16-byte chunk c
+        // of row v at chunk c ^ ((v >> 1) & 3)), so the eight rows an ldmatrix
+        // reads fall in eight different bank groups.
+        constexpr uint32_t SKIP = 0xffffffffu;
+        uint32_t so[10], dof[10];
+        {
+            const int r = lane & 7;
+#pragma unroll
+            for (int j = 0; j < 10; ++j) {
+                const int b = (tw + 4 * j) * 4 + (lane >> 3);
+                int t, vb, cb;
+                uint32_t dst;
+                if (b < 128) {
+                    t = b >> 5;
+                    vb = (b & 31) >> 2;
+                    cb = b & 3;
+                    dst = (uint32_t)(vb * 2048 + (t * 4 + cb) * 128 + r * 16);
+                } else {
+                    t = 4;
+                    vb = (b - 128) >> 2;
+                    cb = (b - 128) & 3;
+                    dst = (uint32_t)(WG_A_BYTES + vb * 512 + cb * 128 + r * 16);
+                }
+                const int row = vb * 8 + r;
+                so[j] = (b < 128 && t >= ntap) ? SKIP  // uniform over the group (32 blocks per tap)
+                                               : (uint32_t)(t * WG_RAW_TILE + row * (CH * 2) + ((cb ^ ((row >> 1) & 3)) << 4));
+                dof[j] = dst;
+            }
+        }
         bool ok = true;
         for (int k = 0; k < nk; ++k) {
             const int s = k % WG_NRAW, o = k % WG_NOP;
@@ -611,25 +643,15 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
             }
             named_sync_128();
             if (!ok) continue;
-            // 160 blocks of 8 x 8 (A: 4 taps x 8 row blocks x 4 channel blocks; B: 8 x 4),
-            // four per ldmatrix / stmatrix pair; lane l addresses row l % 8 of block l / 8
-            const int r = lane & 7;
-            for (int i = tw; i < 40; i += 4) {
-                const int b = i * 4 + (lane >> 3);
-                uint32_t src, dst;
-                if (b < 128) {
-                    const int t = b >> 5, rem = b & 31, vb = rem >> 2, cb = rem & 3;
-                    if (t >= ntap) continue;  // uniform over the group (32 blocks per tap)
-                    src = smem_u32(rb + t * WG_RAW_TILE + (vb * 8 + r) * (CH * 2) + cb * 16);
-                    dst = smem_u32(ob + vb * 2048 + (t * 4 + cb) * 128 + r * 16);
-                } else {
-                    const int bb = b - 128, vb = bb >> 2, cb = bb & 3;
-                    src = smem_u32(rb + 4 * WG_RAW_TILE + (vb * 8 + r) * (CH * 2) + cb * 16);
-                    dst = smem_u32(ob + WG_A_BYTES + vb * 512 + cb * 128 + r * 16);
-                }
+            // four 8 x 8 blocks per ldmatrix / stmatrix pair; lane l addresses row
+            // l % 8 of block l / 8 of the group
+            const uint32_t rbu = smem_u32(rb), obu = smem_u32(ob);
+#pragma unroll
+            for (int j = 0; j < 10; ++j) {
+                if (so[j] == SKIP) continue;
                 uint32_t v4[4];
-                ldsm_x4_trans(src, v4);
-                stsm_x4(dst, v4);
+                ldsm_x4_trans(rbu + so[j], v4);
+                stsm_x4(obu + dof[j], v4);
             }
             // generic-proxy writes read by the tensor cores, and a raw stage the
             // TMA overwrites next
@@ -663,7 +685,8 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
     }
 }
 
-// The padded volume viewed as [rows][32 channels], box {32 channels, 64 rows}.
+// The padded volume viewed as [rows][32 channels], box {32 channels, 64 rows},
+// 64-byte swizzled in shared memory.
 int make_wgrad_map(CUtensorMap* map, const __nv_bfloat16* base, long long rows) {
     EncodeTiledFn enc = nullptr;
     ST_TRY(get_encode_tiled(&enc));
@@ -672,7 +695,7 @@ int make_wgrad_map(CUtensorMap* map, const __nv_bfloat16* base, long long rows) 
     cuuint32_t box[2] = {CH, WG_KSTEP};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(base), dims, strides, box,
-                     estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     ST_CHECK(r == CUDA_SUCCESS, ST_ERR_CUDA, "cuTensorMapEncodeTiled (wgrad) failed (%d)", (int)r);
     return ST_OK;
