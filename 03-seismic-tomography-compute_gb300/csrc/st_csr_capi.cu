@@ -477,10 +477,10 @@ static int normal_cg_impl(st_csr* m, const float* d, double lam, int max_iter, d
     // scaled by their ratio, a few times at most.
     double tr = 0.0;
     if (confirm || true_rel) ST_TRY(residual(&tr));
-    for (int round = 0; confirm && round < 4 && tr > tol && !R.breakdown && R.iters > 0 && R.iters < max_iter &&
+    for (int round = 0; confirm && round < 10 && tr > tol && !R.breakdown && R.iters > 0 && R.iters < max_iter &&
                         R.rel < tol;
          ++round) {
-        const double target = R.rel * (tol / tr) * 0.98;
+        const double target = R.rel * (tol / tr) * 0.995;
         ST_TRY(resume_cg(P, W, max_iter, target, 16, &R, m->stream));
         ST_TRY(residual(&tr));
     }

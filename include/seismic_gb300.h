@@ -754,7 +754,7 @@ enum { ST_CG_JACOBI = 1, ST_CG_CONFIRM_TRUE = 2 };
  * ||rhs||. The solve stops when the recurrence residual falls below tol; with
  * jacobi & ST_CG_CONFIRM_TRUE the stop is confirmed on the true residual:
  * while that is above tol, the iteration continues to a tighter recurrence
- * target (at most four times, within max_iter). iters and final_rel are those
+ * target (at most ten times, within max_iter). iters and final_rel are those
  * of the last iteration. */
 int st_normal_cg_device(st_csr* A, const float* d, double lam, int max_iter, double tol, int jacobi, float* x,
                         float* rhs, int* iters, double* final_rel, double* true_rel);
