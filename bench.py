@@ -304,9 +304,11 @@ def run_reference(args):
 def run_tomography(args):
     """Traveltime tomography on 100^3 cells with 2M straight rays: the ray
     matrix build, SpMV / SpMV^T bandwidth, and time to a 1e-6 true relative
-    residual of (A^T A + 1e-2 I) x = A^T b for the plain Jacobi-CG and for
-    the flexible CG with the learned preconditioner (trained first on 64
-    smaller seeded systems; training time reported separately)."""
+    residual of (A^T A + 1e-2 I) x = A^T b for the Jacobi-CG, for plain CG
+    (no preconditioner), for the PCG with the fitted stencil preconditioner
+    and for the flexible CG with the learned preconditioner (trained first on
+    64 smaller seeded systems; training and fitting times reported
+    separately)."""
     import torch
     import seismic_engine as se
     from seismic_engine import precond as pc
@@ -356,6 +358,16 @@ def run_tomography(args):
     t_cg = time.perf_counter() - t0
     out["jacobi_cg"] = {"iterations": it, "seconds": t_cg, "ms_per_iteration": 1e3 * t_cg / max(it, 1),
                         "true_rel": true_rel}
+    # plain CG (no preconditioner, sparse_ops.cpp:8-50 on the normal equations): the baseline the
+    # learned preconditioner's time target is stated against
+    x = torch.zeros(n ** 3, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    it_p, rel_p, true_p = se.normal_cg_device(A, d, tp.lam, x, 20000, 1e-6, False, confirm_true=True)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    out["plain_cg"] = {"iterations": it_p, "seconds": t_plain, "ms_per_iteration": 1e3 * t_plain / max(it_p, 1),
+                       "true_rel": true_p}
     # the fitted stencil preconditioner: weights learned on another seeded system of the same ray
     # density (50^3 cells, 500k rays), then applied here
     w_st, st_stats = pc.fit_stencil_weights()
@@ -366,7 +378,8 @@ def run_tomography(args):
     torch.cuda.synchronize()
     t_s = time.perf_counter() - t0
     out["stencil_pcg"] = {"iterations": it_s, "seconds": t_s, "ms_per_iteration": 1e3 * t_s / max(it_s, 1),
-                          "true_rel": true_s, "time_ratio_vs_jacobi_cg": t_s / t_cg, "weights": list(w_st),
+                          "true_rel": true_s, "time_ratio_vs_jacobi_cg": t_s / t_cg,
+                          "time_ratio_vs_plain_cg": t_s / t_plain, "weights": list(w_st),
                           "fit": st_stats}
     if not args.no_learned:
         net, stats = pc.train_on_ray_systems(n=32, n_rays=60000, seeds=range(1000, 1064), lam=tp.lam)
@@ -383,7 +396,8 @@ def run_tomography(args):
         torch.cuda.synchronize()
         t_l = time.perf_counter() - t0
         out["learned_fcg"] = {"iterations": it_l, "seconds": t_l, "ms_per_iteration": 1e3 * t_l / max(it_l, 1),
-                              "true_rel": rel_l, "time_ratio_vs_jacobi_cg": t_l / t_cg, "training": stats}
+                              "true_rel": rel_l, "time_ratio_vs_jacobi_cg": t_l / t_cg,
+                              "time_ratio_vs_plain_cg": t_l / t_plain, "training": stats}
         native.close()
     A.close()
     return out
